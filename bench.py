@@ -1,0 +1,407 @@
+#!/usr/bin/env python
+"""Throughput of the QG-YBJ+ time step on GB300, in cell-steps/s.
+
+Workload: 512 x 512 x 256 (n1 x n2 x n3), mixed precision (FP32 transforms,
+products and leapfrog update; FP64 tridiagonal inversions), exponential
+stratification, seeded random-phase eddies peaked at k=8 plus a surface wave
+(synthetic inputs; the reference ships no initial-condition files).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N>1 runs one independent replica per GPU (the step shards only by running
+independent ensemble members), with a barrier and the maximum time over
+ranks.  The reference arm times the FP64 CPU restatement of the reference's
+step (the Fortran reference cannot be built here) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "qg-ybjp-model_gb300"
+for _p in (str(ROOT), str(PKG)):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+FALLBACK_HBM_GBS = 6800.0
+# DRAM bytes per launch of the dominant kernel from an ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum); None until captured.
+MEASURED_TRAFFIC = {}
+
+
+# ---------------------------------------------------------------------------
+# distributed helpers (replicas: no collective on the data path)
+# ---------------------------------------------------------------------------
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def dist_setup(world: int, backend: str):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def reduce_max(dist, x: float, device=None) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_value(world: int, cells: int, steps: int, max_seconds: float) -> float:
+    """Cell-steps/s of all replicas together (weak scaling)."""
+    return world * cells * steps / max_seconds
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.lines: list[str] = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "100", "-i", str(self.gpu)],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        time.sleep(0.15)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=5)
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# algorithmic bytes
+# ---------------------------------------------------------------------------
+def algorithmic_bytes(n: int, n3: int, zb: int, precision: str) -> dict:
+    """Compulsory bytes per launch of each kernel class.
+
+    State fields count the retained modes (the 2/3 disk, L=1) once per read
+    or write; (kx,y) scratch planes count n*(K+1) complex values.  s = bytes
+    per complex value (8 mixed, 16 FP64)."""
+    from qgybj.config import dealias_mask, kmax
+    s = 8 if precision == "mixed" else 16
+    retained = int(dealias_mask(n).sum())
+    K = kmax(n)
+    fld = retained * s              # one state field, one level
+    pln = n * (K + 1) * s           # one scratch plane, one level
+    return {
+        "col_inv": zb * (4 * fld + 6 * pln),
+        "row_main": zb * (6 * pln + 6 * pln),
+        "col_update": zb * (6 * pln + 14 * fld + 4 * pln),
+        "row_qw": zb * (4 * pln + 2 * pln),
+        "col_qw": zb * (2 * pln + 2 * fld),
+        "solve": n3 * 6 * fld,
+        "dissipation": n3 * 2 * fld,
+        "step": 22 * fld * n3,
+        "step_dense": 22 * (n // 2 + 1) * n * n3 * s,
+    }
+
+
+# ---------------------------------------------------------------------------
+def run_ours(args, world, rank, local):
+    import numpy as np
+    import torch
+
+    import qgybj
+    from qgybj.config import CONFIGS, make_initial_condition, model_parameters
+
+    dist = dist_setup(world, "nccl")
+    torch.cuda.set_device(local)
+    rc = CONFIGS[args.config]
+    precision = args.precision or rc.precision
+    ic = make_initial_condition(rc)
+    params = model_parameters(rc, ic.delt)
+    sim = qgybj.Simulation(params, precision, device=local)
+    sim.set_state("psi", ic.psi)
+    sim.set_state("BR", ic.BR)
+    sim.set_state("BI", ic.BI)
+    sim.init_state(True, True)
+    n, n3 = rc.n, rc.n3
+    cells = n * n * n3
+    # warm-up (the first step is the forward Euler start)
+    sim.steps_async(args.warmup, True)
+    sim.synchronize()
+    # per-kernel device times of one step (events around each launch)
+    prof = sim.profile_step(False)
+    launches_per_step = sum(c for _, c in prof.values())
+    # timed region
+    stream = torch.cuda.ExternalStream(sim.stream(), device=torch.device("cuda", local))
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(local)
+    barrier(dist)
+    torch.cuda.synchronize()
+    sim.synchronize()
+    clocks.start()
+    time.sleep(0.25)
+    e0.record(stream)
+    sim.steps_async(args.steps, False)
+    e1.record(stream)
+    sim.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier(dist)
+    ms = e0.elapsed_time(e1)
+    ms_max = reduce_max(dist, ms, device=torch.device("cuda", local))
+    value = whole_job_value(world, cells, args.steps, ms_max / 1e3)
+    st = sim.diagnostics_fp64()
+    finite = all(math.isfinite(v) for v in st.values())
+
+    # end to end through the C-ABI with host buffers: upload the state from
+    # pinned host memory, K synchronous qg_step calls each followed by the
+    # FP64 diagnostics read back, download psi, BR, BI.
+    e2e = None
+    if not args.no_e2e:
+        shape = (n3, n, n // 2 + 1)
+        names_in = ("q", "qo", "BR", "BI", "BRo", "BIo", "psi", "AR", "AI")
+        host_in = {}
+        for f in names_in:
+            t = torch.empty(shape, dtype=torch.complex128, pin_memory=True)
+            sim.get_state(f, out=t.numpy())
+            host_in[f] = t
+        host_out = {f: torch.empty(shape, dtype=torch.complex128, pin_memory=True) for f in ("psi", "BR", "BI")}
+        k_e2e = args.e2e_steps or args.steps
+        barrier(dist)
+        t0 = time.perf_counter()
+        for f in names_in:
+            sim.set_state(f, host_in[f])
+        for _ in range(k_e2e):
+            sim.step(False)
+            sim.diagnostics_fp64()
+        for f, t in host_out.items():
+            sim.get_state(f, out=t.numpy())
+        t1 = time.perf_counter()
+        e2e_s = reduce_max(dist, t1 - t0, device=torch.device("cuda", local))
+        fbytes = int(np.prod(shape)) * 16
+        e2e = {"value": whole_job_value(world, cells, k_e2e, e2e_s), "unit": "cell-steps/s",
+               "h2d_bytes_per_step": len(names_in) * fbytes / k_e2e,
+               "d2h_bytes_per_step": (3 * fbytes + 7 * 8 * k_e2e) / k_e2e,
+               "steps": k_e2e, "seconds": e2e_s,
+               "path": "qg_set_state x9 (pinned host) + K x (qg_step + qg_diagnostics_fp64) + qg_get_state x3"}
+
+    # FP64 GPU step on the same workload (the metric compares the two)
+    fp64 = None
+    if not args.no_fp64 and precision == "mixed":
+        sim64 = qgybj.Simulation(params, "fp64", device=local)
+        sim64.set_state("psi", ic.psi); sim64.set_state("BR", ic.BR); sim64.set_state("BI", ic.BI)
+        sim64.init_state(True, True)
+        sim64.steps_async(2, True)
+        sim64.synchronize()
+        s64 = torch.cuda.ExternalStream(sim64.stream(), device=torch.device("cuda", local))
+        k64 = max(2, min(args.steps, args.fp64_steps))
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(s64)
+        sim64.steps_async(k64, False)
+        a1.record(s64)
+        sim64.synchronize()
+        ms64 = a0.elapsed_time(a1)
+        fp64 = {"value": cells * k64 / (ms64 / 1e3), "ms_per_step": ms64 / k64, "steps": k64}
+        sim64.close()
+
+    out = None
+    if rank == 0:
+        peak, peak_kind = measured_peak_hbm()
+        ab = algorithmic_bytes(n, n3, sim_batch(sim), precision)
+        dom = max((k for k in prof if prof[k][1] > 0), key=lambda k: prof[k][0])
+        dom_ms = prof[dom][0] / prof[dom][1]
+        achieved = ab[dom] / (dom_ms / 1e3) / 1e9
+        step_ms = ms / args.steps
+        out = {
+            "metric": "cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if precision == "mixed" else "f64", "data": "synthetic (seeded)",
+            "config": {"workload": rc.name, "n1": n, "n2": n, "n3": n3, "precision": precision,
+                       "solves_dtype": "f64", "stratification": rc.stratification, "k0": rc.k0, "seed": rc.seed,
+                       "parallelism": f"replicas{world}",
+                       "l2": "inputs larger than L2: resident state ~%.1f GB per step" % (ab["step"] / 1e9)},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                         "algorithmic_bytes_per_launch": ab[dom], "ms_per_launch": dom_ms,
+                         "traffic": MEASURED_TRAFFIC.get((dom, rc.name, precision))},
+            "step_roofline": {"bytes_per_step": ab["step"], "achieved": ab["step"] / (step_ms / 1e3) / 1e9,
+                              "frac": ab["step"] / (step_ms / 1e3) / 1e9 / peak, "unit": "GB/s",
+                              "bytes_per_step_dense_layout": ab["step_dense"],
+                              "frac_dense_layout": ab["step_dense"] / (step_ms / 1e3) / 1e9 / peak},
+            "kernels_ms_per_step": {k: v[0] for k, v in prof.items() if v[1]},
+            "launches_per_step": {k: v[1] for k, v in prof.items() if v[1]},
+            "gpu_launches": launches_per_step * args.steps,
+            "clocks": clk, "e2e": e2e, "fp64_gpu": fp64,
+            "mixed_over_fp64": (value / world / fp64["value"]) if fp64 else None,
+            "state_finite": finite,
+        }
+    sim.close()
+    return out
+
+
+def sim_batch(sim) -> int:
+    """Levels per phase-A batch as chosen by the library (same rule)."""
+    from qgybj.config import kmax
+    n, n3 = sim.n, sim.n3
+    kxp = ((kmax(n) + 1 + 7) // 8) * 8
+    per = 6 * n * kxp * (8 if sim.precision == "mixed" else 16)
+    zb = sim.cfg.levels_per_batch or max(1, (48 << 20) // per)
+    zb = min(zb, n3)
+    nb = (n3 + zb - 1) // zb
+    return (n3 + nb - 1) // nb
+
+
+# ---------------------------------------------------------------------------
+def cpu_oracle_rate(rc, nz: int, steps: int, warm: int, workers: int):
+    """Oracle (FP64 numpy/scipy restatement) on a slab of nz levels at the
+    workload's horizontal resolution: cell-steps/s and seconds."""
+    from oracle import qgybj_oracle as orc
+    from qgybj.config import make_initial_condition, model_parameters, scaled
+    orc.set_workers(workers)
+    sub = scaled(rc, rc.n, nz)
+    ic = make_initial_condition(sub)
+    params = model_parameters(sub, ic.delt)
+    keys = ("n1", "n2", "n3", "dz", "Bu", "Ro", "W2F", "delt", "gamma", "nuh1", "nuh2", "ilap1", "ilap2",
+            "nuh1w", "nuh2w", "ilap1w", "ilap2w", "nuz", "a_ell_ut", "r_2ut")
+    model = orc.Model(orc.Params(**{k: params[k] for k in keys}))
+    st = orc.initial_state(model, ic.psi, ic.BR, ic.BI)
+    st = model.step(st, True)
+    for _ in range(warm):
+        st = model.step(st, False)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        st = model.step(st, False)
+    dt = time.perf_counter() - t0
+    return rc.n * rc.n * nz * steps / dt, dt
+
+
+def run_reference(args, world, rank, local):
+    if rank != 0:
+        return None
+    from qgybj.config import CONFIGS
+    rc = CONFIGS[args.config]
+    workers = os.cpu_count() or 1
+    # calibrate the slab depth so that the whole run stays within ~2 minutes
+    rate, _ = cpu_oracle_rate(rc, 2, 1, 0, workers)
+    budget = float(args.reference_budget_s)
+    per_step = budget / max(1, args.steps + args.warmup)
+    nz = int(max(2, min(rc.n3, per_step * rate / (rc.n * rc.n))))
+    value, secs = cpu_oracle_rate(rc, nz, args.steps, args.warmup, workers)
+    sample = (f"oracle (FP64 numpy/scipy restatement of the reference step) on a {rc.n}x{rc.n}x{nz} slab of "
+              f"the {rc.name} workload, {args.steps} leapfrog steps after {args.warmup} warm-up")
+    return {
+        "metric": "cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": rc.name, "n1": rc.n, "n2": rc.n, "n3": rc.n3, "sample_levels": nz},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": workers, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--config", default="c2")
+    ap.add_argument("--precision", default=None)
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--fp64-steps", type=int, default=10)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-baseline-levels", type=int, default=16)
+    ap.add_argument("--reference-budget-s", type=float, default=120.0)
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_env()
+    if args.impl == "reference":
+        out = run_reference(args, world, rank, local)
+    else:
+        out = run_ours(args, world, rank, local)
+        if out is not None and world == 1 and not args.no_cpu_baseline:
+            from qgybj.config import CONFIGS
+            rc = CONFIGS[args.config]
+            workers = os.cpu_count() or 1
+            v, secs = cpu_oracle_rate(rc, args.cpu_baseline_levels, 2, 0, workers)
+            out["cpu_baseline"] = {
+                "value": v, "unit": "cell-steps/s", "cores": workers, "kind": "port",
+                "sample": f"oracle on a {rc.n}x{rc.n}x{args.cpu_baseline_levels} slab of {rc.name}, "
+                          f"2 leapfrog steps ({secs:.1f} s)"}
+    if out is not None:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

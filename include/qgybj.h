@@ -1,0 +1,183 @@
+/*
+ * qgybj.h — C-ABI of the GB300 (sm_103a) QG-YBJ+ time step.
+ *
+ * The Fortran host of the reference (main_waqg.f90, init.f90, IO_ncf.f90 and
+ * a parameters file) binds these entry points through ISO_C_BINDING in place
+ * of the fft.f90 / derivatives.f90 / elliptic.f90 / mpi.f90 routines.  Every
+ * function returns an int status (QG_OK == 0); qg_last_error() gives the text.
+ *
+ * Array conventions (identical in memory to the reference's Fortran arrays):
+ *   spectral "kvar": interleaved complex double [nz][ikty][iktx]
+ *                    == double complex kvar(iktx, ikty, nz), iktx = n1/2+1, ikty = n2
+ *                    ky in FFT order (kya = 0..n2/2-1, 0*, -n2/2+1..-1, init.f90:35-41)
+ *   physical "rvar": double [nz][n2][n1+2] == double precision rvar(n1+2, n2, nz)
+ * Only interior z levels are exchanged (the reference's halo levels are
+ * dropped).  Pointers may be host or device memory; nothing is retained past
+ * a call.  One host thread per handle; calls on a handle are stream-ordered
+ * on the handle's own CUDA stream and synchronous unless stated otherwise.
+ */
+#ifndef QGYBJ_H
+#define QGYBJ_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+enum qg_status {
+  QG_OK = 0,
+  QG_ERR_ARG = 1,          /* bad dimensions, null pointer, unknown field id       */
+  QG_ERR_CUDA = 2,         /* a CUDA runtime call or kernel launch failed          */
+  QG_ERR_NONFINITE = 3,    /* NaN/Inf in an input array                            */
+  QG_ERR_PIVOT = 4,        /* zero or non-dominant pivot in a tridiagonal factor   */
+                           /*   (the DGTSV INFO>0 case, elliptic.f90:192,209)      */
+  QG_ERR_TIMEOUT = 5,      /* a bounded device-side wait expired                   */
+  QG_ERR_UNSUPPORTED = 6,  /* configuration outside what the build implements      */
+  QG_ERR_NOMEM = 7         /* device allocation failed                             */
+};
+
+enum qg_precision {
+  QG_PREC_FP64 = 0,        /* every operation in FP64                               */
+  QG_PREC_MIXED = 1        /* FP32 FFTs/Jacobians/leapfrog; FP64 tridiagonal solves */
+};                         /*   and FP64 diagnostics                                */
+
+/* Field ids for qg_set_state / qg_get_state (main_waqg.f90:15-60). */
+enum qg_field {
+  QG_Q = 0,      /* qk   : QG potential vorticity at n                 */
+  QG_QOLD = 1,   /* qok  : q at n-1 (filtered)                          */
+  QG_BR = 2,     /* BRk  : real part of B = L+A at n                    */
+  QG_BI = 3,     /* BIk                                                 */
+  QG_BROLD = 4,  /* BRok                                                */
+  QG_BIOLD = 5,  /* BIok                                                */
+  QG_PSI = 6,    /* psik : streamfunction                               */
+  QG_AR = 7,     /* ARk  : real part of A                               */
+  QG_AI = 8,     /* AIk                                                 */
+  QG_CR = 9,     /* CRk  : A_z (get only, elliptic.f90:437-450)         */
+  QG_CI = 10,    /* CIk  : (get only)                                   */
+  QG_QSTAR = 11, /* q* = q - q^w of the last step (get only)            */
+  QG_NFIELDS = 12
+};
+
+/* Run configuration: the values of the reference's parameters module that
+ * the step reads (parameters_test1.f90) plus the base state of
+ * init_base_state (init.f90:177-264).  Arrays are copied by qg_create. */
+typedef struct qg_config {
+  int n1, n2, n3;          /* resolution; n1 == n2, a power of two in [16,1024]; n3 >= 2 */
+  int precision;           /* enum qg_precision                                        */
+  int device;              /* CUDA device ordinal                                      */
+  /* physics switches (parameters_test1.f90:22-29) */
+  int ybj_plus, fixed_flow, no_feedback, passive_scalar, linear, no_dispersion, inviscid;
+  double dz;               /* vertical grid spacing (L3/n3)                            */
+  double Bu, Ro, W2F;      /* Burger, Rossby, wave-to-flow velocity ratio squared      */
+  double delt, gamma;      /* time step, Robert-Asselin coefficient                    */
+  double nuh1, nuh2, nuh1w, nuh2w;   /* horizontal hyperdiffusion coefficients        */
+  int ilap1, ilap2, ilap1w, ilap2w;  /* their Laplacian powers                        */
+  double nuz;              /* vertical q diffusion (dissipation_q_nv)                  */
+  const double* a_ell_ut;  /* [n3] Bu/N^2 at za(iz) = iz*dz                            */
+  const double* rho_ut;    /* [n3] or NULL (= 1)                                       */
+  const double* rho_st;    /* [n3] or NULL (= 1)                                       */
+  const double* r_2ut;     /* [n3] N^2 at za(iz), or NULL (= Bu/a_ell_ut); diagnostics */
+  int levels_per_batch;    /* z levels per phase-A batch; 0 = choose automatically     */
+  int use_graphs;          /* 1 = replay the step as a CUDA graph (default), 0 = launch */
+} qg_config;
+
+typedef struct qg_handle qg_handle;
+
+/* FP64 domain integrals (diagnostics.f90:647-743, 16-211, 1262-1363), each a
+ * vertical sum divided by n3, without the dimensional Uw_scale^2 factors. */
+typedef struct qg_energy {
+  double wke;      /* wave kinetic energy  sum_L |B|^2 - 1/2 |B(0,0)|^2          */
+  double wpe;      /* wave potential energy  (0.5/(N^2 Bu)) kh^2 |A_z|^2          */
+  double wce;      /* 1/8 Bu^-2 kh^4 |A|^2                                         */
+  double ke;       /* flow kinetic energy  kh^2 |psi|^2                            */
+  double pe;       /* flow potential energy  (Bu/N^2) |psi_z|^2                    */
+  double zeta2;    /* <zeta_z^2> = 2 sum kh^4 |psi|^2                              */
+  double omegah2;  /* <omega_H^2> = 2 sum kh^2 |psi_z|^2                           */
+} qg_energy;
+
+/* Fills *cfg with the switches of the YBJ+ step (ybj_plus=1, everything else
+ * 0 except inviscid=1), precision MIXED, device 0, graphs on. */
+int qg_config_defaults(qg_config* cfg);
+
+/* Replaces initialize_fftw (fft.f90:32-52) and the tables of init_arrays /
+ * init_base_state (init.f90:17-264): builds the dealiasing mask, integrating
+ * factors, tridiagonal factor tables and device buffers.  QG_ERR_PIVOT when a
+ * tridiagonal factorisation would need a row interchange or hits a zero pivot. */
+int qg_create(const qg_config* cfg, qg_handle** out);
+
+/* Replaces kill_fftw (fft.f90:112-119). */
+int qg_destroy(qg_handle* h);
+
+/* Text of the last error on h (or of the last qg_create failure when h is NULL). */
+const char* qg_last_error(const qg_handle* h);
+
+/* Host <-> device copies of the resident state, levels [level0, level0+nlev).
+ * kvar is [nlev][ikty][iktx] interleaved complex.  Values on modes with L=0
+ * are discarded by qg_set_state (every step of the reference zeroes them). */
+int qg_set_state(qg_handle* h, int field, const double* kvar, int level0, int nlev);
+int qg_get_state(qg_handle* h, int field, double* kvar, int level0, int nlev);
+
+/* Initialisation sequence of main_waqg.f90:129-147 on the resident state:
+ * optional sumB (derivatives.f90:1073-1118), q = init_q(psi) (init.f90:591),
+ * old levels = current levels, and A = A_solver_ybj_plus(B). */
+int qg_init_state(qg_handle* h, int apply_sumB, int q_from_psi);
+
+/* One full time step on the device: main_waqg.f90:202-317 (euler_first=1,
+ * forward Euler) or 331-467 (leapfrog + Robert-Asselin filter). */
+int qg_step(qg_handle* h, int euler_first);
+
+/* nsteps steps; the first is forward Euler when euler_first=1.  Asynchronous:
+ * returns once the work is queued on the handle's stream. */
+int qg_steps_async(qg_handle* h, int nsteps, int euler_first);
+int qg_synchronize(qg_handle* h);
+
+/* The handle's cudaStream_t (as void*) for event timing by the host. */
+int qg_get_stream(qg_handle* h, void** stream);
+
+/* FP64 energy / enstrophy integrals of the resident state. */
+int qg_diagnostics_fp64(qg_handle* h, qg_energy* out);
+
+/* Kernel classes of one step, for qg_profile_step. */
+enum qg_kernel_class {
+  QG_K_DISSIPATION = 0,  /* dissipation_q_nv (only when inviscid == 0 and nuz != 0) */
+  QG_K_COL_INV = 1,      /* y-inverse transforms of u, v, zeta, q, BR, BI           */
+  QG_K_ROW_MAIN = 2,     /* x-transforms and products of convol/refraction          */
+  QG_K_COL_UPDATE = 3,   /* y-forward transforms, leapfrog/filter, q^w y-inverse    */
+  QG_K_ROW_QW = 4,       /* x-transforms and products of compute_qw                 */
+  QG_K_COL_QW = 5,       /* y-forward transforms of q^w, q* = q - q^w               */
+  QG_K_SOLVE = 6,        /* FP64 tridiagonal solves q*->psi, B->A                   */
+  QG_K_NCLASSES = 7
+};
+
+/* Profiling aid (no counterpart in the reference): runs one step without the
+ * CUDA graph, with CUDA events around every kernel launch, and returns per
+ * kernel class the summed device time (ms) and the number of launches.  The
+ * state advances exactly as with qg_step. */
+int qg_profile_step(qg_handle* h, int euler_first, double* ms, int* launches, int nclasses);
+
+/* ---- routine-level drop-ins (same argument sets as the Fortran routines,
+ *      interior levels only, no scratch arrays) ---------------------------- */
+
+/* fft.f90:55-66: per-level 2D r2c of rvar, divided by n1*n2. */
+int qg_fft_r2c(qg_handle* h, const double* rvar, double* kvar, int nz);
+/* fft.f90:71-83: realit then unnormalised per-level 2D c2r.  kvar is read
+ * only (the reference's in-place transform destroys it). */
+int qg_fft_c2r(qg_handle* h, const double* kvar, double* rvar, int nz);
+/* derivatives.f90:607-803 */
+int qg_convol_waqg(qg_handle* h, const double* uk, const double* vk, const double* qk,
+                   const double* BRk, const double* BIk,
+                   double* nqk, double* nBRk, double* nBIk, int nz);
+/* derivatives.f90:810-900 */
+int qg_refraction_waqg(qg_handle* h, const double* BRk, const double* BIk, const double* psik,
+                       double* rBRk, double* rBIk, int nz);
+/* derivatives.f90:906-1032 */
+int qg_compute_qw(qg_handle* h, const double* BRk, const double* BIk, double* qwk, int nz);
+/* elliptic.f90:145-247: all n3 levels, z-major layout (no transpose). */
+int qg_psi_solver(qg_handle* h, const double* qstar, double* psik);
+/* elliptic.f90:346-460: all n3 levels; ck may be NULL. */
+int qg_A_solver_ybj_plus(qg_handle* h, const double* bk, double* ak, double* ck);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QGYBJ_H */

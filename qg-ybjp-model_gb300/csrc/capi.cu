@@ -1,0 +1,354 @@
+// C-ABI entry points (include/qgybj.h) and the host-side tables built once per
+// handle: dealiasing mask (init.f90:17-80), integrating factors
+// (main_waqg.f90:246-247), base state (init.f90:177-264) and the DGTSV
+// elimination factors of the two vertical operators (elliptic.f90:177-189).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include "engine.h"
+
+struct qg_handle {
+  qg::EngineBase* eng = nullptr;
+  std::string err;
+};
+
+namespace {
+thread_local std::string g_create_err;
+
+int fail(qg_handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg; else g_create_err = msg;
+  return code;
+}
+
+// Correctly rounded float32 of a non-negative integer (nearest-even): the
+// value of the default-REAL power (1.*k)**(2.*ilap) of the reference.
+float f32_round(unsigned __int128 m) {
+  int bits = 0;
+  for (unsigned __int128 t = m; t; t >>= 1) ++bits;
+  if (bits <= 24) return (float)(unsigned long long)m;
+  const int e = bits - 24;
+  unsigned __int128 q = m >> e;
+  const unsigned __int128 r = m - (q << e);
+  const unsigned __int128 half = (unsigned __int128)1 << (e - 1);
+  if (r > half || (r == half && (q & 1))) q += 1;
+  return std::ldexp((float)(unsigned long long)q, e);
+}
+
+float powk(int k, int ex) {
+  unsigned __int128 p = 1;
+  for (int i = 0; i < ex; ++i) p *= (unsigned __int128)(unsigned)k;
+  return f32_round(p);
+}
+
+bool finite_all(const double* a, int n) {
+  for (int i = 0; i < n; ++i) if (!std::isfinite(a[i])) return false;
+  return true;
+}
+
+int build_tables(const qg_config& c, qg::HostTables& t, std::string& err) {
+  const int n = c.n1, n3 = c.n3;
+  const int iktx = n / 2 + 1, ikty = n, kty = n / 2;
+  // --- mask L exactly as init_arrays (init.f90:32-80) ---------------------
+  const double twopi = 4.0 * std::asin(1.0);
+  const float thr_f = (float)(int)((float)n / 3.0f + 0.5f) - 0.5f;
+  const double thr = (double)thr_f;
+  std::vector<int> kya(ikty);
+  for (int iky = 1; iky <= ikty; ++iky) {
+    int jj = iky - 1;
+    if (iky > kty) jj -= 2 * kty;
+    if (iky == kty + 1) jj = 0;
+    if (iky > 2 * kty) jj = 0;
+    kya[iky - 1] = jj;
+  }
+  std::vector<unsigned char> L((size_t)ikty * iktx);
+  int kmax2 = -1, K = 0;
+  for (int iky = 0; iky < ikty; ++iky) {
+    for (int kx = 0; kx < iktx; ++kx) {
+      const int ky = kya[iky];
+      const double kh = (double)std::sqrt((float)(kx * kx + ky * ky));
+      int l = 1;
+      if (iky + 1 == kty + 1) l = 0;
+      else if (kx == 0 && ky < 0) l = 0;
+      else if ((kh * twopi / twopi) > thr) l = 0;
+      L[(size_t)iky * iktx + kx] = (unsigned char)l;
+      if (l) { kmax2 = std::max(kmax2, kx * kx + ky * ky); K = std::max(K, kx); }
+    }
+  }
+  // the compact layout relies on L being the disk kx^2+ky^2 <= kmax2 (minus kx=0,ky<0)
+  for (int iky = 0; iky < ikty; ++iky)
+    for (int kx = 0; kx < iktx; ++kx) {
+      const int ky = kya[iky];
+      const bool disk = iky != kty && kx * kx + ky * ky <= kmax2 && !(kx == 0 && ky < 0);
+      if (disk != (bool)L[(size_t)iky * iktx + kx]) { err = "dealiasing mask is not a disk"; return QG_ERR_UNSUPPORTED; }
+    }
+  t.n = n; t.n3 = n3; t.K = K; t.KX = K + 1; t.KY = 2 * K + 1;
+  t.KXP = ((K + 1 + 7) / 8) * 8;
+  t.kmax2 = kmax2;
+  t.plane = (long long)t.KY * t.KXP;
+  // --- integrating factors (main_waqg.f90:246-247, 371-372) ---------------
+  t.e1.assign(t.plane, 0.0); t.e2.assign(t.plane, 0.0); t.e1w.assign(t.plane, 0.0); t.e2w.assign(t.plane, 0.0);
+  for (int r = 0; r < t.KY; ++r) {
+    const int ky = r <= K ? r : r - t.KY;
+    const int aky = ky < 0 ? -ky : ky;
+    for (int kx = 0; kx <= K; ++kx) {
+      const float s1 = powk(kx, 2 * c.ilap1) + powk(aky, 2 * c.ilap1);
+      const float s2 = powk(kx, 2 * c.ilap2) + powk(aky, 2 * c.ilap2);
+      const float s1w = powk(kx, 2 * c.ilap1w) + powk(aky, 2 * c.ilap1w);
+      const float s2w = powk(kx, 2 * c.ilap2w) + powk(aky, 2 * c.ilap2w);
+      const double IF = c.delt * (c.nuh1 * (double)s1 + c.nuh2 * (double)s2);
+      const double IFw = c.delt * (c.nuh1w * (double)s1w + c.nuh2w * (double)s2w);
+      const long long m = (long long)r * t.KXP + kx;
+      t.e1[m] = std::exp(-IF); t.e2[m] = std::exp(-2 * IF);
+      t.e1w[m] = std::exp(-IFw); t.e2w[m] = std::exp(-2 * IFw);
+    }
+  }
+  // --- twiddles W_n^m = exp(-2 pi i m/n) ---------------------------------
+  t.tw.assign(2 * (size_t)n, 0.0);
+  for (int m = 0; m < n; ++m) {
+    double cs, sn;
+    if ((4 * m) % n == 0) {
+      const int q = (4 * m) / n;
+      const double C4[4] = {1, 0, -1, 0}, S4[4] = {0, 1, 0, -1};
+      cs = C4[q]; sn = S4[q];
+    } else {
+      const double th = twopi * (double)m / (double)n;
+      cs = std::cos(th); sn = std::sin(th);
+    }
+    t.tw[2 * m] = cs; t.tw[2 * m + 1] = -sn;
+  }
+  // --- base state and vertical operators ---------------------------------
+  std::vector<double> a(c.a_ell_ut, c.a_ell_ut + n3), ru(n3, 1.0), rs(n3, 1.0);
+  if (c.rho_ut) ru.assign(c.rho_ut, c.rho_ut + n3);
+  if (c.rho_st) rs.assign(c.rho_st, c.rho_st + n3);
+  t.du.assign(n3, 0.0); t.cu.assign(n3, 0.0); t.cl.assign(n3, 0.0); t.r2.assign(n3, 0.0);
+  for (int i = 0; i < n3; ++i) {
+    if (i < n3 - 1) t.du[i] = ru[i] * a[i] / rs[i];
+    t.cu[i] = i < n3 - 1 ? ru[i] * a[i] / rs[i] : 0.0;
+    t.cl[i] = i > 0 ? ru[i - 1] * a[i - 1] / rs[i] : 0.0;
+    t.r2[i] = c.r_2ut ? c.r_2ut[i] : c.Bu / a[i];
+  }
+  // distinct kh^2 of active columns (L=1, kh^2 != 0), elliptic.f90:171
+  std::map<int, int> idx;
+  for (int r = 0; r < t.KY; ++r) {
+    const int ky = r <= K ? r : r - t.KY;
+    for (int kx = 0; kx <= K; ++kx) {
+      const int kh2 = kx * kx + ky * ky;
+      if (kh2 != 0 && kh2 <= kmax2 && !(kx == 0 && ky < 0)) idx[kh2] = 0;
+    }
+  }
+  int nd = 0;
+  for (auto& kv : idx) kv.second = nd++;
+  t.ndistinct = nd;
+  t.tab_idx.assign(t.plane, -1);
+  for (int r = 0; r < t.KY; ++r) {
+    const int ky = r <= K ? r : r - t.KY;
+    for (int kx = 0; kx <= K; ++kx) {
+      const int kh2 = kx * kx + ky * ky;
+      if (kh2 != 0 && kh2 <= kmax2 && !(kx == 0 && ky < 0)) t.tab_idx[(size_t)r * t.KXP + kx] = idx[kh2];
+    }
+  }
+  t.fac_psi.assign((size_t)nd * n3 * 2, 0.0);
+  t.fac_A.assign((size_t)nd * n3 * 2, 0.0);
+  std::vector<double> d(n3), dl(n3), du(n3);
+  for (auto& kv : idx) {
+    for (int op = 0; op < 2; ++op) {
+      const double kdz = op == 0 ? (double)kv.first * c.dz * c.dz : (double)kv.first * c.dz * c.dz / 4.0;
+      for (int i = 0; i < n3; ++i) {
+        if (i == 0) {
+          d[i] = -(ru[0] * a[0] / rs[0] + kdz);
+          du[i] = ru[0] * a[0] / rs[0];
+        } else if (i == n3 - 1) {
+          d[i] = -(ru[i - 1] * a[i - 1] / rs[i] + kdz);
+          dl[i - 1] = ru[i - 1] * a[i - 1] / rs[i];
+        } else {
+          d[i] = -((ru[i] * a[i] + ru[i - 1] * a[i - 1]) / rs[i] + kdz);
+          du[i] = ru[i] * a[i] / rs[i];
+          dl[i - 1] = ru[i - 1] * a[i - 1] / rs[i];
+        }
+      }
+      // DGTSV elimination order without row interchanges
+      double* out = (op == 0 ? t.fac_psi.data() : t.fac_A.data()) + (size_t)kv.second * n3 * 2;
+      double dp = d[0];
+      for (int i = 0; i < n3 - 1; ++i) {
+        if (dp == 0.0) { err = "zero pivot in tridiagonal factorisation (kh2=" + std::to_string(kv.first) + ")"; return QG_ERR_PIVOT; }
+        if (std::fabs(dp) < std::fabs(dl[i])) {
+          err = "tridiagonal factorisation needs a row interchange (kh2=" + std::to_string(kv.first) + ")";
+          return QG_ERR_PIVOT;
+        }
+        const double f = dl[i] / dp;
+        out[2 * i] = f;
+        out[2 * i + 1] = 1.0 / dp;
+        dp = d[i + 1] - f * du[i];
+      }
+      if (dp == 0.0 || !std::isfinite(dp)) { err = "zero pivot in tridiagonal factorisation"; return QG_ERR_PIVOT; }
+      out[2 * (n3 - 1)] = 0.0;
+      out[2 * (n3 - 1) + 1] = 1.0 / dp;
+    }
+  }
+  return QG_OK;
+}
+
+}  // namespace
+
+namespace qg {
+bool supported_n(int n) { return n == 16 || n == 32 || n == 64 || n == 128 || n == 256 || n == 512 || n == 1024; }
+}  // namespace qg
+
+extern "C" {
+
+int qg_config_defaults(qg_config* c) {
+  if (!c) return QG_ERR_ARG;
+  std::memset(c, 0, sizeof *c);
+  c->precision = QG_PREC_MIXED;
+  c->ybj_plus = 1;
+  c->inviscid = 1;
+  c->ilap1 = c->ilap1w = 2;
+  c->ilap2 = c->ilap2w = 6;
+  c->use_graphs = 1;
+  return QG_OK;
+}
+
+int qg_create(const qg_config* cfg, qg_handle** out) {
+  if (!cfg || !out) return fail(nullptr, QG_ERR_ARG, "null argument");
+  *out = nullptr;
+  const qg_config& c = *cfg;
+  if (c.n1 != c.n2) return fail(nullptr, QG_ERR_UNSUPPORTED, "n1 must equal n2");
+  if (!qg::supported_n(c.n1)) return fail(nullptr, QG_ERR_UNSUPPORTED, "n1 must be a power of two in [16,1024]");
+  if (c.n3 < 2) return fail(nullptr, QG_ERR_ARG, "n3 must be >= 2");
+  if (c.precision != QG_PREC_FP64 && c.precision != QG_PREC_MIXED) return fail(nullptr, QG_ERR_ARG, "bad precision");
+  if (c.ybj_plus != 1) return fail(nullptr, QG_ERR_UNSUPPORTED, "only the YBJ+ step (ybj_plus=1) is implemented");
+  if (!c.a_ell_ut) return fail(nullptr, QG_ERR_ARG, "a_ell_ut is required");
+  if (!(c.dz > 0) || !(c.Bu > 0) || !(c.Ro > 0)) return fail(nullptr, QG_ERR_ARG, "dz, Bu and Ro must be positive");
+  const double sc[] = {c.dz, c.Bu, c.Ro, c.W2F, c.delt, c.gamma, c.nuh1, c.nuh2, c.nuh1w, c.nuh2w, c.nuz};
+  if (!finite_all(sc, (int)(sizeof sc / sizeof sc[0])) || !finite_all(c.a_ell_ut, c.n3) ||
+      (c.rho_ut && !finite_all(c.rho_ut, c.n3)) || (c.rho_st && !finite_all(c.rho_st, c.n3)) ||
+      (c.r_2ut && !finite_all(c.r_2ut, c.n3)))
+    return fail(nullptr, QG_ERR_NONFINITE, "non-finite configuration value");
+  if (c.ilap1 < 0 || c.ilap2 < 0 || c.ilap1w < 0 || c.ilap2w < 0 || c.ilap1 > 9 || c.ilap2 > 9 || c.ilap1w > 9 ||
+      c.ilap2w > 9)
+    return fail(nullptr, QG_ERR_ARG, "ilap out of range [0,9]");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || c.device < 0 || c.device >= ndev)
+    return fail(nullptr, QG_ERR_CUDA, "no CUDA device with that ordinal");
+  qg::HostTables t;
+  std::string err;
+  int rc = build_tables(c, t, err);
+  if (rc) return fail(nullptr, rc, err);
+  qg_handle* h = new qg_handle();
+  h->eng = c.precision == QG_PREC_FP64 ? qg::make_engine_fp64() : qg::make_engine_fp32();
+  rc = h->eng->init(c, t);
+  if (rc) {
+    g_create_err = h->eng->err;
+    delete h->eng;
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return QG_OK;
+}
+
+int qg_destroy(qg_handle* h) {
+  if (!h) return QG_ERR_ARG;
+  delete h->eng;
+  delete h;
+  return QG_OK;
+}
+
+const char* qg_last_error(const qg_handle* h) {
+  if (!h) return g_create_err.c_str();
+  if (!h->err.empty()) return h->err.c_str();
+  return h->eng ? h->eng->err.c_str() : "";
+}
+
+#define QG_ENTRY(h)                       \
+  if (!(h) || !(h)->eng) return QG_ERR_ARG; \
+  (h)->err.clear();
+
+static int fwd(qg_handle* h, int rc) {
+  if (rc && h->err.empty()) h->err = h->eng->err;
+  return rc;
+}
+
+int qg_set_state(qg_handle* h, int field, const double* kvar, int level0, int nlev) {
+  QG_ENTRY(h);
+  return fwd(h, h->eng->set_state(field, kvar, level0, nlev));
+}
+int qg_get_state(qg_handle* h, int field, double* kvar, int level0, int nlev) {
+  QG_ENTRY(h);
+  return fwd(h, h->eng->get_state(field, kvar, level0, nlev));
+}
+int qg_init_state(qg_handle* h, int apply_sumB, int q_from_psi) {
+  QG_ENTRY(h);
+  return fwd(h, h->eng->init_state(apply_sumB, q_from_psi));
+}
+int qg_step(qg_handle* h, int euler_first) {
+  QG_ENTRY(h);
+  return fwd(h, h->eng->step(euler_first));
+}
+int qg_steps_async(qg_handle* h, int nsteps, int euler_first) {
+  QG_ENTRY(h);
+  if (nsteps < 0) return fail(h, QG_ERR_ARG, "nsteps must be >= 0");
+  return fwd(h, h->eng->steps_async(nsteps, euler_first));
+}
+int qg_synchronize(qg_handle* h) {
+  QG_ENTRY(h);
+  return fwd(h, h->eng->synchronize());
+}
+int qg_get_stream(qg_handle* h, void** stream) {
+  QG_ENTRY(h);
+  if (!stream) return fail(h, QG_ERR_ARG, "null stream pointer");
+  *stream = h->eng->stream();
+  return QG_OK;
+}
+int qg_diagnostics_fp64(qg_handle* h, qg_energy* out) {
+  QG_ENTRY(h);
+  if (!out) return fail(h, QG_ERR_ARG, "null output");
+  return fwd(h, h->eng->diagnostics(out));
+}
+int qg_profile_step(qg_handle* h, int euler_first, double* ms, int* launches, int nclasses) {
+  QG_ENTRY(h);
+  if (!ms || !launches || nclasses <= 0) return fail(h, QG_ERR_ARG, "null output or nclasses <= 0");
+  return fwd(h, h->eng->profile_step(euler_first, ms, launches, nclasses));
+}
+int qg_fft_r2c(qg_handle* h, const double* rvar, double* kvar, int nz) {
+  QG_ENTRY(h);
+  if (!rvar || !kvar) return fail(h, QG_ERR_ARG, "null pointer");
+  return fwd(h, h->eng->fft_r2c(rvar, kvar, nz));
+}
+int qg_fft_c2r(qg_handle* h, const double* kvar, double* rvar, int nz) {
+  QG_ENTRY(h);
+  if (!rvar || !kvar) return fail(h, QG_ERR_ARG, "null pointer");
+  return fwd(h, h->eng->fft_c2r(kvar, rvar, nz));
+}
+int qg_convol_waqg(qg_handle* h, const double* uk, const double* vk, const double* qk, const double* BRk,
+                   const double* BIk, double* nqk, double* nBRk, double* nBIk, int nz) {
+  QG_ENTRY(h);
+  if (!uk || !vk || !qk || !BRk || !BIk || !nqk || !nBRk || !nBIk) return fail(h, QG_ERR_ARG, "null pointer");
+  return fwd(h, h->eng->convol_waqg(uk, vk, qk, BRk, BIk, nqk, nBRk, nBIk, nz));
+}
+int qg_refraction_waqg(qg_handle* h, const double* BRk, const double* BIk, const double* psik, double* rBRk,
+                       double* rBIk, int nz) {
+  QG_ENTRY(h);
+  if (!BRk || !BIk || !psik || !rBRk || !rBIk) return fail(h, QG_ERR_ARG, "null pointer");
+  return fwd(h, h->eng->refraction_waqg(BRk, BIk, psik, rBRk, rBIk, nz));
+}
+int qg_compute_qw(qg_handle* h, const double* BRk, const double* BIk, double* qwk, int nz) {
+  QG_ENTRY(h);
+  if (!BRk || !BIk || !qwk) return fail(h, QG_ERR_ARG, "null pointer");
+  return fwd(h, h->eng->compute_qw(BRk, BIk, qwk, nz));
+}
+int qg_psi_solver(qg_handle* h, const double* qstar, double* psik) {
+  QG_ENTRY(h);
+  if (!qstar || !psik) return fail(h, QG_ERR_ARG, "null pointer");
+  return fwd(h, h->eng->psi_solver(qstar, psik));
+}
+int qg_A_solver_ybj_plus(qg_handle* h, const double* bk, double* ak, double* ck) {
+  QG_ENTRY(h);
+  if (!bk || !ak) return fail(h, QG_ERR_ARG, "null pointer");
+  return fwd(h, h->eng->A_solver(bk, ak, ck));
+}
+
+}  // extern "C"

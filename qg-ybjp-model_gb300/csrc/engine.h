@@ -1,0 +1,53 @@
+// Host-side engine interface shared by the C-ABI (capi.cu) and the two
+// precision instantiations (engine_fp32.cu, engine_fp64.cu).
+#pragma once
+#include <string>
+#include <vector>
+#include "../../include/qgybj.h"
+
+namespace qg {
+
+// Tables built once on the host from the configuration (init.f90:17-264).
+struct HostTables {
+  int n, n3, K, KX, KY, KXP, kmax2;
+  long long plane;
+  std::vector<double> e1, e2, e1w, e2w;     // [plane] integrating factors
+  std::vector<double> tw;                   // [2n] cos, sin of -2 pi m / n interleaved
+  std::vector<int> tab_idx;                 // [plane] distinct-kh2 row, -1 = inactive column
+  std::vector<double> fac_psi, fac_A;       // [ndistinct][n3][2] {f_i, 1/d'_i}
+  int ndistinct;
+  std::vector<double> du;                   // [n3] upper diagonal rho_ut a / rho_st
+  std::vector<double> cu, cl;               // [n3] init_q coefficients of psi(z+1), psi(z-1)
+  std::vector<double> r2;                   // [n3] N^2 at za(iz)
+};
+
+struct EngineBase {
+  virtual ~EngineBase() {}
+  std::string err;
+  virtual int init(const qg_config& cfg, const HostTables& t) = 0;
+  virtual int set_state(int field, const double* kvar, int level0, int nlev) = 0;
+  virtual int get_state(int field, double* kvar, int level0, int nlev) = 0;
+  virtual int init_state(int apply_sumB, int q_from_psi) = 0;
+  virtual int step(int euler) = 0;
+  virtual int steps_async(int nsteps, int euler) = 0;
+  virtual int synchronize() = 0;
+  virtual void* stream() = 0;
+  virtual int diagnostics(qg_energy* out) = 0;
+  virtual int profile_step(int euler, double* ms, int* launches, int nclasses) = 0;
+  virtual int fft_r2c(const double* rvar, double* kvar, int nz) = 0;
+  virtual int fft_c2r(const double* kvar, double* rvar, int nz) = 0;
+  virtual int convol_waqg(const double* uk, const double* vk, const double* qk, const double* BRk, const double* BIk,
+                          double* nqk, double* nBRk, double* nBIk, int nz) = 0;
+  virtual int refraction_waqg(const double* BRk, const double* BIk, const double* psik, double* rBRk, double* rBIk,
+                              int nz) = 0;
+  virtual int compute_qw(const double* BRk, const double* BIk, double* qwk, int nz) = 0;
+  virtual int psi_solver(const double* qstar, double* psik) = 0;
+  virtual int A_solver(const double* bk, double* ak, double* ck) = 0;
+};
+
+EngineBase* make_engine_fp32();
+EngineBase* make_engine_fp64();
+
+bool supported_n(int n);
+
+}  // namespace qg

@@ -1,0 +1,613 @@
+// Engine<T>: device buffers, launch sequence and CUDA-graph replay of the
+// step, state conversions, routine-level drop-ins.  T = float (mixed
+// precision: FP64 only in the tridiagonal solves and the diagnostics) or
+// T = double (FP64 everywhere).
+#pragma once
+#include <cstdio>
+#include <cstring>
+#include <cmath>
+#include <algorithm>
+#include "engine.h"
+#include "dense_kernels.cuh"
+
+namespace qg {
+
+#define QG_CK(call)                                                                          \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess) {                                                                 \
+      char b_[512];                                                                          \
+      snprintf(b_, sizeof b_, "%s:%d: %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
+      err = b_;                                                                              \
+      return e_ == cudaErrorMemoryAllocation ? QG_ERR_NOMEM : QG_ERR_CUDA;                   \
+    }                                                                                        \
+  } while (0)
+
+#define QG_LAUNCHED() QG_CK(cudaGetLastError())
+
+#define QG_SWITCH_N(n, ...)                      \
+  switch (n) {                                    \
+    case 16: { constexpr int NN = 16; __VA_ARGS__; break; }    \
+    case 32: { constexpr int NN = 32; __VA_ARGS__; break; }    \
+    case 64: { constexpr int NN = 64; __VA_ARGS__; break; }    \
+    case 128: { constexpr int NN = 128; __VA_ARGS__; break; }  \
+    case 256: { constexpr int NN = 256; __VA_ARGS__; break; }  \
+    case 512: { constexpr int NN = 512; __VA_ARGS__; break; }  \
+    case 1024: { constexpr int NN = 1024; __VA_ARGS__; break; }\
+    default: err = "unsupported n"; return QG_ERR_UNSUPPORTED; \
+  }
+
+enum { F_Q = 0, F_QO, F_BR, F_BI, F_BRO, F_BIO, F_PSI, F_AR, F_AI, F_QSTAR, F_DQ, F_NINT };
+
+template <typename T>
+class Engine final : public EngineBase {
+  using C = cplx<T>;
+
+ public:
+  ~Engine() override { release(); }
+
+  int init(const qg_config& c, const HostTables& t) override {
+    cfg = c;
+    g.n = t.n; g.n3 = t.n3; g.K = t.K; g.KX = t.KX; g.KY = t.KY; g.KXP = t.KXP; g.kmax2 = t.kmax2;
+    g.plane = t.plane;
+    QG_CK(cudaSetDevice(cfg.device));
+    QG_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    const size_t fbytes = (size_t)g.n3 * g.plane * sizeof(C);
+    for (int f = 0; f < F_NINT; ++f) {
+      if (f == F_DQ && !(cfg.inviscid == 0 && cfg.nuz != 0.0)) continue;
+      QG_CK(cudaMalloc(&F[f], fbytes));
+      QG_CK(cudaMemsetAsync(F[f], 0, fbytes, st));
+    }
+    // tables
+    std::vector<T> tmp(g.plane);
+    auto up = [&](T** d, const std::vector<double>& h) -> int {
+      for (long long i = 0; i < g.plane; ++i) tmp[i] = (T)h[i];
+      QG_CK(cudaMalloc(d, g.plane * sizeof(T)));
+      QG_CK(cudaMemcpy(*d, tmp.data(), g.plane * sizeof(T), cudaMemcpyHostToDevice));
+      return QG_OK;
+    };
+    int rc;
+    if ((rc = up(&e1, t.e1)) || (rc = up(&e2, t.e2)) || (rc = up(&e1w, t.e1w)) || (rc = up(&e2w, t.e2w))) return rc;
+    std::vector<C> twh(g.n);
+    for (int m = 0; m < g.n; ++m) twh[m] = mk<T>((T)t.tw[2 * m], (T)t.tw[2 * m + 1]);
+    QG_CK(cudaMalloc(&tw, g.n * sizeof(C)));
+    QG_CK(cudaMemcpy(tw, twh.data(), g.n * sizeof(C), cudaMemcpyHostToDevice));
+    QG_CK(cudaMalloc(&tab_idx, g.plane * sizeof(int)));
+    QG_CK(cudaMemcpy(tab_idx, t.tab_idx.data(), g.plane * sizeof(int), cudaMemcpyHostToDevice));
+    const size_t fb = std::max<size_t>(1, (size_t)t.ndistinct * g.n3) * sizeof(double2);
+    QG_CK(cudaMalloc(&fac_psi, fb));
+    QG_CK(cudaMalloc(&fac_A, fb));
+    if (t.ndistinct > 0) {
+      QG_CK(cudaMemcpy(fac_psi, t.fac_psi.data(), (size_t)t.ndistinct * g.n3 * sizeof(double2), cudaMemcpyHostToDevice));
+      QG_CK(cudaMemcpy(fac_A, t.fac_A.data(), (size_t)t.ndistinct * g.n3 * sizeof(double2), cudaMemcpyHostToDevice));
+    }
+    auto upd = [&](double** d, const std::vector<double>& h) -> int {
+      QG_CK(cudaMalloc(d, h.size() * sizeof(double)));
+      QG_CK(cudaMemcpy(*d, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
+      return QG_OK;
+    };
+    if ((rc = upd(&du, t.du)) || (rc = upd(&cu, t.cu)) || (rc = upd(&cl, t.cl)) || (rc = upd(&r2, t.r2))) return rc;
+    QG_CK(cudaMalloc(&bscr, (size_t)2 * g.n3 * g.plane * sizeof(double2)));
+    QG_CK(cudaMalloc(&diag_part, (size_t)g.n3 * kNDiag * sizeof(double)));
+    QG_CK(cudaMalloc(&diag_out, kNDiag * sizeof(double)));
+    QG_CK(cudaMallocHost(&diag_host, kNDiag * sizeof(double)));
+    // phase-A batching: keep the scratch planes of one batch L2-sized
+    const size_t per_level = (size_t)kNScr * g.n * g.KXP * sizeof(C);
+    int zb = cfg.levels_per_batch;
+    if (zb <= 0) zb = (int)std::max<size_t>(1, (size_t)(48u << 20) / per_level);
+    zb = std::min(zb, g.n3);
+    const int nb = (g.n3 + zb - 1) / zb;
+    Zb = (g.n3 + nb - 1) / nb;
+    QG_CK(cudaMalloc(&S, (size_t)Zb * per_level));
+    sp.delt = cfg.delt; sp.gamma = cfg.gamma; sp.Bu = cfg.Bu; sp.Ro = cfg.Ro; sp.W2F = cfg.W2F;
+    sp.dz = cfg.dz; sp.nuz = cfg.nuz; sp.cdisp = 0.5 / (cfg.Bu * cfg.Ro);
+    sp.adv = cfg.linear ? 0 : 1;
+    sp.refr = cfg.passive_scalar ? 0 : 1;
+    sp.disp = (cfg.no_dispersion || cfg.passive_scalar) ? 0 : 1;
+    sp.use_dq = (cfg.inviscid == 0 && cfg.nuz != 0.0) ? 1 : 0;
+    sp.euler = 0;
+    need_qw = (!cfg.fixed_flow && !cfg.no_feedback);
+    int r0 = set_smem_attrs();
+    if (r0) return r0;
+    QG_CK(cudaStreamSynchronize(st));
+    return QG_OK;
+  }
+
+  void* stream() override { return (void*)st; }
+
+  int synchronize() override { QG_CK(cudaStreamSynchronize(st)); return QG_OK; }
+
+  // ---- state --------------------------------------------------------------
+  int set_state(int field, const double* kvar, int level0, int nlev) override {
+    const int f = map_field(field);
+    if (f < 0 || field == QG_CR || field == QG_CI || field == QG_QSTAR) { err = "field is read-only or unknown"; return QG_ERR_ARG; }
+    if (!kvar || level0 < 0 || nlev <= 0 || level0 + nlev > g.n3) { err = "bad level range or null pointer"; return QG_ERR_ARG; }
+    const size_t bytes = (size_t)nlev * g.n * (g.n / 2 + 1) * sizeof(double2);
+    int rc = ensure(&stage, &stage_bytes, bytes);
+    if (rc) return rc;
+    QG_CK(cudaMemcpyAsync(stage, kvar, bytes, cudaMemcpyDefault, st));
+    k_dense_to_compact<T><<<grid_for((long long)nlev * g.plane), 256, 0, st>>>(g, level0, nlev, (const double2*)stage, F[f]);
+    QG_LAUNCHED();
+    QG_CK(cudaStreamSynchronize(st));
+    return QG_OK;
+  }
+
+  int get_state(int field, double* kvar, int level0, int nlev) override {
+    int f = map_field(field);
+    if (f < 0) { err = "unknown field"; return QG_ERR_ARG; }
+    if (!kvar || level0 < 0 || nlev <= 0 || level0 + nlev > g.n3) { err = "bad level range or null pointer"; return QG_ERR_ARG; }
+    if (field == QG_QSTAR && !need_qw) f = F_Q;
+    const int mode = (field == QG_CR || field == QG_CI) ? 1 : 0;
+    const size_t bytes = (size_t)nlev * g.n * (g.n / 2 + 1) * sizeof(double2);
+    int rc = ensure(&stage, &stage_bytes, bytes);
+    if (rc) return rc;
+    k_compact_to_dense<T><<<grid_for((long long)nlev * g.n * (g.n / 2 + 1)), 256, 0, st>>>(g, level0, nlev, F[f],
+                                                                                          (double2*)stage, mode, cfg.dz);
+    QG_LAUNCHED();
+    QG_CK(cudaMemcpyAsync(kvar, stage, bytes, cudaMemcpyDefault, st));
+    QG_CK(cudaStreamSynchronize(st));
+    return QG_OK;
+  }
+
+  int init_state(int apply_sumB, int q_from_psi) override {
+    if (apply_sumB) {
+      k_sumB<T><<<(unsigned)((g.plane + 127) / 128), 128, 0, st>>>(g, F[F_BR], F[F_BI]);
+      QG_LAUNCHED();
+    }
+    if (q_from_psi) {
+      k_init_q<T><<<grid_for((long long)g.n3 * g.plane), 256, 0, st>>>(g, cfg.dz, cu, cl, F[F_PSI], F[F_Q]);
+      QG_LAUNCHED();
+    }
+    const size_t fbytes = (size_t)g.n3 * g.plane * sizeof(C);
+    QG_CK(cudaMemcpyAsync(F[F_QO], F[F_Q], fbytes, cudaMemcpyDeviceToDevice, st));
+    QG_CK(cudaMemcpyAsync(F[F_BRO], F[F_BR], fbytes, cudaMemcpyDeviceToDevice, st));
+    QG_CK(cudaMemcpyAsync(F[F_BIO], F[F_BI], fbytes, cudaMemcpyDeviceToDevice, st));
+    if (!cfg.passive_scalar) {
+      int rc = launch_solve(F[F_QSTAR], 0, 1);
+      if (rc) return rc;
+    }
+    QG_CK(cudaStreamSynchronize(st));
+    return QG_OK;
+  }
+
+  // ---- the step -------------------------------------------------------------
+  int step(int euler) override {
+    int rc = run_step(euler ? 1 : 0);
+    if (rc) return rc;
+    QG_CK(cudaStreamSynchronize(st));
+    return QG_OK;
+  }
+
+  int steps_async(int nsteps, int euler) override {
+    for (int i = 0; i < nsteps; ++i) {
+      int rc = run_step((euler && i == 0) ? 1 : 0);
+      if (rc) return rc;
+    }
+    return QG_OK;
+  }
+
+  int diagnostics(qg_energy* out) override {
+    k_diag_level<T><<<g.n3, 256, 0, st>>>(g, cfg.dz, cfg.Bu, r2, F[F_BR], F[F_BI], F[F_AR], F[F_AI], F[F_PSI], diag_part);
+    QG_LAUNCHED();
+    k_diag_sum<<<1, 32, 0, st>>>(g.n3, diag_part, diag_out);
+    QG_LAUNCHED();
+    QG_CK(cudaMemcpyAsync(diag_host, diag_out, kNDiag * sizeof(double), cudaMemcpyDeviceToHost, st));
+    QG_CK(cudaStreamSynchronize(st));
+    out->wke = diag_host[0]; out->wpe = diag_host[1]; out->wce = diag_host[2];
+    out->ke = diag_host[3]; out->pe = diag_host[4]; out->zeta2 = diag_host[5]; out->omegah2 = diag_host[6];
+    return QG_OK;
+  }
+
+  // ---- routine-level drop-ins ---------------------------------------------
+  int fft_r2c(const double* rvar, double* kvar, int nz) override {
+    int rc = prep_dense(nz);
+    if (rc) return rc;
+    const long long np = (long long)nz * g.n * (g.n + 2);
+    QG_CK(cudaMemcpyAsync(dstage, rvar, np * sizeof(double), cudaMemcpyDefault, st));
+    k_phys_unpad<T><<<grid_for((long long)nz * g.n * g.n), 256, 0, st>>>(g.n, (long long)nz * g.n * g.n, dstage, P[0]);
+    QG_LAUNCHED();
+    if ((rc = d_r2c(P[0], D[0], nz))) return rc;
+    QG_CK(cudaMemcpyAsync(kvar, D[0], dense_bytes(nz), cudaMemcpyDefault, st));
+    QG_CK(cudaStreamSynchronize(st));
+    return QG_OK;
+  }
+
+  int fft_c2r(const double* kvar, double* rvar, int nz) override {
+    int rc = prep_dense(nz);
+    if (rc) return rc;
+    QG_CK(cudaMemcpyAsync(D[0], kvar, dense_bytes(nz), cudaMemcpyDefault, st));
+    if ((rc = d_c2r(D[0], P[0], nz))) return rc;
+    const long long np = (long long)nz * g.n * (g.n + 2);
+    k_phys_pad<T><<<grid_for(np), 256, 0, st>>>(g.n, np, P[0], dstage);
+    QG_LAUNCHED();
+    QG_CK(cudaMemcpyAsync(rvar, dstage, np * sizeof(double), cudaMemcpyDefault, st));
+    QG_CK(cudaStreamSynchronize(st));
+    return QG_OK;
+  }
+
+  int convol_waqg(const double* uk, const double* vk, const double* qk, const double* BRk, const double* BIk,
+                  double* nqk, double* nBRk, double* nBIk, int nz) override {
+    int rc = prep_dense(nz);
+    if (rc) return rc;
+    const size_t db = dense_bytes(nz);
+    const long long tot = (long long)nz * g.n * (g.n / 2 + 1), pt = (long long)nz * g.n * g.n;
+    QG_CK(cudaMemcpyAsync(D[0], uk, db, cudaMemcpyDefault, st));
+    QG_CK(cudaMemcpyAsync(D[1], vk, db, cudaMemcpyDefault, st));
+    if ((rc = d_c2r(D[0], P[0], nz)) || (rc = d_c2r(D[1], P[1], nz))) return rc;
+    const double* ins[3] = {qk, BRk, BIk};
+    double* outs[3] = {nqk, nBRk, nBIk};
+    for (int k = 0; k < 3; ++k) {
+      QG_CK(cudaMemcpyAsync(D[2], ins[k], db, cudaMemcpyDefault, st));
+      if ((rc = d_c2r(D[2], P[2], nz))) return rc;
+      k_phys<T><<<grid_for(pt), 256, 0, st>>>(pt, 0, P[0], P[2], nullptr, nullptr, P[3]);
+      QG_LAUNCHED();
+      if ((rc = d_r2c(P[3], D[3], nz))) return rc;
+      k_phys<T><<<grid_for(pt), 256, 0, st>>>(pt, 0, P[1], P[2], nullptr, nullptr, P[3]);
+      QG_LAUNCHED();
+      if ((rc = d_r2c(P[3], D[4], nz))) return rc;
+      k_dense_ik<<<grid_for(tot), 256, 0, st>>>(g.n, g.kmax2, tot, D[3], D[4], D[5]);
+      QG_LAUNCHED();
+      QG_CK(cudaMemcpyAsync(outs[k], D[5], db, cudaMemcpyDefault, st));
+      QG_CK(cudaStreamSynchronize(st));
+    }
+    return QG_OK;
+  }
+
+  int refraction_waqg(const double* BRk, const double* BIk, const double* psik, double* rBRk, double* rBIk,
+                      int nz) override {
+    int rc = prep_dense(nz);
+    if (rc) return rc;
+    const size_t db = dense_bytes(nz);
+    const long long tot = (long long)nz * g.n * (g.n / 2 + 1), pt = (long long)nz * g.n * g.n;
+    QG_CK(cudaMemcpyAsync(D[0], psik, db, cudaMemcpyDefault, st));
+    k_dense_op<<<grid_for(tot), 256, 0, st>>>(g.n, g.kmax2, tot, 0, D[0], D[1]);
+    QG_LAUNCHED();
+    if ((rc = d_c2r(D[1], P[0], nz))) return rc;
+    const double* ins[2] = {BRk, BIk};
+    double* outs[2] = {rBRk, rBIk};
+    for (int k = 0; k < 2; ++k) {
+      QG_CK(cudaMemcpyAsync(D[2], ins[k], db, cudaMemcpyDefault, st));
+      if ((rc = d_c2r(D[2], P[1], nz))) return rc;
+      k_phys<T><<<grid_for(pt), 256, 0, st>>>(pt, 0, P[0], P[1], nullptr, nullptr, P[2]);
+      QG_LAUNCHED();
+      if ((rc = d_r2c(P[2], D[3], nz))) return rc;
+      k_dense_mask<<<grid_for(tot), 256, 0, st>>>(g.n, g.kmax2, tot, D[3], D[4]);
+      QG_LAUNCHED();
+      QG_CK(cudaMemcpyAsync(outs[k], D[4], db, cudaMemcpyDefault, st));
+      QG_CK(cudaStreamSynchronize(st));
+    }
+    return QG_OK;
+  }
+
+  int compute_qw(const double* BRk, const double* BIk, double* qwk, int nz) override {
+    int rc = prep_dense(nz);
+    if (rc) return rc;
+    const size_t db = dense_bytes(nz);
+    const long long tot = (long long)nz * g.n * (g.n / 2 + 1), pt = (long long)nz * g.n * g.n;
+    QG_CK(cudaMemcpyAsync(D[0], BRk, db, cudaMemcpyDefault, st));
+    QG_CK(cudaMemcpyAsync(D[1], BIk, db, cudaMemcpyDefault, st));
+    // BRx, BRy, BIx, BIy -> P0..P3
+    const int ops[4] = {1, 2, 1, 2};
+    for (int k = 0; k < 4; ++k) {
+      k_dense_op<<<grid_for(tot), 256, 0, st>>>(g.n, g.kmax2, tot, ops[k], D[k < 2 ? 0 : 1], D[2]);
+      QG_LAUNCHED();
+      if ((rc = d_c2r(D[2], P[k], nz))) return rc;
+    }
+    // qwr = BRy*BIx - BRx*BIy
+    k_phys<T><<<grid_for(pt), 256, 0, st>>>(pt, 2, P[1], P[2], P[0], P[3], P[4]);
+    QG_LAUNCHED();
+    if ((rc = d_r2c(P[4], D[3], nz))) return rc;
+    if ((rc = d_c2r(D[0], P[0], nz)) || (rc = d_c2r(D[1], P[1], nz))) return rc;
+    k_phys<T><<<grid_for(pt), 256, 0, st>>>(pt, 1, P[0], P[1], nullptr, nullptr, P[4]);
+    QG_LAUNCHED();
+    if ((rc = d_r2c(P[4], D[4], nz))) return rc;
+    k_dense_qw<<<grid_for(tot), 256, 0, st>>>(g.n, g.kmax2, tot, D[3], D[4], cfg.Ro, cfg.W2F, D[5]);
+    QG_LAUNCHED();
+    QG_CK(cudaMemcpyAsync(qwk, D[5], db, cudaMemcpyDefault, st));
+    QG_CK(cudaStreamSynchronize(st));
+    return QG_OK;
+  }
+
+  int psi_solver(const double* qstar, double* psik) override {
+    int rc = ensure_tmp();
+    if (rc) return rc;
+    if ((rc = upload_compact(qstar, tmpF[0]))) return rc;
+    if ((rc = solve_generic(tmpF[0], nullptr, nullptr, tmpF[1], nullptr, nullptr, 1, 0))) return rc;
+    return download_compact(tmpF[1], psik, 0);
+  }
+
+  int A_solver(const double* bk, double* ak, double* ck) override {
+    int rc = ensure_tmp();
+    if (rc) return rc;
+    if ((rc = upload_compact(bk, tmpF[0]))) return rc;
+    if ((rc = solve_generic(nullptr, tmpF[0], tmpF[0], nullptr, tmpF[1], tmpF[2], 0, 1))) return rc;
+    if ((rc = download_compact(tmpF[1], ak, 0))) return rc;
+    if (ck) return download_compact(tmpF[1], ck, 1);
+    return QG_OK;
+  }
+
+ private:
+  qg_config cfg{};
+  Geom g{};
+  StepParams sp{};
+  cudaStream_t st = nullptr;
+  C* F[F_NINT] = {};
+  T *e1 = nullptr, *e2 = nullptr, *e1w = nullptr, *e2w = nullptr;
+  C* tw = nullptr;
+  int* tab_idx = nullptr;
+  double2 *fac_psi = nullptr, *fac_A = nullptr, *bscr = nullptr;
+  double *du = nullptr, *cu = nullptr, *cl = nullptr, *r2 = nullptr;
+  double *diag_part = nullptr, *diag_out = nullptr, *diag_host = nullptr;
+  C* S = nullptr;
+  int Zb = 1;
+  bool need_qw = true;
+  void* stage = nullptr; size_t stage_bytes = 0;
+  // dense drop-in buffers
+  int dense_nz = 0;
+  double2* D[6] = {};
+  T* P[5] = {};
+  C* W = nullptr;
+  double* dstage = nullptr;
+  C* tmpF[3] = {};
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+
+  void release() {
+    if (st) cudaStreamSynchronize(st);
+    for (auto& x : gexec) if (x) { cudaGraphExecDestroy(x); x = nullptr; }
+    for (auto& p : F) if (p) { cudaFree(p); p = nullptr; }
+    void* ps[] = {e1, e2, e1w, e2w, tw, tab_idx, fac_psi, fac_A, bscr, du, cu, cl, r2, diag_part, diag_out, S, stage,
+                  W, dstage};
+    for (void* p : ps) if (p) cudaFree(p);
+    for (auto& p : D) if (p) cudaFree(p);
+    for (auto& p : P) if (p) cudaFree(p);
+    for (auto& p : tmpF) if (p) cudaFree(p);
+    if (diag_host) cudaFreeHost(diag_host);
+    if (st) cudaStreamDestroy(st);
+    st = nullptr;
+  }
+
+  static unsigned grid_for(long long n) {
+    long long b = (n + 255) / 256;
+    return (unsigned)std::max<long long>(1, std::min<long long>(b, 152LL * 16));
+  }
+
+  int map_field(int field) const {
+    switch (field) {
+      case QG_Q: return F_Q; case QG_QOLD: return F_QO; case QG_BR: return F_BR; case QG_BI: return F_BI;
+      case QG_BROLD: return F_BRO; case QG_BIOLD: return F_BIO; case QG_PSI: return F_PSI;
+      case QG_AR: case QG_CR: return F_AR;
+      case QG_AI: case QG_CI: return F_AI;
+      case QG_QSTAR: return F_QSTAR;
+      default: return -1;
+    }
+  }
+
+  int ensure(void** p, size_t* have, size_t need) {
+    if (*have >= need) return QG_OK;
+    if (*p) { QG_CK(cudaStreamSynchronize(st)); cudaFree(*p); *p = nullptr; *have = 0; }
+    QG_CK(cudaMalloc(p, need));
+    *have = need;
+    return QG_OK;
+  }
+
+  // smem sizes per kernel
+  size_t sm_colinv() const { return (size_t)(g.n + 2 * Tile<T>::CT * (g.n + 1)) * sizeof(C); }
+  size_t sm_rowmain() const { return (size_t)(g.n + 12 * Tile<T>::RT * g.n) * sizeof(C); }
+  size_t sm_colupd() const { return (size_t)(g.n + 2 * Tile<T>::CT * (g.n + 1) + Tile<T>::CT * g.KY) * sizeof(C); }
+  size_t sm_rowqw() const { return (size_t)(g.n + 7 * Tile<T>::RT * g.n) * sizeof(C); }
+  size_t sm_drow() const { return (size_t)(3 * g.n) * sizeof(C); }
+
+  int set_smem_attrs() {
+    const int mx = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    QG_SWITCH_N(g.n, {
+      QG_CK(cudaFuncSetAttribute(k_col_inv<T, NN>, (cudaFuncAttribute)mx, (int)sm_colinv()));
+      QG_CK(cudaFuncSetAttribute(k_row_main<T, NN>, (cudaFuncAttribute)mx, (int)sm_rowmain()));
+      QG_CK(cudaFuncSetAttribute(k_col_update<T, NN>, (cudaFuncAttribute)mx, (int)sm_colupd()));
+      QG_CK(cudaFuncSetAttribute(k_row_qw<T, NN>, (cudaFuncAttribute)mx, (int)sm_rowqw()));
+      QG_CK(cudaFuncSetAttribute(k_col_qw<T, NN>, (cudaFuncAttribute)mx, (int)sm_colupd()));
+      QG_CK(cudaFuncSetAttribute(k_dcol_inv<T, NN>, (cudaFuncAttribute)mx, (int)sm_colinv()));
+      QG_CK(cudaFuncSetAttribute(k_dcol_fwd<T, NN>, (cudaFuncAttribute)mx, (int)sm_colinv()));
+      QG_CK(cudaFuncSetAttribute(k_drow_c2r<T, NN>, (cudaFuncAttribute)mx, (int)sm_drow()));
+      QG_CK(cudaFuncSetAttribute(k_drow_r2c<T, NN>, (cudaFuncAttribute)mx, (int)sm_drow()));
+    });
+    return QG_OK;
+  }
+
+  StateP<T> state_ptrs() {
+    StateP<T> p;
+    p.q = F[F_Q]; p.qo = F[F_QO]; p.BR = F[F_BR]; p.BI = F[F_BI]; p.BRo = F[F_BRO]; p.BIo = F[F_BIO];
+    p.psi = F[F_PSI]; p.AR = F[F_AR]; p.AI = F[F_AI]; p.qstar = F[F_QSTAR]; p.dq = F[F_DQ];
+    return p;
+  }
+
+  // Profiling: events around each launch when prof_on is set.
+  bool prof_on = false;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_ev;
+  int pbeg(int kind) {
+    if (!prof_on) return QG_OK;
+    cudaEvent_t a, b;
+    QG_CK(cudaEventCreate(&a)); QG_CK(cudaEventCreate(&b));
+    QG_CK(cudaEventRecord(a, st));
+    prof_ev.push_back({kind, {a, b}});
+    return QG_OK;
+  }
+  int pend() {
+    if (!prof_on) return QG_OK;
+    QG_CK(cudaEventRecord(prof_ev.back().second.second, st));
+    return QG_OK;
+  }
+
+ public:
+  int profile_step(int euler, double* ms, int* launches, int nclasses) override {
+    for (int i = 0; i < nclasses; ++i) { ms[i] = 0.0; launches[i] = 0; }
+    prof_on = true;
+    prof_ev.clear();
+    int rc = enqueue_step(euler ? 1 : 0);
+    prof_on = false;
+    cudaError_t e = cudaStreamSynchronize(st);
+    for (auto& pe : prof_ev) {
+      float t = 0.f;
+      if (rc == QG_OK && e == cudaSuccess && cudaEventElapsedTime(&t, pe.second.first, pe.second.second) == cudaSuccess &&
+          pe.first < nclasses) {
+        ms[pe.first] += t;
+        launches[pe.first] += 1;
+      }
+      cudaEventDestroy(pe.second.first);
+      cudaEventDestroy(pe.second.second);
+    }
+    prof_ev.clear();
+    if (rc) return rc;
+    QG_CK(e);
+    return QG_OK;
+  }
+
+ private:
+  // Enqueue one step on st (no synchronisation; graph-capturable).
+  int enqueue_step(int euler) {
+    StepParams s = sp;
+    s.euler = euler;
+    const int CT = Tile<T>::CT, RT = Tile<T>::RT;
+    if (s.use_dq) {
+      if (int rc0 = pbeg(QG_K_DISSIPATION)) return rc0;
+      k_dissipation<T><<<grid_for((long long)g.n3 * g.plane), 256, 0, st>>>(g, cfg.nuz, cfg.dz,
+                                                                              euler ? F[F_Q] : F[F_QO], F[F_DQ]);
+      QG_LAUNCHED();
+      if (int rc0 = pend()) return rc0;
+    }
+    StateP<T> sptr = state_ptrs();
+    for (int z0 = 0; z0 < g.n3; z0 += Zb) {
+      const int zc = std::min(Zb, g.n3 - z0);
+      const dim3 gc(g.KXP / CT, zc), gr(g.n / RT, zc);
+      QG_SWITCH_N(g.n, {
+        if (int rc0 = pbeg(QG_K_COL_INV)) return rc0;
+        k_col_inv<T, NN><<<gc, kThreads, sm_colinv(), st>>>(g, z0, F[F_PSI], F[F_Q], F[F_BR], F[F_BI], S, tw);
+        QG_LAUNCHED();
+        if (int rc0 = pend()) return rc0;
+        if (int rc0 = pbeg(QG_K_ROW_MAIN)) return rc0;
+        k_row_main<T, NN><<<gr, kThreads, sm_rowmain(), st>>>(g, s, S, tw);
+        QG_LAUNCHED();
+        if (int rc0 = pend()) return rc0;
+        if (int rc0 = pbeg(QG_K_COL_UPDATE)) return rc0;
+        k_col_update<T, NN><<<gc, kThreads, sm_colupd(), st>>>(g, s, z0, sptr, e1, e2, e1w, e2w, S, tw,
+                                                                need_qw ? 1 : 0);
+        QG_LAUNCHED();
+        if (int rc0 = pend()) return rc0;
+        if (need_qw) {
+          if (int rc0 = pbeg(QG_K_ROW_QW)) return rc0;
+          k_row_qw<T, NN><<<gr, kThreads, sm_rowqw(), st>>>(g, S, tw);
+          QG_LAUNCHED();
+          if (int rc0 = pend()) return rc0;
+          if (int rc0 = pbeg(QG_K_COL_QW)) return rc0;
+          k_col_qw<T, NN><<<gc, kThreads, sm_colupd(), st>>>(g, s, z0, F[F_Q], F[F_QSTAR], S, tw);
+          QG_LAUNCHED();
+          if (int rc0 = pend()) return rc0;
+        }
+      });
+    }
+    if (int rc0 = pbeg(QG_K_SOLVE)) return rc0;
+    int rc = launch_solve(need_qw ? F[F_QSTAR] : F[F_Q], cfg.fixed_flow ? 0 : 1, cfg.passive_scalar ? 0 : 1);
+    if (rc) return rc;
+    return pend();
+  }
+
+  int launch_solve(C* qs, int do_psi, int do_A) {
+    return solve_generic(qs, F[F_BR], F[F_BI], F[F_PSI], F[F_AR], F[F_AI], do_psi, do_A);
+  }
+
+  int solve_generic(const C* qs, const C* br, const C* bi, C* psi, C* ar, C* ai, int do_psi, int do_A) {
+    if (!do_psi && !do_A) return QG_OK;
+    k_solve<T><<<(unsigned)((g.plane + 127) / 128), 128, 0, st>>>(g, cfg.dz, cfg.Bu, tab_idx, fac_psi, fac_A, du, qs,
+                                                                  br, bi, psi, ar, ai, bscr, do_psi, do_A);
+    QG_LAUNCHED();
+    return QG_OK;
+  }
+
+  int run_step(int euler) {
+    if (!cfg.use_graphs) return enqueue_step(euler);
+    if (!gexec[euler]) {
+      cudaGraph_t graph = nullptr;
+      QG_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      int rc = enqueue_step(euler);
+      cudaError_t e = cudaStreamEndCapture(st, &graph);
+      if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
+      if (e != cudaSuccess) { err = std::string("graph capture: ") + cudaGetErrorString(e); return QG_ERR_CUDA; }
+      e = cudaGraphInstantiate(&gexec[euler], graph, 0);
+      cudaGraphDestroy(graph);
+      if (e != cudaSuccess) { err = std::string("graph instantiate: ") + cudaGetErrorString(e); return QG_ERR_CUDA; }
+    }
+    QG_CK(cudaGraphLaunch(gexec[euler], st));
+    return QG_OK;
+  }
+
+  // ---- dense drop-in plumbing ---------------------------------------------
+  size_t dense_bytes(int nz) const { return (size_t)nz * g.n * (g.n / 2 + 1) * sizeof(double2); }
+  int iktxP() const { const int ct = Tile<T>::CT; return ((g.n / 2 + 1 + ct - 1) / ct) * ct; }
+
+  int prep_dense(int nz) {
+    if (nz <= 0) { err = "nz must be positive"; return QG_ERR_ARG; }
+    if (nz <= dense_nz) return QG_OK;
+    QG_CK(cudaStreamSynchronize(st));
+    for (auto& p : D) if (p) { cudaFree(p); p = nullptr; }
+    for (auto& p : P) if (p) { cudaFree(p); p = nullptr; }
+    if (W) { cudaFree(W); W = nullptr; }
+    if (dstage) { cudaFree(dstage); dstage = nullptr; }
+    for (auto& p : D) QG_CK(cudaMalloc(&p, dense_bytes(nz)));
+    for (auto& p : P) QG_CK(cudaMalloc(&p, (size_t)nz * g.n * g.n * sizeof(T)));
+    QG_CK(cudaMalloc(&W, (size_t)nz * g.n * iktxP() * sizeof(C)));
+    QG_CK(cudaMalloc(&dstage, (size_t)nz * g.n * (g.n + 2) * sizeof(double)));
+    dense_nz = nz;
+    return QG_OK;
+  }
+
+  int d_c2r(const double2* spec, T* phys, int nz) {
+    const int CT = Tile<T>::CT;
+    QG_SWITCH_N(g.n, {
+      k_dcol_inv<T, NN><<<dim3(iktxP() / CT, nz), kThreads, sm_colinv(), st>>>(iktxP(), spec, W, tw);
+      QG_LAUNCHED();
+      k_drow_c2r<T, NN><<<dim3(g.n / 2, nz), kThreads, sm_drow(), st>>>(iktxP(), W, phys, tw);
+      QG_LAUNCHED();
+    });
+    return QG_OK;
+  }
+
+  int d_r2c(const T* phys, double2* spec, int nz) {
+    const int CT = Tile<T>::CT;
+    QG_SWITCH_N(g.n, {
+      k_drow_r2c<T, NN><<<dim3(g.n / 2, nz), kThreads, sm_drow(), st>>>(iktxP(), phys, W, tw);
+      QG_LAUNCHED();
+      k_dcol_fwd<T, NN><<<dim3(iktxP() / CT, nz), kThreads, sm_colinv(), st>>>(iktxP(), W, spec, tw);
+      QG_LAUNCHED();
+    });
+    return QG_OK;
+  }
+
+  int ensure_tmp() {
+    const size_t fbytes = (size_t)g.n3 * g.plane * sizeof(C);
+    for (auto& p : tmpF) if (!p) { QG_CK(cudaMalloc(&p, fbytes)); QG_CK(cudaMemsetAsync(p, 0, fbytes, st)); }
+    return QG_OK;
+  }
+
+  int upload_compact(const double* kvar, C* dst) {
+    const size_t bytes = dense_bytes(g.n3);
+    int rc = ensure(&stage, &stage_bytes, bytes);
+    if (rc) return rc;
+    QG_CK(cudaMemcpyAsync(stage, kvar, bytes, cudaMemcpyDefault, st));
+    k_dense_to_compact<T><<<grid_for((long long)g.n3 * g.plane), 256, 0, st>>>(g, 0, g.n3, (const double2*)stage, dst);
+    QG_LAUNCHED();
+    return QG_OK;
+  }
+
+  int download_compact(const C* src, double* kvar, int mode) {
+    const size_t bytes = dense_bytes(g.n3);
+    int rc = ensure(&stage, &stage_bytes, bytes);
+    if (rc) return rc;
+    k_compact_to_dense<T><<<grid_for((long long)g.n3 * g.n * (g.n / 2 + 1)), 256, 0, st>>>(g, 0, g.n3, src,
+                                                                                           (double2*)stage, mode, cfg.dz);
+    QG_LAUNCHED();
+    QG_CK(cudaMemcpyAsync(kvar, stage, bytes, cudaMemcpyDefault, st));
+    QG_CK(cudaStreamSynchronize(st));
+    return QG_OK;
+  }
+};
+
+}  // namespace qg

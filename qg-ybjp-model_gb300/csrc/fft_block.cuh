@@ -1,0 +1,123 @@
+// Batched power-of-two FFTs held in shared memory, executed by a whole CTA.
+//
+// Stockham autosort, decimation in time, radices 8/4/2: pass p with radix R
+// reads x[j + r*N/R], twiddles by W_{Ns*R}^{(j mod Ns) r}, does a length-R DFT
+// in registers and writes y[(j - j mod Ns)*R + j mod Ns + r*Ns]; Ns is the
+// product of the radices of the earlier passes.  Forward uses
+// W_M = exp(-2 pi i/M) (FFTW_FORWARD); backward uses the conjugate and is
+// unnormalised (FFTW_BACKWARD), so backward(forward(x)) = N x.
+#pragma once
+#include "common.cuh"
+
+namespace qg {
+
+template <typename T, bool FWD> struct Dft;
+
+// forward: multiply by W8^1 = (1-i)/sqrt2, W8^3 = (-1-i)/sqrt2 ; backward: conjugates
+template <typename T, bool FWD>
+__device__ __forceinline__ void dft2(cplx<T>& a, cplx<T>& b) {
+  cplx<T> t = a; a = cadd(t, b); b = csub(t, b);
+}
+
+template <typename T, bool FWD>
+__device__ __forceinline__ cplx<T> mul_w4(cplx<T> a) {  // * W4^1 (fwd -i, bwd +i)
+  return FWD ? cmul_mi(a) : cmul_i(a);
+}
+
+template <typename T, bool FWD>
+__device__ __forceinline__ void dft4(cplx<T>* v) {
+  cplx<T> s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+  cplx<T> s13 = cadd(v[1], v[3]), d13 = mul_w4<T, FWD>(csub(v[1], v[3]));
+  v[0] = cadd(s02, s13);
+  v[2] = csub(s02, s13);
+  v[1] = cadd(d02, d13);
+  v[3] = csub(d02, d13);
+}
+
+template <typename T, bool FWD>
+__device__ __forceinline__ void dft8(cplx<T>* v) {
+  const T h = (T)0.70710678118654752440084436210485;
+  cplx<T> a[4], b[4];
+#pragma unroll
+  for (int n = 0; n < 4; ++n) { a[n] = cadd(v[n], v[n + 4]); b[n] = csub(v[n], v[n + 4]); }
+  // b[n] *= W8^n
+  {
+    cplx<T> t = b[1];
+    if (FWD) { b[1].x = (t.x + t.y) * h; b[1].y = (t.y - t.x) * h; }
+    else     { b[1].x = (t.x - t.y) * h; b[1].y = (t.y + t.x) * h; }
+    b[2] = mul_w4<T, FWD>(b[2]);
+    t = b[3];
+    if (FWD) { b[3].x = (t.y - t.x) * h; b[3].y = -(t.x + t.y) * h; }
+    else     { b[3].x = -(t.x + t.y) * h; b[3].y = (t.x - t.y) * h; }
+  }
+  dft4<T, FWD>(a);
+  dft4<T, FWD>(b);
+  v[0] = a[0]; v[2] = a[1]; v[4] = a[2]; v[6] = a[3];
+  v[1] = b[0]; v[3] = b[1]; v[5] = b[2]; v[7] = b[3];
+}
+
+template <typename T, int R, bool FWD>
+__device__ __forceinline__ void dftR(cplx<T>* v) {
+  if constexpr (R == 8) dft8<T, FWD>(v);
+  else if constexpr (R == 4) dft4<T, FWD>(v);
+  else dft2<T, FWD>(v[0], v[1]);
+}
+
+template <int REM> struct PassRadix { static constexpr int value = REM >= 8 ? 8 : (REM >= 4 ? 4 : 2); };
+
+// One Stockham pass over `batch` transforms of length N stored with leading
+// dimension ld; tw[m] = W_N^m (forward sign).
+template <typename T, int N, int R, int NS, bool FWD>
+__device__ __forceinline__ void stockham_pass(const cplx<T>* __restrict__ src, cplx<T>* __restrict__ dst,
+                                              int ld, int batch, const cplx<T>* __restrict__ tw) {
+  constexpr int NB = N / R;
+  const int total = batch * NB;
+  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+    const int b = t / NB;
+    const int j = t - b * NB;
+    const cplx<T>* s = src + (long)b * ld;
+    cplx<T>* d = dst + (long)b * ld;
+    cplx<T> v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = s[j + r * NB];
+    const int k = j & (NS - 1);
+    if constexpr (NS > 1) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        cplx<T> w = tw[k * r * (N / (NS * R))];
+        if (!FWD) w.y = -w.y;
+        v[r] = cmul(v[r], w);
+      }
+    }
+    dftR<T, R, FWD>(v);
+    const int base = (j - k) * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) d[base + r * NS] = v[r];
+  }
+}
+
+template <typename T, int N, bool FWD, int NS>
+__device__ __forceinline__ cplx<T>* fft_passes(cplx<T>* a, cplx<T>* b, int ld, int batch, const cplx<T>* tw) {
+  if constexpr (NS >= N) {
+    return a;
+  } else {
+    constexpr int R = PassRadix<N / NS>::value;
+    stockham_pass<T, N, R, NS, FWD>(a, b, ld, batch, tw);
+    __syncthreads();
+    return fft_passes<T, N, FWD, NS * R>(b, a, ld, batch, tw);
+  }
+}
+
+// All threads of the CTA must call.  Input in `a`, `b` is scratch of the same
+// size; returns the buffer that holds the result.  Ends with __syncthreads().
+template <typename T, int N, bool FWD>
+__device__ __forceinline__ cplx<T>* block_fft(cplx<T>* a, cplx<T>* b, int ld, int batch, const cplx<T>* tw) {
+  return fft_passes<T, N, FWD, 1>(a, b, ld, batch, tw);
+}
+
+template <typename T, int N>
+__device__ __forceinline__ void load_twiddles(cplx<T>* tw_s, const cplx<T>* __restrict__ tw_g) {
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw_s[i] = tw_g[i];
+}
+
+}  // namespace qg

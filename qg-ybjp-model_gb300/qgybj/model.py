@@ -1,0 +1,191 @@
+"""Host-side mirror of the reference's use of its step routines.
+
+``Simulation`` owns one library handle and exposes the routines of the
+reference under their Fortran names (fft_r2c, fft_c2r, convol_waqg,
+refraction_waqg, compute_qw, psi_solver, A_solver_ybj_plus, sumB/init_q via
+init_state) with numpy arrays in the reference's memory layout, plus the
+resident-state interface (set_state/get_state/step) that replaces the time
+loop of main_waqg.f90.  Status codes other than QG_OK raise QgError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import FIELDS, QG_PREC_FP64, QG_PREC_MIXED, QgConfig, QgEnergy, check, lib, ptr
+from .config import RunConfig, make_initial_condition, model_parameters
+
+
+def _arr(a, n3=None):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Simulation:
+    def __init__(self, params: dict, precision: str = "fp64", device: int = 0, levels_per_batch: int = 0,
+                 use_graphs: int = 1, flags: dict | None = None):
+        L = lib()
+        cfg = QgConfig()
+        check(L.qg_config_defaults(C.byref(cfg)))
+        self.n, self.n3 = int(params["n1"]), int(params["n3"])
+        cfg.n1, cfg.n2, cfg.n3 = int(params["n1"]), int(params["n2"]), int(params["n3"])
+        cfg.precision = QG_PREC_FP64 if precision == "fp64" else QG_PREC_MIXED
+        cfg.device = device
+        for k in ("dz", "Bu", "Ro", "W2F", "delt", "gamma", "nuh1", "nuh2", "nuh1w", "nuh2w", "nuz"):
+            setattr(cfg, k, float(params.get(k, 0.0)))
+        for k in ("ilap1", "ilap2", "ilap1w", "ilap2w"):
+            setattr(cfg, k, int(params.get(k, 2)))
+        for k, v in (flags or {}).items():
+            setattr(cfg, k, int(v))
+        self._keep = []
+        for k in ("a_ell_ut", "rho_ut", "rho_st", "r_2ut"):
+            v = params.get(k)
+            if v is not None:
+                a = np.ascontiguousarray(v, dtype=np.float64)
+                self._keep.append(a)
+                setattr(cfg, k, a.ctypes.data_as(C.POINTER(C.c_double)))
+        cfg.levels_per_batch = levels_per_batch
+        cfg.use_graphs = use_graphs
+        self.cfg = cfg
+        h = C.c_void_p()
+        check(L.qg_create(C.byref(cfg), C.byref(h)))
+        self.h = h
+        self.precision = precision
+
+    # -- lifecycle -------------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            lib().qg_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, st):
+        check(st, self.h)
+
+    @property
+    def spectral_shape(self):
+        return (self.n3, self.n, self.n // 2 + 1)
+
+    # -- resident state ----------------------------------------------------------
+    def set_state(self, name: str, kvar, level0: int = 0):
+        if isinstance(kvar, np.ndarray):
+            kvar = np.ascontiguousarray(kvar, dtype=np.complex128)
+            nlev = kvar.shape[0]
+        else:
+            nlev = kvar.shape[0]
+        self._ck(lib().qg_set_state(self.h, FIELDS[name], ptr(kvar), level0, nlev))
+
+    def get_state(self, name: str, level0: int = 0, nlev: int | None = None, out=None):
+        nlev = self.n3 - level0 if nlev is None else nlev
+        if out is None:
+            out = np.empty((nlev, self.n, self.n // 2 + 1), dtype=np.complex128)
+        self._ck(lib().qg_get_state(self.h, FIELDS[name], ptr(out), level0, nlev))
+        return out
+
+    def init_state(self, apply_sumB: bool = True, q_from_psi: bool = True):
+        self._ck(lib().qg_init_state(self.h, int(apply_sumB), int(q_from_psi)))
+
+    def step(self, euler_first: bool = False):
+        self._ck(lib().qg_step(self.h, int(euler_first)))
+
+    def steps_async(self, nsteps: int, euler_first: bool = False):
+        self._ck(lib().qg_steps_async(self.h, int(nsteps), int(euler_first)))
+
+    def synchronize(self):
+        self._ck(lib().qg_synchronize(self.h))
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._ck(lib().qg_get_stream(self.h, C.byref(s)))
+        return int(s.value or 0)
+
+    def diagnostics_fp64(self) -> dict:
+        e = QgEnergy()
+        self._ck(lib().qg_diagnostics_fp64(self.h, C.byref(e)))
+        return {k: getattr(e, k) for k, _ in QgEnergy._fields_}
+
+    def profile_step(self, euler_first: bool = False) -> dict:
+        """One step with CUDA events around each launch: {class: (ms, launches)}."""
+        from ._lib import KERNEL_CLASSES
+        n = len(KERNEL_CLASSES)
+        ms = (C.c_double * n)()
+        cnt = (C.c_int * n)()
+        self._ck(lib().qg_profile_step(self.h, int(euler_first), ms, cnt, n))
+        return {k: (ms[i], cnt[i]) for i, k in enumerate(KERNEL_CLASSES)}
+
+    # -- routine-level drop-ins --------------------------------------------------
+    def fft_r2c(self, rvar: np.ndarray) -> np.ndarray:
+        rvar = np.ascontiguousarray(rvar, dtype=np.float64)
+        nz = rvar.shape[0]
+        assert rvar.shape[1:] == (self.n, self.n + 2)
+        out = np.empty((nz, self.n, self.n // 2 + 1), dtype=np.complex128)
+        self._ck(lib().qg_fft_r2c(self.h, ptr(rvar), ptr(out), nz))
+        return out
+
+    def fft_c2r(self, kvar: np.ndarray) -> np.ndarray:
+        kvar = np.ascontiguousarray(kvar, dtype=np.complex128)
+        nz = kvar.shape[0]
+        out = np.empty((nz, self.n, self.n + 2), dtype=np.float64)
+        self._ck(lib().qg_fft_c2r(self.h, ptr(kvar), ptr(out), nz))
+        return out
+
+    def _c(self, a):
+        return np.ascontiguousarray(a, dtype=np.complex128)
+
+    def convol_waqg(self, uk, vk, qk, BRk, BIk):
+        ins = [self._c(a) for a in (uk, vk, qk, BRk, BIk)]
+        nz = ins[0].shape[0]
+        outs = [np.empty_like(ins[0]) for _ in range(3)]
+        self._ck(lib().qg_convol_waqg(self.h, *[ptr(a) for a in ins], *[ptr(a) for a in outs], nz))
+        return tuple(outs)
+
+    def refraction_waqg(self, BRk, BIk, psik):
+        ins = [self._c(a) for a in (BRk, BIk, psik)]
+        nz = ins[0].shape[0]
+        outs = [np.empty_like(ins[0]) for _ in range(2)]
+        self._ck(lib().qg_refraction_waqg(self.h, *[ptr(a) for a in ins], *[ptr(a) for a in outs], nz))
+        return tuple(outs)
+
+    def compute_qw(self, BRk, BIk):
+        ins = [self._c(a) for a in (BRk, BIk)]
+        out = np.empty_like(ins[0])
+        self._ck(lib().qg_compute_qw(self.h, ptr(ins[0]), ptr(ins[1]), ptr(out), ins[0].shape[0]))
+        return out
+
+    def psi_solver(self, qstar):
+        q = self._c(qstar)
+        out = np.empty_like(q)
+        self._ck(lib().qg_psi_solver(self.h, ptr(q), ptr(out)))
+        return out
+
+    def A_solver_ybj_plus(self, bk):
+        b = self._c(bk)
+        a, c = np.empty_like(b), np.empty_like(b)
+        self._ck(lib().qg_A_solver_ybj_plus(self.h, ptr(b), ptr(a), ptr(c)))
+        return a, c
+
+
+def simulation_for(rc: RunConfig, device: int = 0, precision: str | None = None):
+    """Handle and initial condition of a run configuration: the
+    initialisation of main_waqg.f90:117-147 with the seeded generator in
+    place of generate_fields_stag / ncread_*."""
+    ic = make_initial_condition(rc)
+    params = model_parameters(rc, ic.delt)
+    sim = Simulation(params, precision or rc.precision, device=device, levels_per_batch=rc.levels_per_batch,
+                     use_graphs=rc.use_graphs)
+    sim.set_state("psi", ic.psi)
+    sim.set_state("BR", ic.BR)
+    sim.set_state("BI", ic.BI)
+    sim.init_state(apply_sumB=True, q_from_psi=True)
+    return sim, ic, params

@@ -1,0 +1,246 @@
+"""CUDA path vs the FP64 oracle, through the C-ABI (libqgybj.so).
+
+Tolerances (relative L2 per field):
+  FP64 path: 1e-12 (1e-11 for the exponential-stratification inversions,
+             whose condition number is ~1e5 larger);
+  mixed path (FP32 transforms/update, FP64 solves): 1e-5 after 100 steps,
+             2e-6 for single routine calls.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle import qgybj_oracle as orc
+from qgybj import Simulation
+from qgybj._lib import QG_ERR_ARG, QG_ERR_NONFINITE, QG_ERR_PIVOT, QG_ERR_UNSUPPORTED, QgError
+from qgybj.config import CONFIGS, make_initial_condition, model_parameters, scaled
+from tests.helpers import oracle_params, random_masked, random_physical, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp64": 1e-12, "mixed": 2e-6}
+FIELDS = ("q", "qo", "BR", "BI", "BRo", "BIo", "psi", "AR", "AI")
+
+
+def pair(rc, precision, flags=None, **kw):
+    flags = flags or {}
+    ic = make_initial_condition(rc)
+    params = model_parameters(rc, ic.delt)
+    if "nuz" in flags:
+        params["nuz"] = flags.pop("nuz")
+    model = orc.Model(oracle_params(params, **flags))
+    st = orc.initial_state(model, ic.psi, ic.BR, ic.BI)
+    sim = Simulation(params, precision, flags=flags, **kw)
+    sim.set_state("psi", ic.psi)
+    sim.set_state("BR", ic.BR)
+    sim.set_state("BI", ic.BI)
+    sim.init_state(True, True)
+    return model, st, sim
+
+
+def compare(sim, st, tol, fields=FIELDS):
+    errs = {f: rel_l2(sim.get_state(f), getattr(st, f)) for f in fields}
+    bad = {f: e for f, e in errs.items() if not e <= tol}
+    assert not bad, f"fields above {tol}: {bad} (all: {errs})"
+    return errs
+
+
+# --- transforms ------------------------------------------------------------------
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("n", [16, 64, 256])
+def test_fft_dropins(precision, n):
+    rc = scaled(CONFIGS["c0"], n, 4)
+    model, st, sim = pair(rc, precision)
+    r = random_physical(n, 3, 1)
+    rp = np.zeros((3, n, n + 2)); rp[:, :, :n] = r
+    k = sim.fft_r2c(rp)
+    assert rel_l2(k, model.fft_r2c(r)) < TOL[precision]
+    spec = random_masked(n, 3, 2, masked=False)        # unmasked, Nyquist row included
+    back = sim.fft_c2r(spec)
+    ref = model.fft_c2r(spec)
+    assert rel_l2(back[:, :, :n], ref) < TOL[precision]
+    assert np.abs(back[:, :, n:]).max() == 0
+    sim.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_transform_method_dropins(precision):
+    n, nz = 64, 3
+    rc = scaled(CONFIGS["c0"], n, 4)
+    model, st, sim = pair(rc, precision)
+    psi = random_masked(n, nz, 3); psi[:, 0, 0] = 0
+    q = random_masked(n, nz, 4)
+    BR, BI = random_masked(n, nz, 5, masked=False), random_masked(n, nz, 6, masked=False)
+    uk, vk = model.compute_velo(psi)
+    got = sim.convol_waqg(uk, vk, q, BR, BI)
+    exp = model.convol_waqg(uk, vk, q, BR, BI)
+    for a, b in zip(got, exp):
+        assert rel_l2(a, b) < TOL[precision]
+    got = sim.refraction_waqg(BR, BI, psi)
+    exp = model.refraction_waqg(BR, BI, psi)
+    for a, b in zip(got, exp):
+        assert rel_l2(a, b) < TOL[precision]
+    assert rel_l2(sim.compute_qw(BR, BI), model.compute_qw(BR, BI)) < TOL[precision]
+    sim.close()
+
+
+@pytest.mark.parametrize("strat", ["c0", "c1"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_solver_dropins(strat, precision):
+    rc = scaled(CONFIGS[strat], 64, 32)
+    model, st, sim = pair(rc, precision)
+    q = random_masked(64, 32, 7)
+    tol = (1e-12 if strat == "c0" else 1e-11) if precision == "fp64" else 2e-6
+    assert rel_l2(sim.psi_solver(q), model.psi_solver(q)) < tol
+    A, Cz = sim.A_solver_ybj_plus(q)
+    Ae, Ce = model.A_solver_ybj_plus(q)
+    assert rel_l2(A, Ae) < tol and rel_l2(Cz, Ce) < tol
+    sim.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_init_state(precision):
+    rc = scaled(CONFIGS["c1"], 32, 16)
+    model, st, sim = pair(rc, precision)
+    tol = 1e-11 if precision == "fp64" else 2e-6
+    compare(sim, st, tol, FIELDS + ("CR", "CI"))
+    sim.close()
+
+
+# --- full steps -----------------------------------------------------------------
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_steps_small(precision):
+    rc = scaled(CONFIGS["c0"], 32, 16)
+    model, st, sim = pair(rc, precision)
+    sim.step(euler_first=True)
+    st = model.step(st, True)
+    for _ in range(9):
+        sim.step(False)
+        st = model.step(st, False)
+    compare(sim, st, 1e-12 if precision == "fp64" else 1e-5)
+    got = sim.diagnostics_fp64()
+    exp = model.diagnostics(st)
+    for k, v in exp.items():
+        assert abs(got[k] - v) <= (1e-12 if precision == "fp64" else 1e-5) * abs(v) + 1e-300, k
+    sim.close()
+
+
+def test_c0_fp64_200_steps():
+    """64^2 x 64, FP64, 200 leapfrog steps: relative L2 <= 1e-12 per field."""
+    rc = CONFIGS["c0"]
+    model, st, sim = pair(rc, "fp64")
+    sim.step(True)
+    sim.steps_async(rc.steps - 1, False)
+    sim.synchronize()
+    st = model.run(st, rc.steps, first=True)
+    compare(sim, st, 1e-12)
+    sim.close()
+
+
+def test_c0_mixed_100_steps():
+    rc = CONFIGS["c0"]
+    model, st, sim = pair(rc, "mixed")
+    sim.steps_async(100, True)
+    sim.synchronize()
+    st = model.run(st, 100, first=True)
+    compare(sim, st, 1e-5)
+    sim.close()
+
+
+@pytest.mark.parametrize("flags", [
+    {"linear": 1}, {"no_feedback": 1}, {"fixed_flow": 1}, {"passive_scalar": 1}, {"no_dispersion": 1},
+    {"inviscid": 0, "nuz": 3e-4},
+])
+def test_physics_switches(flags):
+    rc = scaled(CONFIGS["c0"], 32, 8)
+    model, st, sim = pair(rc, "fp64", dict(flags))
+    st = model.run(st, 4, first=True)
+    sim.steps_async(4, True)
+    sim.synchronize()
+    compare(sim, st, 1e-12)
+    sim.close()
+
+
+def test_batching_and_graphs_are_bitwise_invariant():
+    rc = scaled(CONFIGS["c1"], 64, 12)
+    outs = []
+    for lpb, graphs in ((0, 1), (1, 0), (5, 1)):
+        model, st, sim = pair(rc, "mixed", levels_per_batch=lpb, use_graphs=graphs)
+        sim.steps_async(3, True)
+        sim.synchronize()
+        outs.append([sim.get_state(f) for f in FIELDS])
+        sim.close()
+    for o in outs[1:]:
+        for a, b in zip(outs[0], o):
+            assert np.array_equal(a, b)
+
+
+# --- full sizes -----------------------------------------------------------------
+def test_c1_fp64_full_size_two_steps():
+    rc = CONFIGS["c1"]
+    orc.set_workers(16)
+    model, st, sim = pair(rc, "fp64")
+    sim.steps_async(2, True)
+    sim.synchronize()
+    st = model.run(st, 2, first=True)
+    compare(sim, st, 1e-11)
+    sim.close()
+    orc.set_workers(1)
+
+
+def test_c2_mixed_full_size_vs_fp64_gpu_100_steps():
+    """512^2 x 256: the mixed path after 100 steps against the FP64 GPU path
+    (itself checked against the oracle above), per-field relative L2 <= 1e-5."""
+    rc = CONFIGS["c2"]
+    ic = make_initial_condition(rc)
+    params = model_parameters(rc, ic.delt)
+    res = {}
+    for prec in ("fp64", "mixed"):
+        sim = Simulation(params, prec)
+        sim.set_state("psi", ic.psi); sim.set_state("BR", ic.BR); sim.set_state("BI", ic.BI)
+        sim.init_state(True, True)
+        sim.steps_async(rc.steps, True)
+        sim.synchronize()
+        res[prec] = {f: sim.get_state(f) for f in ("q", "psi", "BR", "BI", "AR", "AI")}
+        sim.close()
+    errs = {f: rel_l2(res["mixed"][f], res["fp64"][f]) for f in res["fp64"]}
+    assert all(e <= 1e-5 for e in errs.values()), errs
+    for f, a in res["mixed"].items():
+        assert np.isfinite(a).all()
+
+
+# --- error statuses ---------------------------------------------------------------
+def _params(n=32, n3=8):
+    rc = scaled(CONFIGS["c0"], n, n3)
+    ic = make_initial_condition(rc)
+    return model_parameters(rc, ic.delt)
+
+
+def test_error_statuses():
+    p = _params()
+    with pytest.raises(QgError) as e:
+        Simulation(dict(p, n2=64), "fp64")
+    assert e.value.status == QG_ERR_UNSUPPORTED
+    with pytest.raises(QgError) as e:
+        Simulation(dict(p, n1=48, n2=48), "fp64")
+    assert e.value.status == QG_ERR_UNSUPPORTED
+    with pytest.raises(QgError) as e:
+        Simulation(dict(p, delt=float("nan")), "fp64")
+    assert e.value.status == QG_ERR_NONFINITE
+    with pytest.raises(QgError) as e:
+        Simulation(dict(p, a_ell_ut=-np.ones(8)), "fp64")
+    assert e.value.status == QG_ERR_PIVOT
+    with pytest.raises(QgError) as e:
+        Simulation(p, "fp64", flags={"ybj_plus": 0})
+    assert e.value.status == QG_ERR_UNSUPPORTED
+    sim = Simulation(p, "fp64")
+    with pytest.raises(QgError) as e:
+        sim.set_state("CR", np.zeros((8, 32, 17), complex))
+    assert e.value.status == QG_ERR_ARG
+    with pytest.raises(QgError) as e:
+        sim.set_state("q", np.zeros((9, 32, 17), complex))
+    assert e.value.status == QG_ERR_ARG
+    # a valid call after errors still works
+    sim.step(True)
+    sim.close()
