@@ -179,7 +179,7 @@ def run_ours(args, world, rank, local):
 
     dist = dist_setup(world, "nccl")
     torch.cuda.set_device(local)
-    rc = CONFIGS[args.config]
+    rc = workload(args)
     precision = args.precision or rc.precision
     ic = make_initial_condition(rc)
     params = model_parameters(rc, ic.delt)
@@ -306,6 +306,16 @@ def run_ours(args, world, rank, local):
     return out
 
 
+def workload(args):
+    """The run configuration timed: a named configuration, optionally at
+    another resolution (--n/--n3, used for small profiling cases)."""
+    from qgybj.config import CONFIGS, scaled
+    rc = CONFIGS[args.config]
+    if args.n or args.n3:
+        rc = scaled(rc, args.n or rc.n, args.n3 or rc.n3)
+    return rc
+
+
 def sim_batch(sim) -> int:
     """Levels per phase-A batch as chosen by the library (same rule)."""
     from qgybj.config import kmax
@@ -345,8 +355,7 @@ def cpu_oracle_rate(rc, nz: int, steps: int, warm: int, workers: int):
 def run_reference(args, world, rank, local):
     if rank != 0:
         return None
-    from qgybj.config import CONFIGS
-    rc = CONFIGS[args.config]
+    rc = workload(args)
     workers = os.cpu_count() or 1
     # calibrate the slab depth so that the whole run stays within ~2 minutes
     rate, _ = cpu_oracle_rate(rc, 2, 1, 0, workers)
@@ -375,6 +384,8 @@ def main(argv=None):
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--config", default="c2")
     ap.add_argument("--precision", default=None)
+    ap.add_argument("--n", type=int, default=0, help="override n1 = n2 (profiling cases)")
+    ap.add_argument("--n3", type=int, default=0, help="override n3 (profiling cases)")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--fp64-steps", type=int, default=10)
     ap.add_argument("--no-e2e", action="store_true")
@@ -391,8 +402,7 @@ def main(argv=None):
     else:
         out = run_ours(args, world, rank, local)
         if out is not None and world == 1 and not args.no_cpu_baseline:
-            from qgybj.config import CONFIGS
-            rc = CONFIGS[args.config]
+            rc = workload(args)
             workers = os.cpu_count() or 1
             v, secs = cpu_oracle_rate(rc, args.cpu_baseline_levels, 2, 0, workers)
             out["cpu_baseline"] = {

@@ -121,6 +121,7 @@ int qg_get_state(qg_handle* h, int field, double* kvar, int level0, int nlev);
  * optional sumB (derivatives.f90:1073-1118), q = init_q(psi) (init.f90:591),
  * old levels = current levels, and A = A_solver_ybj_plus(B). */
 int qg_init_state(qg_handle* h, int apply_sumB, int q_from_psi);
+/* With fixed_flow = 1, q is set to 0 instead (main_waqg.f90:141-146). */
 
 /* One full time step on the device: main_waqg.f90:202-317 (euler_first=1,
  * forward Euler) or 331-467 (leapfrog + Robert-Asselin filter). */

@@ -20,7 +20,10 @@ LIB = OUTDIR / "libqgybj.so"
 
 UNITS = ["capi", "engine_fp32", "engine_fp64"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(INCLUDE)]
+# host code: no floating-point contraction, so the host-built tables (DGTSV
+# factors, integrating factors) round identically on x86-64 and aarch64
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+              "-I", str(INCLUDE)]
 
 
 def _nvcc() -> str:

@@ -153,6 +153,8 @@ int build_tables(const qg_config& c, qg::HostTables& t, std::string& err) {
   t.fac_psi.assign((size_t)nd * n3 * 2, 0.0);
   t.fac_A.assign((size_t)nd * n3 * 2, 0.0);
   std::vector<double> d(n3), dl(n3), du(n3);
+  // FP64 path: {f_i, d'_i} for DGTSV's exact arithmetic; mixed path: {f_i, 1/d'_i}
+  const bool exact = c.precision == QG_PREC_FP64;
   for (auto& kv : idx) {
     for (int op = 0; op < 2; ++op) {
       const double kdz = op == 0 ? (double)kv.first * c.dz * c.dz : (double)kv.first * c.dz * c.dz / 4.0;
@@ -180,12 +182,12 @@ int build_tables(const qg_config& c, qg::HostTables& t, std::string& err) {
         }
         const double f = dl[i] / dp;
         out[2 * i] = f;
-        out[2 * i + 1] = 1.0 / dp;
+        out[2 * i + 1] = exact ? dp : 1.0 / dp;
         dp = d[i + 1] - f * du[i];
       }
       if (dp == 0.0 || !std::isfinite(dp)) { err = "zero pivot in tridiagonal factorisation"; return QG_ERR_PIVOT; }
       out[2 * (n3 - 1)] = 0.0;
-      out[2 * (n3 - 1) + 1] = 1.0 / dp;
+      out[2 * (n3 - 1) + 1] = exact ? dp : 1.0 / dp;
     }
   }
   return QG_OK;

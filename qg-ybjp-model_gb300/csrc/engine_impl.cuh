@@ -128,6 +128,14 @@ class Engine final : public EngineBase {
     QG_CK(cudaMemcpyAsync(stage, kvar, bytes, cudaMemcpyDefault, st));
     k_dense_to_compact<T><<<grid_for((long long)nlev * g.plane), 256, 0, st>>>(g, level0, nlev, (const double2*)stage, F[f]);
     QG_LAUNCHED();
+    if (f == F_PSI && sizeof(T) == 4) {
+      // mixed path: keep psi in FP64 until qg_init_state has built q from it
+      // (init_q's vertical second difference would amplify FP32 rounding)
+      if (!psi64) QG_CK(cudaMalloc(&psi64, (size_t)g.n3 * g.plane * sizeof(double2)));
+      k_dense_to_compact<double><<<grid_for((long long)nlev * g.plane), 256, 0, st>>>(g, level0, nlev,
+                                                                                      (const double2*)stage, psi64);
+      QG_LAUNCHED();
+    }
     QG_CK(cudaStreamSynchronize(st));
     return QG_OK;
   }
@@ -154,8 +162,15 @@ class Engine final : public EngineBase {
       k_sumB<T><<<(unsigned)((g.plane + 127) / 128), 128, 0, st>>>(g, F[F_BR], F[F_BI]);
       QG_LAUNCHED();
     }
-    if (q_from_psi) {
-      k_init_q<T><<<grid_for((long long)g.n3 * g.plane), 256, 0, st>>>(g, cfg.dz, cu, cl, F[F_PSI], F[F_Q]);
+    if (cfg.fixed_flow) {
+      // fixed flow: q = 0 for all times (main_waqg.f90:141-146)
+      QG_CK(cudaMemsetAsync(F[F_Q], 0, (size_t)g.n3 * g.plane * sizeof(C), st));
+    } else if (q_from_psi) {
+      if (psi64) {
+        k_init_q<T, double><<<grid_for((long long)g.n3 * g.plane), 256, 0, st>>>(g, cfg.dz, cu, cl, psi64, F[F_Q]);
+      } else {
+        k_init_q<T, T><<<grid_for((long long)g.n3 * g.plane), 256, 0, st>>>(g, cfg.dz, cu, cl, F[F_PSI], F[F_Q]);
+      }
       QG_LAUNCHED();
     }
     const size_t fbytes = (size_t)g.n3 * g.plane * sizeof(C);
@@ -167,6 +182,7 @@ class Engine final : public EngineBase {
       if (rc) return rc;
     }
     QG_CK(cudaStreamSynchronize(st));
+    if (psi64) { cudaFree(psi64); psi64 = nullptr; }
     return QG_OK;
   }
 
@@ -339,6 +355,7 @@ class Engine final : public EngineBase {
   double *du = nullptr, *cu = nullptr, *cl = nullptr, *r2 = nullptr;
   double *diag_part = nullptr, *diag_out = nullptr, *diag_host = nullptr;
   C* S = nullptr;
+  double2* psi64 = nullptr;
   int Zb = 1;
   bool need_qw = true;
   void* stage = nullptr; size_t stage_bytes = 0;
@@ -356,7 +373,7 @@ class Engine final : public EngineBase {
     for (auto& x : gexec) if (x) { cudaGraphExecDestroy(x); x = nullptr; }
     for (auto& p : F) if (p) { cudaFree(p); p = nullptr; }
     void* ps[] = {e1, e2, e1w, e2w, tw, tab_idx, fac_psi, fac_A, bscr, du, cu, cl, r2, diag_part, diag_out, S, stage,
-                  W, dstage};
+                  W, dstage, psi64};
     for (void* p : ps) if (p) cudaFree(p);
     for (auto& p : D) if (p) cudaFree(p);
     for (auto& p : P) if (p) cudaFree(p);
@@ -390,21 +407,23 @@ class Engine final : public EngineBase {
     return QG_OK;
   }
 
-  // smem sizes per kernel
+  // shared memory of the step kernels (twiddles + padded transforms)
+  template <int NN> static constexpr size_t sm_col6() { return (size_t)(NN + 6 * Tiles<T, NN>::CT * Tiles<T, NN>::LD) * sizeof(C); }
+  template <int NN> static constexpr size_t sm_col2() { return (size_t)(NN + 2 * Tiles<T, NN>::CT * Tiles<T, NN>::LD) * sizeof(C); }
+  template <int NN> static constexpr size_t sm_row7() { return (size_t)(NN + 7 * Tiles<T, NN>::RT * Tiles<T, NN>::LD) * sizeof(C); }
+  template <int NN> static constexpr size_t sm_row4() { return (size_t)(NN + 4 * Tiles<T, NN>::RT * Tiles<T, NN>::LD) * sizeof(C); }
+  // shared memory of the dense (routine-level) kernels
   size_t sm_colinv() const { return (size_t)(g.n + 2 * Tile<T>::CT * (g.n + 1)) * sizeof(C); }
-  size_t sm_rowmain() const { return (size_t)(g.n + 12 * Tile<T>::RT * g.n) * sizeof(C); }
-  size_t sm_colupd() const { return (size_t)(g.n + 2 * Tile<T>::CT * (g.n + 1) + Tile<T>::CT * g.KY) * sizeof(C); }
-  size_t sm_rowqw() const { return (size_t)(g.n + 7 * Tile<T>::RT * g.n) * sizeof(C); }
   size_t sm_drow() const { return (size_t)(3 * g.n) * sizeof(C); }
 
   int set_smem_attrs() {
     const int mx = cudaFuncAttributeMaxDynamicSharedMemorySize;
     QG_SWITCH_N(g.n, {
-      QG_CK(cudaFuncSetAttribute(k_col_inv<T, NN>, (cudaFuncAttribute)mx, (int)sm_colinv()));
-      QG_CK(cudaFuncSetAttribute(k_row_main<T, NN>, (cudaFuncAttribute)mx, (int)sm_rowmain()));
-      QG_CK(cudaFuncSetAttribute(k_col_update<T, NN>, (cudaFuncAttribute)mx, (int)sm_colupd()));
-      QG_CK(cudaFuncSetAttribute(k_row_qw<T, NN>, (cudaFuncAttribute)mx, (int)sm_rowqw()));
-      QG_CK(cudaFuncSetAttribute(k_col_qw<T, NN>, (cudaFuncAttribute)mx, (int)sm_colupd()));
+      QG_CK(cudaFuncSetAttribute(k_col_inv<T, NN>, (cudaFuncAttribute)mx, (int)sm_col6<NN>()));
+      QG_CK(cudaFuncSetAttribute(k_row_main<T, NN>, (cudaFuncAttribute)mx, (int)sm_row7<NN>()));
+      QG_CK(cudaFuncSetAttribute(k_col_update<T, NN>, (cudaFuncAttribute)mx, (int)sm_col6<NN>()));
+      QG_CK(cudaFuncSetAttribute(k_row_qw<T, NN>, (cudaFuncAttribute)mx, (int)sm_row4<NN>()));
+      QG_CK(cudaFuncSetAttribute(k_col_qw<T, NN>, (cudaFuncAttribute)mx, (int)sm_col2<NN>()));
       QG_CK(cudaFuncSetAttribute(k_dcol_inv<T, NN>, (cudaFuncAttribute)mx, (int)sm_colinv()));
       QG_CK(cudaFuncSetAttribute(k_dcol_fwd<T, NN>, (cudaFuncAttribute)mx, (int)sm_colinv()));
       QG_CK(cudaFuncSetAttribute(k_drow_c2r<T, NN>, (cudaFuncAttribute)mx, (int)sm_drow()));
@@ -466,7 +485,6 @@ class Engine final : public EngineBase {
   int enqueue_step(int euler) {
     StepParams s = sp;
     s.euler = euler;
-    const int CT = Tile<T>::CT, RT = Tile<T>::RT;
     if (s.use_dq) {
       if (int rc0 = pbeg(QG_K_DISSIPATION)) return rc0;
       k_dissipation<T><<<grid_for((long long)g.n3 * g.plane), 256, 0, st>>>(g, cfg.nuz, cfg.dz,
@@ -477,28 +495,28 @@ class Engine final : public EngineBase {
     StateP<T> sptr = state_ptrs();
     for (int z0 = 0; z0 < g.n3; z0 += Zb) {
       const int zc = std::min(Zb, g.n3 - z0);
-      const dim3 gc(g.KXP / CT, zc), gr(g.n / RT, zc);
       QG_SWITCH_N(g.n, {
+        const dim3 gc(g.KXP / Tiles<T, NN>::CT, zc), gr(g.n / Tiles<T, NN>::RT, zc);
         if (int rc0 = pbeg(QG_K_COL_INV)) return rc0;
-        k_col_inv<T, NN><<<gc, kThreads, sm_colinv(), st>>>(g, z0, F[F_PSI], F[F_Q], F[F_BR], F[F_BI], S, tw);
+        k_col_inv<T, NN><<<gc, kColThreads, sm_col6<NN>(), st>>>(g, z0, F[F_PSI], F[F_Q], F[F_BR], F[F_BI], S, tw);
         QG_LAUNCHED();
         if (int rc0 = pend()) return rc0;
         if (int rc0 = pbeg(QG_K_ROW_MAIN)) return rc0;
-        k_row_main<T, NN><<<gr, kThreads, sm_rowmain(), st>>>(g, s, S, tw);
+        k_row_main<T, NN><<<gr, kThreadsB, sm_row7<NN>(), st>>>(g, s, S, tw);
         QG_LAUNCHED();
         if (int rc0 = pend()) return rc0;
         if (int rc0 = pbeg(QG_K_COL_UPDATE)) return rc0;
-        k_col_update<T, NN><<<gc, kThreads, sm_colupd(), st>>>(g, s, z0, sptr, e1, e2, e1w, e2w, S, tw,
+        k_col_update<T, NN><<<gc, kColThreads, sm_col6<NN>(), st>>>(g, s, z0, sptr, e1, e2, e1w, e2w, S, tw,
                                                                 need_qw ? 1 : 0);
         QG_LAUNCHED();
         if (int rc0 = pend()) return rc0;
         if (need_qw) {
           if (int rc0 = pbeg(QG_K_ROW_QW)) return rc0;
-          k_row_qw<T, NN><<<gr, kThreads, sm_rowqw(), st>>>(g, S, tw);
+          k_row_qw<T, NN><<<gr, kThreadsB, sm_row4<NN>(), st>>>(g, S, tw);
           QG_LAUNCHED();
           if (int rc0 = pend()) return rc0;
           if (int rc0 = pbeg(QG_K_COL_QW)) return rc0;
-          k_col_qw<T, NN><<<gc, kThreads, sm_colupd(), st>>>(g, s, z0, F[F_Q], F[F_QSTAR], S, tw);
+          k_col_qw<T, NN><<<gc, kThreadsB, sm_col2<NN>(), st>>>(g, s, z0, F[F_Q], F[F_QSTAR], S, tw);
           QG_LAUNCHED();
           if (int rc0 = pend()) return rc0;
         }

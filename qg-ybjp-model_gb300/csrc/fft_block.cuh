@@ -121,3 +121,80 @@ __device__ __forceinline__ void load_twiddles(cplx<T>* tw_s, const cplx<T>* __re
 }
 
 }  // namespace qg
+
+namespace qg {
+
+// ---------------------------------------------------------------------------
+// In-place batched FFTs with compile-time shape, used by the step kernels.
+//
+// BATCH transforms of length N live in one shared buffer, transform b at
+// b*PadLD<N> with element i at pad_idx(i) = i + i/16: one padding slot every
+// 16 elements makes the radix-8 Stockham reads (stride N/8) and writes
+// (stride 1, 8, 64, ...) bank-conflict free for 8- and 16-byte elements.
+// Each pass reads all of a thread's butterflies into registers, synchronises,
+// then writes them back (so one buffer suffices); NT threads of the CTA take
+// part (compile-time, so every loop unrolls).
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ constexpr int pad_idx(int i) { return i + (i >> 4); }
+template <int N> struct PadLD { static constexpr int value = N + (N >> 4); };
+
+template <typename T, int N, int R, int NS, bool FWD, int BATCH, int NT>
+__device__ __forceinline__ void ip_pass(cplx<T>* __restrict__ buf, const cplx<T>* __restrict__ tw) {
+  constexpr int NB = N / R;
+  constexpr int TASKS = BATCH * NB;
+  constexpr int PER = (TASKS + NT - 1) / NT;
+  constexpr int LD = PadLD<N>::value;
+  cplx<T> v[PER][R];
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int t = tid + p * NT;
+    if ((TASKS % NT) == 0 || t < TASKS) {
+      const int b = t / NB, j = t % NB;
+      const cplx<T>* s = buf + b * LD;
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[p][r] = s[pad_idx(j + r * NB)];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int t = tid + p * NT;
+    if ((TASKS % NT) == 0 || t < TASKS) {
+      const int b = t / NB, j = t % NB;
+      const int k = j & (NS - 1);
+      if constexpr (NS > 1) {
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+          cplx<T> w = tw[k * r * (N / (NS * R))];
+          if (!FWD) w.y = -w.y;
+          v[p][r] = cmul(v[p][r], w);
+        }
+      }
+      dftR<T, R, FWD>(v[p]);
+      cplx<T>* d = buf + b * LD;
+      const int base = (j - k) * R + k;
+#pragma unroll
+      for (int r = 0; r < R; ++r) d[pad_idx(base + r * NS)] = v[p][r];
+    }
+  }
+  __syncthreads();
+}
+
+template <typename T, int N, bool FWD, int BATCH, int NT, int NS>
+__device__ __forceinline__ void ip_passes(cplx<T>* buf, const cplx<T>* tw) {
+  if constexpr (NS < N) {
+    constexpr int R = PassRadix<N / NS>::value;
+    ip_pass<T, N, R, NS, FWD, BATCH, NT>(buf, tw);
+    ip_passes<T, N, FWD, BATCH, NT, NS * R>(buf, tw);
+  }
+}
+
+// All NT threads must call; the data must be visible to all of them (call
+// after a __syncthreads()).  Ends with a __syncthreads().
+template <typename T, int N, bool FWD, int BATCH, int NT>
+__device__ __forceinline__ void fft_ip(cplx<T>* buf, const cplx<T>* tw) {
+  ip_passes<T, N, FWD, BATCH, NT, 1>(buf, tw);
+}
+
+}  // namespace qg

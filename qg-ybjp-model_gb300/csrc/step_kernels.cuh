@@ -36,55 +36,78 @@ __device__ __forceinline__ void realit_col(cplx<T>* col, int n) {
   for (int j = 1 + threadIdx.x; j < n / 2; j += blockDim.x) col[n - j] = cconj(col[j]);
 }
 
+// Tile shapes: CT columns per column-kernel CTA (6*CT transforms ~100 KB of
+// shared memory), RT rows per row-kernel CTA.
+template <typename T, int N> struct Tiles {
+  static constexpr int CB = (int)sizeof(cplx<T>);
+  static constexpr int ct0 = (16384 / CB) / N;
+  static constexpr int CT = ct0 >= 8 ? 8 : (ct0 >= 1 ? ct0 : 1);
+  static constexpr int rt0 = (8192 / CB) / N;
+  static constexpr int RT = rt0 >= 2 ? 2 : 1;
+  static constexpr int LD = PadLD<N>::value;
+};
+constexpr int kColThreads = 256;   // k_col_inv, k_col_update
+constexpr int kThreadsB = 256;     // row kernels, k_col_qw
+
+template <typename T, int N>
+__device__ __forceinline__ void load_tw(cplx<T>* tw_s, const cplx<T>* __restrict__ tw_g, int nt) {
+  for (int i = threadIdx.x; i < N; i += nt) tw_s[i] = tw_g[i];
+}
+
 // ===========================================================================
 // Phase A, kernel 1: y-inverse FFTs of the six fields needed in physical space
 // ===========================================================================
 template <typename T, int N>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kColThreads, 2)
 k_col_inv(Geom g, int zbase, const cplx<T>* __restrict__ psi, const cplx<T>* __restrict__ q,
           const cplx<T>* __restrict__ BR, const cplx<T>* __restrict__ BI, cplx<T>* __restrict__ S,
           const cplx<T>* __restrict__ twg) {
-  constexpr int CT = Tile<T>::CT;
-  constexpr int LD = N + 1;
+  constexpr int CT = Tiles<T, N>::CT, LD = Tiles<T, N>::LD, NT = kColThreads;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* bufA = tw + N;
-  cplx<T>* bufB = bufA + CT * LD;
+  cplx<T>* buf = tw + N;                       // [6][CT][LD]
+  const int tid = threadIdx.x;
   const int zb = blockIdx.y, z = zbase + zb;
   const int kx0 = blockIdx.x * CT;
-  load_twiddles<T, N>(tw, twg);
+  load_tw<T, N>(tw, twg, NT);
   const long long zoff = (long long)z * g.plane;
-  for (int f = 0; f < 6; ++f) {
-    const cplx<T>* src = f < 3 ? psi : (f == 3 ? q : (f == 4 ? BR : BI));
-    for (int idx = threadIdx.x; idx < CT * N; idx += blockDim.x) {
-      const int c = idx % CT, j = idx / CT;
+#pragma unroll
+  for (int src = 0; src < 4; ++src) {
+    const cplx<T>* F = src == 0 ? psi : (src == 1 ? q : (src == 2 ? BR : BI));
+#pragma unroll 4
+    for (int e = tid; e < CT * N; e += NT) {
+      const int c = e % CT, j = e / CT;
       const int kx = kx0 + c;
-      cplx<T> v = mk<T>(0, 0);
       const int r = g.row_of_fft_index(j);
-      if (kx <= g.K && r >= 0) {
-        const int ky = g.ky_of_row(r);
-        const cplx<T> s = src[zoff + (long long)r * g.KXP + kx];
-        if (f == 0) {            // u = -i ky psi   (derivatives.f90:1309)
-          v = cscale(cmul_mi(s), (T)ky);
-        } else if (f == 1) {     // v = i kx psi    (derivatives.f90:1310)
-          v = cscale(cmul_i(s), (T)kx);
-        } else if (f == 2) {     // zeta = -kh^2 psi (derivatives.f90:842)
-          v = cscale(s, -(T)(kx * kx + ky * ky));
-        } else {
-          v = s;
-        }
+      const bool in = kx <= g.K && r >= 0;
+      const cplx<T> sv = in ? F[zoff + (long long)r * g.KXP + kx] : mk<T>(0, 0);
+      const int o = c * LD + pad_idx(j);
+      if (src == 0) {
+        const T ky = in ? (T)g.ky_of_row(r) : (T)0;
+        buf[0 * CT * LD + o] = cscale(cmul_mi(sv), ky);                          // u = -i ky psi (derivatives.f90:1309)
+        buf[1 * CT * LD + o] = cscale(cmul_i(sv), (T)kx);                        // v = i kx psi  (derivatives.f90:1310)
+        buf[2 * CT * LD + o] = cscale(sv, -((T)(kx * kx) + ky * ky));            // zeta = -kh^2 psi (derivatives.f90:842)
+      } else {
+        buf[(src + 2) * CT * LD + o] = sv;
       }
-      bufA[c * LD + j] = v;
+    }
+  }
+  __syncthreads();
+  if (kx0 == 0) {    // realit (fft.f90:88-107) on the kx=0 column of each field
+    for (int e = tid; e < 6 * (N / 2 - 1); e += NT) {
+      const int f = e / (N / 2 - 1), j = 1 + e % (N / 2 - 1);
+      cplx<T>* col = buf + f * CT * LD;
+      col[pad_idx(N - j)] = cconj(col[pad_idx(j)]);
     }
     __syncthreads();
-    if (kx0 == 0) realit_col<T>(bufA, N);
-    __syncthreads();
-    cplx<T>* res = block_fft<T, N, false>(bufA, bufB, LD, CT, tw);
-    for (int idx = threadIdx.x; idx < CT * N; idx += blockDim.x) {
-      const int c = idx % CT, y = idx / CT;
-      S[scr_off(zb, f, y, N, g.KXP) + kx0 + c] = res[c * LD + y];
-    }
-    __syncthreads();
+  }
+  // two groups of three fields keep a thread's butterflies in registers
+  fft_ip<T, N, false, 3 * CT, NT>(buf, tw);
+  fft_ip<T, N, false, 3 * CT, NT>(buf + 3 * CT * LD, tw);
+#pragma unroll 4
+  for (int e = tid; e < 6 * CT * N; e += NT) {
+    const int c = e % CT, y = (e / CT) % N, f = e / (CT * N);
+    S[scr_off(zb, f, y, N, g.KXP) + kx0 + c] = buf[(f * CT + c) * LD + pad_idx(y)];
   }
 }
 
@@ -107,72 +130,73 @@ __device__ __forceinline__ void unpack_spec(const cplx<T>* F, int k, int n, cplx
   X = mk<T>((a.x + b.x) * (T)0.5, (a.y - b.y) * (T)0.5);
   Y = mk<T>((a.y + b.y) * (T)0.5, (b.x - a.x) * (T)0.5);
 }
+// the same on a padded shared-memory transform
+template <typename T>
+__device__ __forceinline__ void unpack_pad(const cplx<T>* F, int k, int n, cplx<T>& X, cplx<T>& Y) {
+  const cplx<T> a = F[pad_idx(k)], b = F[pad_idx(k == 0 ? 0 : n - k)];
+  X = mk<T>((a.x + b.x) * (T)0.5, (a.y - b.y) * (T)0.5);
+  Y = mk<T>((a.y + b.y) * (T)0.5, (b.x - a.x) * (T)0.5);
+}
 
 // ===========================================================================
 // Phase A, kernel 2: rows — physical products of convol_waqg / refraction_waqg
 // ===========================================================================
 template <typename T, int N>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreadsB)
 k_row_main(Geom g, StepParams sp, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
-  constexpr int RT = Tile<T>::RT;
-  constexpr int LD = N;
+  constexpr int RT = Tiles<T, N>::RT, LD = Tiles<T, N>::LD, NT = kThreadsB;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* bA = tw + N;               // 4*RT rows
-  cplx<T>* bB = bA + 4 * RT * LD;
-  cplx<T>* bC = bB + 4 * RT * LD;
+  cplx<T>* bA = tw + N;                 // [RT][3][LD]: (u,v), (zeta,q), (br,bi)
+  cplx<T>* bC = bA + 3 * RT * LD;       // [RT][4][LD]: products
+  const int tid = threadIdx.x;
   const int zb = blockIdx.y;
   const int y0 = blockIdx.x * RT;
-  load_twiddles<T, N>(tw, twg);
   const int K = g.K;
-  // packed spectra: (u,v), (zeta,q), (BR,BI)
-  for (int idx = threadIdx.x; idx < 3 * RT * N; idx += blockDim.x) {
-    const int k = idx % N, p = (idx / N) % 3, rr = idx / (3 * N);
+  load_tw<T, N>(tw, twg, NT);
+#pragma unroll 4
+  for (int e = tid; e < 3 * RT * N; e += NT) {
+    const int k = e % N, p = (e / N) % 3, rr = e / (3 * N);
     const int y = y0 + rr;
     const cplx<T>* X = S + scr_off(zb, 2 * p, y, N, g.KXP);
     const cplx<T>* Y = S + scr_off(zb, 2 * p + 1, y, N, g.KXP);
-    bA[(rr * 3 + p) * LD + k] = pack_spec<T>(X, Y, k, N, K);
+    bA[(rr * 3 + p) * LD + pad_idx(k)] = pack_spec<T>(X, Y, k, N, K);
   }
   __syncthreads();
-  cplx<T>* ph = block_fft<T, N, false>(bA, bB, LD, 3 * RT, tw);
-  // products -> bC: (u q, v q), (u br, v br), (u bi, v bi), (zeta br, zeta bi)
-  for (int idx = threadIdx.x; idx < RT * N; idx += blockDim.x) {
-    const int x = idx % N, rr = idx / N;
-    const cplx<T> uv = ph[(rr * 3 + 0) * LD + x];
-    const cplx<T> zq = ph[(rr * 3 + 1) * LD + x];
-    const cplx<T> bb = ph[(rr * 3 + 2) * LD + x];
-    bC[(rr * 4 + 0) * LD + x] = mk<T>(uv.x * zq.y, uv.y * zq.y);
-    bC[(rr * 4 + 1) * LD + x] = mk<T>(uv.x * bb.x, uv.y * bb.x);
-    bC[(rr * 4 + 2) * LD + x] = mk<T>(uv.x * bb.y, uv.y * bb.y);
-    bC[(rr * 4 + 3) * LD + x] = mk<T>(zq.x * bb.x, zq.x * bb.y);
+  fft_ip<T, N, false, 3 * RT, NT>(bA, tw);
+  // products: (u q, v q), (u br, v br), (u bi, v bi), (zeta br, zeta bi)
+#pragma unroll 4
+  for (int e = tid; e < RT * N; e += NT) {
+    const int x = e % N, rr = e / N;
+    const int px = pad_idx(x);
+    const cplx<T> uv = bA[(rr * 3 + 0) * LD + px];
+    const cplx<T> zq = bA[(rr * 3 + 1) * LD + px];
+    const cplx<T> bb = bA[(rr * 3 + 2) * LD + px];
+    bC[(rr * 4 + 0) * LD + px] = mk<T>(uv.x * zq.y, uv.y * zq.y);
+    bC[(rr * 4 + 1) * LD + px] = mk<T>(uv.x * bb.x, uv.y * bb.x);
+    bC[(rr * 4 + 2) * LD + px] = mk<T>(uv.x * bb.y, uv.y * bb.y);
+    bC[(rr * 4 + 3) * LD + px] = mk<T>(zq.x * bb.x, zq.x * bb.y);
   }
   __syncthreads();
-  cplx<T>* scr = (ph == bA) ? bB : bA;
-  cplx<T>* sp4 = block_fft<T, N, true>(bC, scr, LD, 4 * RT, tw);
+  fft_ip<T, N, true, 4 * RT, NT>(bC, tw);
   const T adv = sp.adv ? (T)1 : (T)0;
   const T half = sp.refr ? (T)0.5 : (T)0;
-  for (int idx = threadIdx.x; idx < RT * (K + 1); idx += blockDim.x) {
-    const int k = idx % (K + 1), rr = idx / (K + 1);
+  for (int e = tid; e < RT * (K + 1); e += NT) {
+    const int k = e % (K + 1), rr = e / (K + 1);
     const int y = y0 + rr;
     cplx<T> uq, vq, ubr, vbr, ubi, vbi, zbr, zbi;
-    unpack_spec<T>(sp4 + (rr * 4 + 0) * LD, k, N, uq, vq);
-    unpack_spec<T>(sp4 + (rr * 4 + 1) * LD, k, N, ubr, vbr);
-    unpack_spec<T>(sp4 + (rr * 4 + 2) * LD, k, N, ubi, vbi);
-    unpack_spec<T>(sp4 + (rr * 4 + 3) * LD, k, N, zbr, zbi);
+    unpack_pad<T>(bC + (rr * 4 + 0) * LD, k, N, uq, vq);
+    unpack_pad<T>(bC + (rr * 4 + 1) * LD, k, N, ubr, vbr);
+    unpack_pad<T>(bC + (rr * 4 + 2) * LD, k, N, ubi, vbi);
+    unpack_pad<T>(bC + (rr * 4 + 3) * LD, k, N, zbr, zbi);
     const T kx = (T)k;
     // G = i kx F(uX) (+- refraction), H = F(vX); tendency = F_y(G) + i ky F_y(H)
-    const cplx<T> Gq = cscale(cmul_i(uq), kx * adv);
-    const cplx<T> Hq = cscale(vq, adv);
-    const cplx<T> GBR = csub(cscale(cmul_i(ubr), kx * adv), cscale(zbi, half));
-    const cplx<T> HBR = cscale(vbr, adv);
-    const cplx<T> GBI = cadd(cscale(cmul_i(ubi), kx * adv), cscale(zbr, half));
-    const cplx<T> HBI = cscale(vbi, adv);
-    S[scr_off(zb, 0, y, N, g.KXP) + k] = Gq;
-    S[scr_off(zb, 1, y, N, g.KXP) + k] = Hq;
-    S[scr_off(zb, 2, y, N, g.KXP) + k] = GBR;
-    S[scr_off(zb, 3, y, N, g.KXP) + k] = HBR;
-    S[scr_off(zb, 4, y, N, g.KXP) + k] = GBI;
-    S[scr_off(zb, 5, y, N, g.KXP) + k] = HBI;
+    S[scr_off(zb, 0, y, N, g.KXP) + k] = cscale(cmul_i(uq), kx * adv);
+    S[scr_off(zb, 1, y, N, g.KXP) + k] = cscale(vq, adv);
+    S[scr_off(zb, 2, y, N, g.KXP) + k] = csub(cscale(cmul_i(ubr), kx * adv), cscale(zbi, half));
+    S[scr_off(zb, 3, y, N, g.KXP) + k] = cscale(vbr, adv);
+    S[scr_off(zb, 4, y, N, g.KXP) + k] = cadd(cscale(cmul_i(ubi), kx * adv), cscale(zbr, half));
+    S[scr_off(zb, 5, y, N, g.KXP) + k] = cscale(vbi, adv);
   }
 }
 
@@ -182,137 +206,118 @@ template <typename T> struct StateP {
   cplx<T>* psi; cplx<T>* AR; cplx<T>* AI; cplx<T>* qstar; const cplx<T>* dq;
 };
 
-// Fill bufA columns from scratch plane f (all n rows), zero beyond kx = K.
-template <typename T, int N, int CT>
-__device__ __forceinline__ void load_scr_cols(cplx<T>* bufA, const cplx<T>* __restrict__ S, const Geom& g,
-                                              int zb, int f, int kx0) {
-  constexpr int LD = N + 1;
-  for (int idx = threadIdx.x; idx < CT * N; idx += blockDim.x) {
-    const int c = idx % CT, y = idx / CT;
-    const int kx = kx0 + c;
-    bufA[c * LD + y] = kx <= g.K ? S[scr_off(zb, f, y, N, g.KXP) + kx] : mk<T>(0, 0);
-  }
-}
-
 // ===========================================================================
 // Phase A, kernel 3: y-forward FFTs, time update, y-inverse FFTs for q^w
 // ===========================================================================
 template <typename T, int N>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kColThreads, 2)
 k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict__ e1t, const T* __restrict__ e2t,
              const T* __restrict__ e1wt, const T* __restrict__ e2wt, cplx<T>* __restrict__ S,
              const cplx<T>* __restrict__ twg, int qw_prep) {
-  constexpr int CT = Tile<T>::CT;
-  constexpr int LD = N + 1;
+  constexpr int CT = Tiles<T, N>::CT, LD = Tiles<T, N>::LD, NT = kColThreads;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* bufA = tw + N;
-  cplx<T>* bufB = bufA + CT * LD;
-  cplx<T>* R = bufB + CT * LD;          // [CT][KY]
+  cplx<T>* buf = tw + N;                 // [6][CT][LD]
+  const int tid = threadIdx.x;
   const int zb = blockIdx.y, z = zbase + zb;
   const int kx0 = blockIdx.x * CT;
   const int KY = g.KY;
-  load_twiddles<T, N>(tw, twg);
+  load_tw<T, N>(tw, twg, NT);
+#pragma unroll 4
+  for (int e = tid; e < 6 * CT * N; e += NT) {
+    const int c = e % CT, y = (e / CT) % N, h = e / (CT * N);
+    const int kx = kx0 + c;
+    buf[(h * CT + c) * LD + pad_idx(y)] = kx <= g.K ? S[scr_off(zb, h, y, N, g.KXP) + kx] : mk<T>(0, 0);
+  }
+  __syncthreads();
+  fft_ip<T, N, true, 3 * CT, NT>(buf, tw);
+  fft_ip<T, N, true, 3 * CT, NT>(buf + 3 * CT * LD, tw);
+  // tendencies and time update (main_waqg.f90:237-264, 362-415)
   const T inv_n2 = (T)1 / ((T)N * (T)N);
   const long long zoff = (long long)z * g.plane;
   const T dt = (T)sp.delt;
   const T gam = (T)sp.gamma;
   const T cdisp = sp.disp ? (T)sp.cdisp : (T)0;
-  for (int X = 0; X < 3; ++X) {
-    for (int h = 0; h < 2; ++h) {
-      load_scr_cols<T, N, CT>(bufA, S, g, zb, 2 * X + h, kx0);
-      __syncthreads();
-      cplx<T>* res = block_fft<T, N, true>(bufA, bufB, LD, CT, tw);
-      for (int idx = threadIdx.x; idx < CT * KY; idx += blockDim.x) {
-        const int c = idx % CT, r = idx / CT;
-        const cplx<T> v = res[c * LD + g.fft_index_of_row(r)];
-        if (h == 0) {
-          R[c * KY + r] = v;
-        } else {
-          const T ky = (T)g.ky_of_row(r);
-          cplx<T> a = R[c * KY + r];
-          a.x -= ky * v.y; a.y += ky * v.x;      // + i ky v
-          R[c * KY + r] = a;
-        }
-      }
-      __syncthreads();
-    }
-    // time update of field X on this column tile (main_waqg.f90:237-264, 362-415)
-    for (int idx = threadIdx.x; idx < CT * KY; idx += blockDim.x) {
-      const int c = idx % CT, r = idx / CT;
-      const int kx = kx0 + c;
-      if (kx > g.K) continue;
-      const int ky = g.ky_of_row(r);
-      const long long m = zoff + (long long)r * g.KXP + kx;
-      const long long mt = (long long)r * g.KXP + kx;
-      const bool L = g.mask(kx, ky);
-      const T kh2 = (T)(kx * kx + ky * ky);
-      const cplx<T> tend = cscale(R[c * KY + r], inv_n2);
-      cplx<T>* cur = X == 0 ? st.q : (X == 1 ? st.BR : st.BI);
-      cplx<T>* old = X == 0 ? st.qo : (X == 1 ? st.BRo : st.BIo);
-      const cplx<T> xc = cur[m];
-      const cplx<T> xo = sp.euler ? xc : old[m];
-      cplx<T> xn = mk<T>(0, 0), xf = mk<T>(0, 0);
-      if (L) {
-        if (X == 0) {
-          const T e1 = e1t[mt], e2 = e2t[mt];
-          const cplx<T> dqv = sp.use_dq ? st.dq[m] : mk<T>(0, 0);
-          if (sp.euler) {
-            xn = cscale(cadd(csub(xo, cscale(tend, dt)), cscale(dqv, dt)), e1);
-          } else {
-            xn = cadd(csub(cscale(xo, e2), cscale(cscale(tend, (T)2 * dt), e1)), cscale(cscale(dqv, (T)2 * dt), e2));
-          }
-        } else {
-          const T e1 = e1wt[mt], e2 = e2wt[mt];
-          // BR: tend_BR + c kh2 AI ; BI: tend_BI - c kh2 AR
-          const cplx<T> Av = X == 1 ? st.AI[m] : st.AR[m];
-          const T sgn = X == 1 ? (T)1 : (T)-1;
-          const cplx<T> full = cadd(tend, cscale(Av, sgn * cdisp * kh2));
-          if (sp.euler) {
-            xn = cscale(csub(xo, cscale(full, dt)), e1);
-          } else {
-            xn = csub(cscale(xo, e2), cscale(cscale(full, (T)2 * dt), e1));
-          }
-        }
+  for (int e = tid; e < 3 * CT * KY; e += NT) {
+    const int c = e % CT, r = (e / CT) % KY, X = e / (CT * KY);
+    const int kx = kx0 + c;
+    if (kx > g.K) continue;
+    const int ky = g.ky_of_row(r);
+    const int j = pad_idx(g.fft_index_of_row(r));
+    const cplx<T> G = buf[((2 * X) * CT + c) * LD + j];
+    const cplx<T> H = buf[((2 * X + 1) * CT + c) * LD + j];
+    const cplx<T> tend = cscale(mk<T>(G.x - (T)ky * H.y, G.y + (T)ky * H.x), inv_n2);   // G + i ky H
+    const long long m = zoff + (long long)r * g.KXP + kx;
+    const long long mt = (long long)r * g.KXP + kx;
+    const bool L = g.mask(kx, ky);
+    const T kh2 = (T)(kx * kx + ky * ky);
+    cplx<T>* cur = X == 0 ? st.q : (X == 1 ? st.BR : st.BI);
+    cplx<T>* old = X == 0 ? st.qo : (X == 1 ? st.BRo : st.BIo);
+    const cplx<T> xc = cur[m];
+    const cplx<T> xo = sp.euler ? xc : old[m];
+    cplx<T> xn = mk<T>(0, 0), xf = mk<T>(0, 0);
+    if (L) {
+      if (X == 0) {
+        const T e1 = e1t[mt], e2 = e2t[mt];
+        const cplx<T> dqv = sp.use_dq ? st.dq[m] : mk<T>(0, 0);
         if (sp.euler) {
-          xf = xo;      // old level <- current (main_waqg.f90:232-234)
-        } else {        // Robert-Asselin filter (main_waqg.f90:395-410)
-          xf = cadd(xc, cscale(cadd(csub(xo, cscale(xc, (T)2)), xn), gam));
+          xn = cscale(cadd(csub(xo, cscale(tend, dt)), cscale(dqv, dt)), e1);
+        } else {
+          xn = cadd(csub(cscale(xo, e2), cscale(cscale(tend, (T)2 * dt), e1)), cscale(cscale(dqv, (T)2 * dt), e2));
         }
-      } else if (sp.euler) {
-        xf = xo;        // the reference keeps the unmasked n=0 field as old level
+      } else {
+        const T e1 = e1wt[mt], e2 = e2wt[mt];
+        // BR: tend_BR + c kh2 AI ; BI: tend_BI - c kh2 AR
+        const cplx<T> Av = X == 1 ? st.AI[m] : st.AR[m];
+        const T sgn = X == 1 ? (T)1 : (T)-1;
+        const cplx<T> full = cadd(tend, cscale(Av, sgn * cdisp * kh2));
+        if (sp.euler) {
+          xn = cscale(csub(xo, cscale(full, dt)), e1);
+        } else {
+          xn = csub(cscale(xo, e2), cscale(cscale(full, (T)2 * dt), e1));
+        }
       }
-      cur[m] = xn;
-      old[m] = xf;
+      if (sp.euler) {
+        xf = xo;      // old level <- current (main_waqg.f90:232-234)
+      } else {        // Robert-Asselin filter (main_waqg.f90:395-410)
+        xf = cadd(xc, cscale(cadd(csub(xo, cscale(xc, (T)2)), xn), gam));
+      }
+    } else if (sp.euler) {
+      xf = xo;
+    }
+    cur[m] = xn;
+    old[m] = xf;
+  }
+  if (!qw_prep) return;
+  __syncthreads();   // this CTA's writes of BR, BI are visible to it after the barrier
+  // y-inverse FFTs of BR, i ky BR, BI, i ky BI at n+1 (compute_qw, derivatives.f90:929-957)
+#pragma unroll 4
+  for (int e = tid; e < 4 * CT * N; e += NT) {
+    const int c = e % CT, j = (e / CT) % N, f = e / (CT * N);
+    const int kx = kx0 + c;
+    const int r = g.row_of_fft_index(j);
+    cplx<T> v = mk<T>(0, 0);
+    if (kx <= g.K && r >= 0) {
+      const cplx<T> s = (f < 2 ? st.BR : st.BI)[zoff + (long long)r * g.KXP + kx];
+      v = (f & 1) ? cscale(cmul_i(s), (T)g.ky_of_row(r)) : s;
+    }
+    buf[(f * CT + c) * LD + pad_idx(j)] = v;
+  }
+  __syncthreads();
+  if (kx0 == 0) {
+    for (int e = tid; e < 4 * (N / 2 - 1); e += NT) {
+      const int f = e / (N / 2 - 1), j = 1 + e % (N / 2 - 1);
+      cplx<T>* col = buf + f * CT * LD;
+      col[pad_idx(N - j)] = cconj(col[pad_idx(j)]);
     }
     __syncthreads();
   }
-  if (!qw_prep) return;
-  // y-inverse FFTs of BR, i ky BR, BI, i ky BI at n+1 (compute_qw, derivatives.f90:929-957)
-  __threadfence_block();
-  for (int f = 0; f < 4; ++f) {
-    const cplx<T>* src = f < 2 ? st.BR : st.BI;
-    const bool dy = (f & 1);
-    for (int idx = threadIdx.x; idx < CT * N; idx += blockDim.x) {
-      const int c = idx % CT, j = idx / CT;
-      const int kx = kx0 + c;
-      cplx<T> v = mk<T>(0, 0);
-      const int r = g.row_of_fft_index(j);
-      if (kx <= g.K && r >= 0) {
-        const cplx<T> s = src[zoff + (long long)r * g.KXP + kx];
-        v = dy ? cscale(cmul_i(s), (T)g.ky_of_row(r)) : s;
-      }
-      bufA[c * LD + j] = v;
-    }
-    __syncthreads();
-    if (kx0 == 0) realit_col<T>(bufA, N);
-    __syncthreads();
-    cplx<T>* res = block_fft<T, N, false>(bufA, bufB, LD, CT, tw);
-    for (int idx = threadIdx.x; idx < CT * N; idx += blockDim.x) {
-      const int c = idx % CT, y = idx / CT;
-      S[scr_off(zb, f, y, N, g.KXP) + kx0 + c] = res[c * LD + y];
-    }
-    __syncthreads();
+  fft_ip<T, N, false, 2 * CT, NT>(buf, tw);
+  fft_ip<T, N, false, 2 * CT, NT>(buf + 2 * CT * LD, tw);
+#pragma unroll 4
+  for (int e = tid; e < 4 * CT * N; e += NT) {
+    const int c = e % CT, y = (e / CT) % N, f = e / (CT * N);
+    S[scr_off(zb, f, y, N, g.KXP) + kx0 + c] = buf[(f * CT + c) * LD + pad_idx(y)];
   }
 }
 
@@ -320,22 +325,22 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
 // Phase A, kernel 4: rows — products of compute_qw
 // ===========================================================================
 template <typename T, int N>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreadsB)
 k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
-  constexpr int RT = Tile<T>::RT;
-  constexpr int LD = N;
+  constexpr int RT = Tiles<T, N>::RT, LD = Tiles<T, N>::LD, NT = kThreadsB;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* bA = tw + N;               // 3*RT rows
-  cplx<T>* bB = bA + 3 * RT * LD;
-  cplx<T>* bC = bB + 3 * RT * LD;     // RT rows
+  cplx<T>* bA = tw + N;               // [RT][3][LD]
+  cplx<T>* bC = bA + 3 * RT * LD;     // [RT][LD]
+  const int tid = threadIdx.x;
   const int zb = blockIdx.y;
   const int y0 = blockIdx.x * RT;
   const int K = g.K;
-  load_twiddles<T, N>(tw, twg);
+  load_tw<T, N>(tw, twg, NT);
   // packed: (BR, BI), (BRx, BIx), (BRy, BIy)
-  for (int idx = threadIdx.x; idx < 3 * RT * N; idx += blockDim.x) {
-    const int k = idx % N, p = (idx / N) % 3, rr = idx / (3 * N);
+#pragma unroll 4
+  for (int e = tid; e < 3 * RT * N; e += NT) {
+    const int k = e % N, p = (e / N) % 3, rr = e / (3 * N);
     const int y = y0 + rr;
     const cplx<T>* sBR = S + scr_off(zb, 0, y, N, g.KXP);
     const cplx<T>* sBRy = S + scr_off(zb, 1, y, N, g.KXP);
@@ -346,39 +351,37 @@ k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
       v = pack_spec<T>(sBR, sBI, k, N, K);
     } else if (p == 2) {
       v = pack_spec<T>(sBRy, sBIy, k, N, K);
+    } else if (k == 0 || (k > K && k < N - K)) {
+      v = mk<T>(0, 0);      // x-derivatives vanish at kx = 0
     } else {
-      // x-derivatives: i kx times the half spectra (zero at kx = 0)
-      if (k == 0 || (k > K && k < N - K)) {
-        v = mk<T>(0, 0);
-      } else {
-        const int kk = k <= K ? k : N - k;
-        const cplx<T> a = cscale(cmul_i(sBR[kk]), (T)kk), b = cscale(cmul_i(sBI[kk]), (T)kk);
-        v = k <= K ? mk<T>(a.x - b.y, a.y + b.x) : mk<T>(a.x + b.y, b.x - a.y);
-      }
+      const int kk = k <= K ? k : N - k;
+      const cplx<T> a = cscale(cmul_i(sBR[kk]), (T)kk), b = cscale(cmul_i(sBI[kk]), (T)kk);
+      v = k <= K ? mk<T>(a.x - b.y, a.y + b.x) : mk<T>(a.x + b.y, b.x - a.y);
     }
-    bA[(rr * 3 + p) * LD + k] = v;
+    bA[(rr * 3 + p) * LD + pad_idx(k)] = v;
   }
   __syncthreads();
-  cplx<T>* ph = block_fft<T, N, false>(bA, bB, LD, 3 * RT, tw);
-  for (int idx = threadIdx.x; idx < RT * N; idx += blockDim.x) {
-    const int x = idx % N, rr = idx / N;
-    const cplx<T> b = ph[(rr * 3 + 0) * LD + x];    // (br, bi)
-    const cplx<T> bx = ph[(rr * 3 + 1) * LD + x];   // (brx, bix)
-    const cplx<T> by = ph[(rr * 3 + 2) * LD + x];   // (bry, biy)
-    const T p1 = by.x * bx.y - bx.x * by.y;          // BRy BIx - BRx BIy (derivatives.f90:973)
-    const T p2 = b.x * b.x + b.y * b.y;              // BR^2 + BI^2     (derivatives.f90:996)
-    bC[rr * LD + x] = mk<T>(p1, p2);
+  fft_ip<T, N, false, 3 * RT, NT>(bA, tw);
+#pragma unroll 4
+  for (int e = tid; e < RT * N; e += NT) {
+    const int x = e % N, rr = e / N;
+    const int px = pad_idx(x);
+    const cplx<T> b = bA[(rr * 3 + 0) * LD + px];    // (br, bi)
+    const cplx<T> bx = bA[(rr * 3 + 1) * LD + px];   // (brx, bix)
+    const cplx<T> by = bA[(rr * 3 + 2) * LD + px];   // (bry, biy)
+    const T p1 = by.x * bx.y - bx.x * by.y;           // BRy BIx - BRx BIy (derivatives.f90:973)
+    const T p2 = b.x * b.x + b.y * b.y;               // BR^2 + BI^2     (derivatives.f90:996)
+    bC[rr * LD + px] = mk<T>(p1, p2);
   }
   __syncthreads();
-  cplx<T>* scr = (ph == bA) ? bB : bA;
-  cplx<T>* F = block_fft<T, N, true>(bC, scr, LD, RT, tw);
-  for (int idx = threadIdx.x; idx < RT * (K + 1); idx += blockDim.x) {
-    const int k = idx % (K + 1), rr = idx / (K + 1);
+  fft_ip<T, N, true, RT, NT>(bC, tw);
+  for (int e = tid; e < RT * (K + 1); e += NT) {
+    const int k = e % (K + 1), rr = e / (K + 1);
     const int y = y0 + rr;
     cplx<T> P1, P2;
-    unpack_spec<T>(F + rr * LD, k, N, P1, P2);
-    const T q = (T)0.25 * (T)(k * k);
-    S[scr_off(zb, 0, y, N, g.KXP) + k] = csub(P1, cscale(P2, q));
+    unpack_pad<T>(bC + rr * LD, k, N, P1, P2);
+    const T qk = (T)0.25 * (T)(k * k);
+    S[scr_off(zb, 0, y, N, g.KXP) + k] = csub(P1, cscale(P2, qk));
     S[scr_off(zb, 1, y, N, g.KXP) + k] = P2;
   }
 }
@@ -387,48 +390,40 @@ k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
 // Phase A, kernel 5: y-forward FFTs of the q^w planes, q* = q - q^w
 // ===========================================================================
 template <typename T, int N>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreadsB)
 k_col_qw(Geom g, StepParams sp, int zbase, const cplx<T>* __restrict__ q, cplx<T>* __restrict__ qstar,
          const cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
-  constexpr int CT = Tile<T>::CT;
-  constexpr int LD = N + 1;
+  constexpr int CT = Tiles<T, N>::CT, LD = Tiles<T, N>::LD, NT = kThreadsB;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* bufA = tw + N;
-  cplx<T>* bufB = bufA + CT * LD;
-  cplx<T>* R = bufB + CT * LD;
+  cplx<T>* buf = tw + N;                 // [2][CT][LD]
+  const int tid = threadIdx.x;
   const int zb = blockIdx.y, z = zbase + zb;
   const int kx0 = blockIdx.x * CT;
   const int KY = g.KY;
-  load_twiddles<T, N>(tw, twg);
-  for (int h = 0; h < 2; ++h) {
-    load_scr_cols<T, N, CT>(bufA, S, g, zb, h, kx0);
-    __syncthreads();
-    cplx<T>* res = block_fft<T, N, true>(bufA, bufB, LD, CT, tw);
-    for (int idx = threadIdx.x; idx < CT * KY; idx += blockDim.x) {
-      const int c = idx % CT, r = idx / CT;
-      const cplx<T> v = res[c * LD + g.fft_index_of_row(r)];
-      if (h == 0) {
-        R[c * KY + r] = v;
-      } else {
-        const T ky = (T)g.ky_of_row(r);
-        R[c * KY + r] = csub(R[c * KY + r], cscale(v, (T)0.25 * ky * ky));
-      }
-    }
-    __syncthreads();
+  load_tw<T, N>(tw, twg, NT);
+#pragma unroll 4
+  for (int e = tid; e < 2 * CT * N; e += NT) {
+    const int c = e % CT, y = (e / CT) % N, h = e / (CT * N);
+    const int kx = kx0 + c;
+    buf[(h * CT + c) * LD + pad_idx(y)] = kx <= g.K ? S[scr_off(zb, h, y, N, g.KXP) + kx] : mk<T>(0, 0);
   }
+  __syncthreads();
+  fft_ip<T, N, true, 2 * CT, NT>(buf, tw);
   const T inv_n2 = (T)1 / ((T)N * (T)N);
   const T s = (T)sp.Ro * (T)sp.W2F;
   const long long zoff = (long long)z * g.plane;
-  for (int idx = threadIdx.x; idx < CT * KY; idx += blockDim.x) {
-    const int c = idx % CT, r = idx / CT;
+  for (int e = tid; e < CT * KY; e += NT) {
+    const int c = e % CT, r = e / CT;
     const int kx = kx0 + c;
     if (kx > g.K) continue;
     const int ky = g.ky_of_row(r);
+    const int j = pad_idx(g.fft_index_of_row(r));
     const long long m = zoff + (long long)r * g.KXP + kx;
     cplx<T> out = mk<T>(0, 0);
     if (g.mask(kx, ky)) {
-      const cplx<T> qw = cscale(cscale(R[c * KY + r], inv_n2), s);
+      const cplx<T> R = csub(buf[c * LD + j], cscale(buf[(CT + c) * LD + j], (T)0.25 * (T)ky * (T)ky));
+      const cplx<T> qw = cscale(cscale(R, inv_n2), s);
       out = csub(q[m], qw);       // q* = q - q^w (main_waqg.f90:430-439)
     }
     qstar[m] = out;
@@ -469,8 +464,23 @@ __global__ void k_dissipation(Geom g, double nuz, double dz, const cplx<T>* __re
 // ===========================================================================
 // Phase B: FP64 tridiagonal solves per (kx,ky) column (elliptic.f90:145-460)
 // ===========================================================================
-// fac[idx*n3 + i] = {f_i = dl_i/d'_i, 1/d'_i} of DGTSV's elimination for the
+// fac[idx*n3 + i] = {f_i = dl_i/d'_i, p_i} of DGTSV's elimination for the
 // distinct kh^2 row idx; du[i] = rho_ut(i)*a(i)/rho_st(i).
+//   EXACT (FP64 path): p_i = d'_i, and every operation is the correctly
+//     rounded IEEE operation of DGTSV (no contraction, true division), so
+//     the solve reproduces LAPACK's reference DGTSV bit for bit.
+//   fast (mixed path): p_i = 1/d'_i, fused multiply-adds.
+template <bool EXACT>
+struct Tri {
+  static __device__ __forceinline__ double fwd(double b, double f, double bp) {
+    return EXACT ? __dsub_rn(b, __dmul_rn(f, bp)) : fma(-f, bp, b);
+  }
+  static __device__ __forceinline__ double back(double b, double u, double x, double p) {
+    return EXACT ? __ddiv_rn(__dsub_rn(b, __dmul_rn(u, x)), p) : fma(-u, x, b) * p;
+  }
+  static __device__ __forceinline__ double last(double b, double p) { return EXACT ? __ddiv_rn(b, p) : b * p; }
+};
+
 template <typename T>
 __global__ void __launch_bounds__(128)
 k_solve(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
@@ -478,6 +488,7 @@ k_solve(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
         const cplx<T>* __restrict__ qs, const cplx<T>* __restrict__ BR, const cplx<T>* __restrict__ BI,
         cplx<T>* __restrict__ psi, cplx<T>* __restrict__ AR, cplx<T>* __restrict__ AI,
         double2* __restrict__ bscr, int do_psi, int do_A) {
+  using Op = Tri<sizeof(T) == 8>;
   const long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (m >= g.plane) return;
   const int kx = (int)(m % g.KXP);
@@ -494,51 +505,52 @@ k_solve(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
   }
   if (do_psi) {
     const double2* F = fac_psi + (long long)idx * n3;
-    const double s = dz * dz;
+    const double s = __dmul_rn(dz, dz);
     cplx<T> v = qs[m];
-    double br = s * (double)v.x, bi = s * (double)v.y;
+    double br = __dmul_rn(s, (double)v.x), bi = __dmul_rn(s, (double)v.y);
     bscr[m] = make_double2(br, bi);
     for (int i = 1; i < n3; ++i) {
       const double f = F[i - 1].x;
       v = qs[i * P + m];
-      br = s * (double)v.x - f * br;
-      bi = s * (double)v.y - f * bi;
+      br = Op::fwd(__dmul_rn(s, (double)v.x), f, br);
+      bi = Op::fwd(__dmul_rn(s, (double)v.y), f, bi);
       bscr[i * P + m] = make_double2(br, bi);
     }
-    double xr = br * F[n3 - 1].y, xi = bi * F[n3 - 1].y;
+    double xr = Op::last(br, F[n3 - 1].y), xi = Op::last(bi, F[n3 - 1].y);
     psi[(n3 - 1) * P + m] = mk<T>((T)xr, (T)xi);
     for (int i = n3 - 2; i >= 0; --i) {
       const double2 b = bscr[i * P + m];
-      const double rd = F[i].y, u = du[i];
-      xr = (b.x - u * xr) * rd;
-      xi = (b.y - u * xi) * rd;
+      const double p = F[i].y, u = du[i];
+      xr = Op::back(b.x, u, xr, p);
+      xi = Op::back(b.y, u, xi, p);
       psi[i * P + m] = mk<T>((T)xr, (T)xi);
     }
   }
   if (do_A) {
     const double2* F = fac_A + (long long)idx * n3;
-    const double s = dz * dz * Bu;
+    const double s = __dmul_rn(__dmul_rn(dz, dz), Bu);
     cplx<T> vr = BR[m], vi = BI[m];
-    double a0 = s * (double)vr.x, a1 = s * (double)vr.y, b0 = s * (double)vi.x, b1 = s * (double)vi.y;
+    double a0 = __dmul_rn(s, (double)vr.x), a1 = __dmul_rn(s, (double)vr.y);
+    double b0 = __dmul_rn(s, (double)vi.x), b1 = __dmul_rn(s, (double)vi.y);
     bscr[m] = make_double2(a0, a1);
     bscr[n3 * P + m] = make_double2(b0, b1);
     for (int i = 1; i < n3; ++i) {
       const double f = F[i - 1].x;
       vr = BR[i * P + m]; vi = BI[i * P + m];
-      a0 = s * (double)vr.x - f * a0; a1 = s * (double)vr.y - f * a1;
-      b0 = s * (double)vi.x - f * b0; b1 = s * (double)vi.y - f * b1;
+      a0 = Op::fwd(__dmul_rn(s, (double)vr.x), f, a0); a1 = Op::fwd(__dmul_rn(s, (double)vr.y), f, a1);
+      b0 = Op::fwd(__dmul_rn(s, (double)vi.x), f, b0); b1 = Op::fwd(__dmul_rn(s, (double)vi.y), f, b1);
       bscr[i * P + m] = make_double2(a0, a1);
       bscr[(n3 + i) * P + m] = make_double2(b0, b1);
     }
-    const double rdn = F[n3 - 1].y;
-    a0 *= rdn; a1 *= rdn; b0 *= rdn; b1 *= rdn;
+    const double pn = F[n3 - 1].y;
+    a0 = Op::last(a0, pn); a1 = Op::last(a1, pn); b0 = Op::last(b0, pn); b1 = Op::last(b1, pn);
     AR[(n3 - 1) * P + m] = mk<T>((T)a0, (T)a1);
     AI[(n3 - 1) * P + m] = mk<T>((T)b0, (T)b1);
     for (int i = n3 - 2; i >= 0; --i) {
       const double2 x = bscr[i * P + m], y = bscr[(n3 + i) * P + m];
-      const double rd = F[i].y, u = du[i];
-      a0 = (x.x - u * a0) * rd; a1 = (x.y - u * a1) * rd;
-      b0 = (y.x - u * b0) * rd; b1 = (y.y - u * b1) * rd;
+      const double p = F[i].y, u = du[i];
+      a0 = Op::back(x.x, u, a0, p); a1 = Op::back(x.y, u, a1, p);
+      b0 = Op::back(y.x, u, b0, p); b1 = Op::back(y.y, u, b1, p);
       AR[i * P + m] = mk<T>((T)a0, (T)a1);
       AI[i * P + m] = mk<T>((T)b0, (T)b1);
     }
@@ -621,11 +633,15 @@ __global__ void k_sumB(Geom g, cplx<T>* __restrict__ BR, cplx<T>* __restrict__ B
   }
 }
 
-// init_q (init.f90:591-652): q = [d/dz(a dpsi/dz) - kh^2 psi] with Neumann ends.
-template <typename T>
+// init_q (init.f90:591-652): q = [d/dz(a dpsi/dz) - kh^2 psi] with Neumann
+// ends, evaluated in FP64 in the reference's order with correctly rounded
+// operations and no contraction: the terms a*psi (a up to ~e^10 under
+// strong stratification) cancel, so the rounding sequence matters.
+template <typename T, typename TI>
 __global__ void k_init_q(Geom g, double dz, const double* __restrict__ cu, const double* __restrict__ cl,
-                         const cplx<T>* __restrict__ psi, cplx<T>* __restrict__ q) {
+                         const cplx<TI>* __restrict__ psi, cplx<T>* __restrict__ q) {
   const long long tot = (long long)g.n3 * g.plane;
+  const double dz2 = __dmul_rn(dz, dz);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
     const int z = (int)(i / g.plane);
     const long long m = i - (long long)z * g.plane;
@@ -633,24 +649,28 @@ __global__ void k_init_q(Geom g, double dz, const double* __restrict__ cu, const
     const int ky = g.ky_of_row(r);
     cplx<T> out = mk<T>(0, 0);
     if (g.mask(kx, ky)) {
-      const double kdz = (double)(kx * kx + ky * ky) * dz * dz;
-      const cplx<T> p0 = psi[i];
+      const double kdz = __dmul_rn(__dmul_rn((double)(kx * kx + ky * ky), dz), dz);
+      const cplx<TI> p0 = psi[i];
       double vr, vi;
       if (z == 0) {
-        const cplx<T> pp = psi[i + g.plane];
-        vr = cu[0] * pp.x - (cu[0] + kdz) * p0.x;
-        vi = cu[0] * pp.y - (cu[0] + kdz) * p0.y;
+        const cplx<TI> pp = psi[i + g.plane];
+        const double d = __dadd_rn(cu[0], kdz);
+        vr = __dsub_rn(__dmul_rn(cu[0], (double)pp.x), __dmul_rn(d, (double)p0.x));
+        vi = __dsub_rn(__dmul_rn(cu[0], (double)pp.y), __dmul_rn(d, (double)p0.y));
       } else if (z == g.n3 - 1) {
-        const cplx<T> pm = psi[i - g.plane];
-        vr = -(cl[z] + kdz) * p0.x + cl[z] * pm.x;
-        vi = -(cl[z] + kdz) * p0.y + cl[z] * pm.y;
+        const cplx<TI> pm = psi[i - g.plane];
+        const double d = __dadd_rn(cl[z], kdz);
+        vr = __dadd_rn(-__dmul_rn(d, (double)p0.x), __dmul_rn(cl[z], (double)pm.x));
+        vi = __dadd_rn(-__dmul_rn(d, (double)p0.y), __dmul_rn(cl[z], (double)pm.y));
       } else {
-        const cplx<T> pp = psi[i + g.plane], pm = psi[i - g.plane];
-        const double dd = cu[z] + cl[z];
-        vr = cu[z] * pp.x - (dd + kdz) * p0.x + cl[z] * pm.x;
-        vi = cu[z] * pp.y - (dd + kdz) * p0.y + cl[z] * pm.y;
+        const cplx<TI> pp = psi[i + g.plane], pm = psi[i - g.plane];
+        const double d = __dadd_rn(__dadd_rn(cu[z], cl[z]), kdz);
+        vr = __dadd_rn(__dsub_rn(__dmul_rn(cu[z], (double)pp.x), __dmul_rn(d, (double)p0.x)),
+                       __dmul_rn(cl[z], (double)pm.x));
+        vi = __dadd_rn(__dsub_rn(__dmul_rn(cu[z], (double)pp.y), __dmul_rn(d, (double)p0.y)),
+                       __dmul_rn(cl[z], (double)pm.y));
       }
-      out = mk<T>((T)(vr / (dz * dz)), (T)(vi / (dz * dz)));
+      out = mk<T>((T)__ddiv_rn(vr, dz2), (T)__ddiv_rn(vi, dz2));
     }
     q[i] = out;
   }

@@ -152,7 +152,7 @@ def make_initial_condition(rc: RunConfig) -> InitialCondition:
 
     psi: |psi_k| ~ exp(-(k/k0)^2/2)/k (energy spectrum ~ k exp(-(k/k0)^2)),
     independent uniform phases for a barotropic part and a first-baroclinic
-    part sqrt(2) cos(pi zs) of equal energy, scaled so rms(zeta) = 1
+    part of equal energy, scaled so rms(zeta) = 1
     (flow Rossby number = Ro).  B = exp(-((1-zs)/wave_depth)^2) at kh=0
     (LA = B there, wave velocity amplitude 1, W2F = 1).  delt from the
     advective CFL number on the initial velocity.
@@ -172,7 +172,7 @@ def make_initial_condition(rc: RunConfig) -> InitialCondition:
     P_bt = amp * np.exp(1j * ph_bt)
     P_bc = amp * np.exp(1j * ph_bc)
     zs = (np.arange(1, n3 + 1) - 0.5) * rc.dz
-    vert = np.sqrt(2.0) * np.cos(np.pi * zs)
+    vert = first_baroclinic_mode(rc)
     psi = P_bt[None] + vert[:, None, None] * P_bc[None]
     psi = np.where(L[None], psi, 0)
     # rms vorticity over the volume
@@ -198,6 +198,24 @@ def make_initial_condition(rc: RunConfig) -> InitialCondition:
     BR[:, 0, 0] = np.exp(-((1.0 - zs) / rc.wave_depth) ** 2)
     BI = np.zeros_like(BR)
     return InitialCondition(psi=psi.astype(np.complex128), BR=BR, BI=BI, delt=float(delt), umax=umax)
+
+
+def first_baroclinic_mode(rc: RunConfig) -> np.ndarray:
+    """First baroclinic eigenvector of the discrete vertical operator of
+    psi_solver (elliptic.f90:177-189 without the kh^2 term, Neumann ends),
+    normalised to mean square 1 and positive at the bottom.  For constant
+    N^2 it is sqrt(2) cos(pi zs)."""
+    from scipy.linalg import eigh_tridiagonal
+    a = rc.a_ell_ut()
+    n3 = rc.n3
+    d = np.empty(n3)
+    d[0] = -a[0]
+    d[1:-1] = -(a[1:-1] + a[:-2])
+    d[-1] = -a[-2]
+    w, v = eigh_tridiagonal(d, a[:-1])
+    phi = v[:, -2]                       # eigenvalues ascending: -2 = first nonzero
+    phi = phi / np.sqrt(np.mean(phi * phi))
+    return phi if phi[0] > 0 else -phi
 
 
 def model_parameters(rc: RunConfig, delt: float) -> dict:

@@ -91,11 +91,13 @@ def test_solver_dropins(strat, precision):
     rc = scaled(CONFIGS[strat], 64, 32)
     model, st, sim = pair(rc, precision)
     q = random_masked(64, 32, 7)
-    tol = (1e-12 if strat == "c0" else 1e-11) if precision == "fp64" else 2e-6
-    assert rel_l2(sim.psi_solver(q), model.psi_solver(q)) < tol
+    # FP64: DGTSV's arithmetic is reproduced exactly; mixed: FP32 inputs,
+    # and C = A_z (a difference) loses a further two digits
+    tol, tolc = (1e-15, 1e-15) if precision == "fp64" else (2e-6, 1e-4)
+    assert rel_l2(sim.psi_solver(q), model.psi_solver(q)) <= tol
     A, Cz = sim.A_solver_ybj_plus(q)
     Ae, Ce = model.A_solver_ybj_plus(q)
-    assert rel_l2(A, Ae) < tol and rel_l2(Cz, Ce) < tol
+    assert rel_l2(A, Ae) <= tol and rel_l2(Cz, Ce) <= tolc
     sim.close()
 
 
