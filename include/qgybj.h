@@ -108,7 +108,8 @@ int qg_create(const qg_config* cfg, qg_handle** out);
 /* Replaces kill_fftw (fft.f90:112-119). */
 int qg_destroy(qg_handle* h);
 
-/* Text of the last error on h (or of the last qg_create failure when h is NULL). */
+/* Text of the last error on h, or, when h is NULL, of the last failed call
+ * made without a handle on this thread (qg_create, qg_fft_c2r_noalloc). */
 const char* qg_last_error(const qg_handle* h);
 
 /* Host <-> device copies of the resident state, levels [level0, level0+nlev).
@@ -177,6 +178,29 @@ int qg_compute_qw(qg_handle* h, const double* BRk, const double* BIk, double* qw
 int qg_psi_solver(qg_handle* h, const double* qstar, double* psik);
 /* elliptic.f90:346-460: all n3 levels; ck may be NULL. */
 int qg_A_solver_ybj_plus(qg_handle* h, const double* bk, double* ak, double* ck);
+
+/* Allocation-free variant of qg_fft_c2r.  No counterpart in the reference.
+ * For callers that cannot allocate device memory: a host whose device memory
+ * is fixed at start-up under a hard cap shared with other processes on the
+ * GPU, or a host loop that cannot pay for cudaMalloc/cudaFree (cudaFree
+ * synchronises the whole device and would stall work on other streams).
+ * The caller owns both buffers; the call allocates nothing (no cudaMalloc,
+ * cudaFree or allocating library routine).  FP64.
+ *   kvar: device pointer, interleaved complex [nz][n][n/2+1] (read only)
+ *   rvar: device pointer, double [nz][n][n+2]; the two padding values per row are 0
+ * The (kx,y) intermediate lives in a file-scope 8 MiB static device array,
+ * held by every GPU that loads the library until the process exits: n must
+ * be a power of two in [16, 512] so that one level's plane fits, otherwise
+ * QG_ERR_UNSUPPORTED; levels are transformed in chunks, so any nz works.
+ * The work is queued on `stream` (a cudaStream_t; NULL = the legacy default
+ * stream) and the call returns without synchronising.  The first call on a
+ * device does a one-time set-up with that device current (device addresses
+ * of the static arrays, twiddle upload, kernel attributes); make that first
+ * call before any stream capture.  All calls share the one static scratch:
+ * calls that overlap on the GPU (unordered streams) race, so order them on
+ * one stream.  Each call writes every scratch element before reading it, so
+ * nothing needs clearing between calls.  Errors: qg_last_error(NULL). */
+int qg_fft_c2r_noalloc(const double* kvar, double* rvar, int n, int nz, void* stream);
 
 #ifdef __cplusplus
 }

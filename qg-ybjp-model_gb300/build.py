@@ -18,7 +18,7 @@ OUTDIR = HERE / "qgybj"
 BUILD = HERE / "_build"
 LIB = OUTDIR / "libqgybj.so"
 
-UNITS = ["capi", "engine_fp32", "engine_fp64"]
+UNITS = ["capi", "engine_fp32", "engine_fp64", "noalloc"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code: no floating-point contraction, so the host-built tables (DGTSV
 # factors, integrating factors) round identically on x86-64 and aarch64

@@ -196,6 +196,7 @@ int build_tables(const qg_config& c, qg::HostTables& t, std::string& err) {
 }  // namespace
 
 namespace qg {
+void set_handleless_error(const std::string& msg) { g_create_err = msg; }
 bool supported_n(int n) { return n == 16 || n == 32 || n == 64 || n == 128 || n == 256 || n == 512 || n == 1024; }
 }  // namespace qg
 

@@ -64,6 +64,30 @@ k_drow_c2r(int iktxP, const cplx<T>* __restrict__ W, T* __restrict__ phys, const
   }
 }
 
+// Same transform as k_drow_c2r, written straight into the reference's padded
+// physical layout double[nz][N][N+2] (the two padding values of a row are 0).
+template <typename T, int N>
+__global__ void __launch_bounds__(kThreads)
+k_drow_c2r_pad(int iktxP, const cplx<T>* __restrict__ W, double* __restrict__ out, const cplx<T>* __restrict__ twg) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
+  cplx<T>* bA = tw + N;
+  cplx<T>* bB = bA + N;
+  const int z = blockIdx.y, y0 = 2 * blockIdx.x;
+  load_twiddles<T, N>(tw, twg);
+  const cplx<T>* X = W + ((long long)z * N + y0) * iktxP;
+  const cplx<T>* Y = X + iktxP;
+  for (int k = threadIdx.x; k < N; k += blockDim.x) bA[k] = pack_full<T>(X, Y, k, N);
+  __syncthreads();
+  cplx<T>* res = block_fft<T, N, false>(bA, bB, N, 1, tw);
+  double* r0 = out + ((long long)z * N + y0) * (N + 2);
+  double* r1 = r0 + (N + 2);
+  for (int x = threadIdx.x; x < N + 2; x += blockDim.x) {
+    r0[x] = x < N ? (double)res[x].x : 0.0;
+    r1[x] = x < N ? (double)res[x].y : 0.0;
+  }
+}
+
 template <typename T, int N>
 __global__ void __launch_bounds__(kThreads)
 k_drow_r2c(int iktxP, const T* __restrict__ phys, cplx<T>* __restrict__ W, const cplx<T>* __restrict__ twg) {

@@ -50,4 +50,8 @@ EngineBase* make_engine_fp64();
 
 bool supported_n(int n);
 
+// Error text of calls made without a handle (qg_create, qg_fft_c2r_noalloc),
+// returned by qg_last_error(NULL) on the calling thread.
+void set_handleless_error(const std::string& msg);
+
 }  // namespace qg

@@ -23,7 +23,7 @@ EXPORTS = (
     "qg_config_defaults", "qg_create", "qg_destroy", "qg_last_error", "qg_set_state", "qg_get_state",
     "qg_init_state", "qg_step", "qg_steps_async", "qg_synchronize", "qg_get_stream", "qg_diagnostics_fp64",
     "qg_fft_r2c", "qg_fft_c2r", "qg_convol_waqg", "qg_refraction_waqg", "qg_compute_qw", "qg_psi_solver",
-    "qg_A_solver_ybj_plus", "qg_profile_step",
+    "qg_A_solver_ybj_plus", "qg_profile_step", "qg_fft_c2r_noalloc",
 )
 KERNEL_CLASSES = ("dissipation", "col_inv", "row_main", "col_update", "row_qw", "col_qw", "solve")
 
@@ -81,6 +81,7 @@ def lib() -> C.CDLL:
         "qg_psi_solver": (ip, [vp, vp, vp]),
         "qg_A_solver_ybj_plus": (ip, [vp, vp, vp, vp]),
         "qg_profile_step": (ip, [vp, ip, dp, C.POINTER(C.c_int), ip]),
+        "qg_fft_c2r_noalloc": (ip, [vp, vp, ip, ip, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
