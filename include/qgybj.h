@@ -62,7 +62,7 @@ enum qg_field {
  * the step reads (parameters_test1.f90) plus the base state of
  * init_base_state (init.f90:177-264).  Arrays are copied by qg_create. */
 typedef struct qg_config {
-  int n1, n2, n3;          /* resolution; n1 == n2, a power of two in [16,1024]; n3 >= 2 */
+  int n1, n2, n3;          /* resolution; n1 == n2, a power of two in [16,1024]; 2 <= n3 <= 4096 */
   int precision;           /* enum qg_precision                                        */
   int device;              /* CUDA device ordinal                                      */
   /* physics switches (parameters_test1.f90:22-29) */

@@ -150,10 +150,11 @@ int build_tables(const qg_config& c, qg::HostTables& t, std::string& err) {
       if (kh2 != 0 && kh2 <= kmax2 && !(kx == 0 && ky < 0)) t.tab_idx[(size_t)r * t.KXP + kx] = idx[kh2];
     }
   }
-  t.fac_psi.assign((size_t)nd * n3 * 2, 0.0);
-  t.fac_A.assign((size_t)nd * n3 * 2, 0.0);
+  t.fac_psi.assign((size_t)nd * n3 * 4, 0.0);
+  t.fac_A.assign((size_t)nd * n3 * 4, 0.0);
   std::vector<double> d(n3), dl(n3), du(n3);
-  // FP64 path: {f_i, d'_i} for DGTSV's exact arithmetic; mixed path: {f_i, 1/d'_i}
+  // FP64 path: {f_i, d'_i, 0, 0} for DGTSV's exact arithmetic;
+  // mixed path: {f_i, s/d'_i, u_i/d'_i, 0} with s the RHS scaling of the operator
   const bool exact = c.precision == QG_PREC_FP64;
   for (auto& kv : idx) {
     for (int op = 0; op < 2; ++op) {
@@ -172,7 +173,8 @@ int build_tables(const qg_config& c, qg::HostTables& t, std::string& err) {
         }
       }
       // DGTSV elimination order without row interchanges
-      double* out = (op == 0 ? t.fac_psi.data() : t.fac_A.data()) + (size_t)kv.second * n3 * 2;
+      double* out = (op == 0 ? t.fac_psi.data() : t.fac_A.data()) + (size_t)kv.second * n3 * 4;
+      const double s = op == 0 ? c.dz * c.dz : c.dz * c.dz * c.Bu;
       double dp = d[0];
       for (int i = 0; i < n3 - 1; ++i) {
         if (dp == 0.0) { err = "zero pivot in tridiagonal factorisation (kh2=" + std::to_string(kv.first) + ")"; return QG_ERR_PIVOT; }
@@ -181,13 +183,15 @@ int build_tables(const qg_config& c, qg::HostTables& t, std::string& err) {
           return QG_ERR_PIVOT;
         }
         const double f = dl[i] / dp;
-        out[2 * i] = f;
-        out[2 * i + 1] = exact ? dp : 1.0 / dp;
+        out[4 * i] = f;
+        out[4 * i + 1] = exact ? dp : s / dp;
+        out[4 * i + 2] = exact ? 0.0 : du[i] / dp;
         dp = d[i + 1] - f * du[i];
       }
       if (dp == 0.0 || !std::isfinite(dp)) { err = "zero pivot in tridiagonal factorisation"; return QG_ERR_PIVOT; }
-      out[2 * (n3 - 1)] = 0.0;
-      out[2 * (n3 - 1) + 1] = exact ? dp : 1.0 / dp;
+      out[4 * (n3 - 1)] = 0.0;
+      out[4 * (n3 - 1) + 1] = exact ? dp : s / dp;
+      out[4 * (n3 - 1) + 2] = 0.0;
     }
   }
   return QG_OK;
@@ -221,6 +225,7 @@ int qg_create(const qg_config* cfg, qg_handle** out) {
   if (c.n1 != c.n2) return fail(nullptr, QG_ERR_UNSUPPORTED, "n1 must equal n2");
   if (!qg::supported_n(c.n1)) return fail(nullptr, QG_ERR_UNSUPPORTED, "n1 must be a power of two in [16,1024]");
   if (c.n3 < 2) return fail(nullptr, QG_ERR_ARG, "n3 must be >= 2");
+  if (c.n3 > 4096) return fail(nullptr, QG_ERR_UNSUPPORTED, "n3 must be <= 4096 (one column's FP64 solve in shared memory)");
   if (c.precision != QG_PREC_FP64 && c.precision != QG_PREC_MIXED) return fail(nullptr, QG_ERR_ARG, "bad precision");
   if (c.ybj_plus != 1) return fail(nullptr, QG_ERR_UNSUPPORTED, "only the YBJ+ step (ybj_plus=1) is implemented");
   if (!c.a_ell_ut) return fail(nullptr, QG_ERR_ARG, "a_ell_ut is required");

@@ -74,12 +74,12 @@ class Engine final : public EngineBase {
     QG_CK(cudaMemcpy(tw, twh.data(), g.n * sizeof(C), cudaMemcpyHostToDevice));
     QG_CK(cudaMalloc(&tab_idx, g.plane * sizeof(int)));
     QG_CK(cudaMemcpy(tab_idx, t.tab_idx.data(), g.plane * sizeof(int), cudaMemcpyHostToDevice));
-    const size_t fb = std::max<size_t>(1, (size_t)t.ndistinct * g.n3) * sizeof(double2);
+    const size_t fb = std::max<size_t>(1, (size_t)t.ndistinct * g.n3) * sizeof(double4);
     QG_CK(cudaMalloc(&fac_psi, fb));
     QG_CK(cudaMalloc(&fac_A, fb));
     if (t.ndistinct > 0) {
-      QG_CK(cudaMemcpy(fac_psi, t.fac_psi.data(), (size_t)t.ndistinct * g.n3 * sizeof(double2), cudaMemcpyHostToDevice));
-      QG_CK(cudaMemcpy(fac_A, t.fac_A.data(), (size_t)t.ndistinct * g.n3 * sizeof(double2), cudaMemcpyHostToDevice));
+      QG_CK(cudaMemcpy(fac_psi, t.fac_psi.data(), (size_t)t.ndistinct * g.n3 * sizeof(double4), cudaMemcpyHostToDevice));
+      QG_CK(cudaMemcpy(fac_A, t.fac_A.data(), (size_t)t.ndistinct * g.n3 * sizeof(double4), cudaMemcpyHostToDevice));
     }
     auto upd = [&](double** d, const std::vector<double>& h) -> int {
       QG_CK(cudaMalloc(d, h.size() * sizeof(double)));
@@ -87,7 +87,6 @@ class Engine final : public EngineBase {
       return QG_OK;
     };
     if ((rc = upd(&du, t.du)) || (rc = upd(&cu, t.cu)) || (rc = upd(&cl, t.cl)) || (rc = upd(&r2, t.r2))) return rc;
-    QG_CK(cudaMalloc(&bscr, (size_t)2 * g.n3 * g.plane * sizeof(double2)));
     QG_CK(cudaMalloc(&diag_part, (size_t)g.n3 * kNDiag * sizeof(double)));
     QG_CK(cudaMalloc(&diag_out, kNDiag * sizeof(double)));
     QG_CK(cudaMallocHost(&diag_host, kNDiag * sizeof(double)));
@@ -351,7 +350,8 @@ class Engine final : public EngineBase {
   T *e1 = nullptr, *e2 = nullptr, *e1w = nullptr, *e2w = nullptr;
   C* tw = nullptr;
   int* tab_idx = nullptr;
-  double2 *fac_psi = nullptr, *fac_A = nullptr, *bscr = nullptr;
+  double4 *fac_psi = nullptr, *fac_A = nullptr;
+  double2* bscr = nullptr;
   double *du = nullptr, *cu = nullptr, *cl = nullptr, *r2 = nullptr;
   double *diag_part = nullptr, *diag_out = nullptr, *diag_host = nullptr;
   C* S = nullptr;
@@ -424,6 +424,7 @@ class Engine final : public EngineBase {
       QG_CK(cudaFuncSetAttribute(k_col_update<T, NN>, (cudaFuncAttribute)mx, (int)sm_col6<NN>()));
       QG_CK(cudaFuncSetAttribute(k_row_qw<T, NN>, (cudaFuncAttribute)mx, (int)sm_row4<NN>()));
       QG_CK(cudaFuncSetAttribute(k_col_qw<T, NN>, (cudaFuncAttribute)mx, (int)sm_col2<NN>()));
+      QG_CK(cudaFuncSetAttribute(k_solve<T>, (cudaFuncAttribute)mx, (int)solve_smem(g.n3)));
       QG_CK(cudaFuncSetAttribute(k_dcol_inv<T, NN>, (cudaFuncAttribute)mx, (int)sm_colinv()));
       QG_CK(cudaFuncSetAttribute(k_dcol_fwd<T, NN>, (cudaFuncAttribute)mx, (int)sm_colinv()));
       QG_CK(cudaFuncSetAttribute(k_drow_c2r<T, NN>, (cudaFuncAttribute)mx, (int)sm_drow()));
@@ -534,8 +535,8 @@ class Engine final : public EngineBase {
 
   int solve_generic(const C* qs, const C* br, const C* bi, C* psi, C* ar, C* ai, int do_psi, int do_A) {
     if (!do_psi && !do_A) return QG_OK;
-    k_solve<T><<<(unsigned)((g.plane + 127) / 128), 128, 0, st>>>(g, cfg.dz, cfg.Bu, tab_idx, fac_psi, fac_A, du, qs,
-                                                                  br, bi, psi, ar, ai, bscr, do_psi, do_A);
+    k_solve<T><<<(unsigned)((g.plane + kSolveTC - 1) / kSolveTC), kSolveThreads, solve_smem(g.n3), st>>>(g, cfg.dz, cfg.Bu, tab_idx, fac_psi, fac_A,
+                                                                           du, qs, br, bi, psi, ar, ai, do_psi, do_A);
     QG_LAUNCHED();
     return QG_OK;
   }

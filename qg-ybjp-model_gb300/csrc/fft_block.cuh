@@ -138,6 +138,31 @@ namespace qg {
 __host__ __device__ __forceinline__ constexpr int pad_idx(int i) { return i + (i >> 4); }
 template <int N> struct PadLD { static constexpr int value = N + (N >> 4); };
 
+// Twiddles laid out per pass: the pass with stride NS and radix R reads
+// W_N^{k r N/(NS R)} at tw[off(NS) + (r-1)*NS + k], so the threads of a warp
+// (consecutive k) read consecutive words.  Fewer than N entries in total.
+__host__ __device__ constexpr int radix_of(int rem) { return rem >= 8 ? 8 : (rem >= 4 ? 4 : 2); }
+template <int N> __host__ __device__ constexpr int tw_off(int ns) {
+  int off = 0;
+  for (int s = 1; s < ns; s *= radix_of(N / s)) if (s > 1) off += s * (radix_of(N / s) - 1);
+  return off;
+}
+
+template <typename T, int N, int NS>
+__device__ __forceinline__ void load_tw_passes(cplx<T>* tw_s, const cplx<T>* __restrict__ tw_g, int nt) {
+  if constexpr (NS < N) {
+    constexpr int R = radix_of(N / NS);
+    if constexpr (NS > 1) {
+      constexpr int off = tw_off<N>(NS);
+      for (int i = threadIdx.x; i < NS * (R - 1); i += nt) {
+        const int r = 1 + i / NS, k = i % NS;
+        tw_s[off + i] = tw_g[k * r * (N / (NS * R))];
+      }
+    }
+    load_tw_passes<T, N, NS * R>(tw_s, tw_g, nt);
+  }
+}
+
 template <typename T, int N, int R, int NS, bool FWD, int BATCH, int NT>
 __device__ __forceinline__ void ip_pass(cplx<T>* __restrict__ buf, const cplx<T>* __restrict__ tw) {
   constexpr int NB = N / R;
@@ -164,9 +189,10 @@ __device__ __forceinline__ void ip_pass(cplx<T>* __restrict__ buf, const cplx<T>
       const int b = t / NB, j = t % NB;
       const int k = j & (NS - 1);
       if constexpr (NS > 1) {
+        constexpr int off = tw_off<N>(NS);
 #pragma unroll
         for (int r = 1; r < R; ++r) {
-          cplx<T> w = tw[k * r * (N / (NS * R))];
+          cplx<T> w = tw[off + (r - 1) * NS + k];
           if (!FWD) w.y = -w.y;
           v[p][r] = cmul(v[p][r], w);
         }

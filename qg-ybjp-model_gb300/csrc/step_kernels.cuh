@@ -49,9 +49,10 @@ template <typename T, int N> struct Tiles {
 constexpr int kColThreads = 256;   // k_col_inv, k_col_update
 constexpr int kThreadsB = 256;     // row kernels, k_col_qw
 
+// per-pass twiddle table of fft_ip (at most N entries)
 template <typename T, int N>
 __device__ __forceinline__ void load_tw(cplx<T>* tw_s, const cplx<T>* __restrict__ tw_g, int nt) {
-  for (int i = threadIdx.x; i < N; i += nt) tw_s[i] = tw_g[i];
+  load_tw_passes<T, N, 1>(tw_s, tw_g, nt);
 }
 
 // ===========================================================================
@@ -232,61 +233,61 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
   __syncthreads();
   fft_ip<T, N, true, 3 * CT, NT>(buf, tw);
   fft_ip<T, N, true, 3 * CT, NT>(buf + 3 * CT * LD, tw);
-  // tendencies and time update (main_waqg.f90:237-264, 362-415)
+  // tendencies and time update (main_waqg.f90:237-264, 362-415): one mode
+  // (column c, row r) per iteration, all of its loads issued together
   const T inv_n2 = (T)1 / ((T)N * (T)N);
   const long long zoff = (long long)z * g.plane;
   const T dt = (T)sp.delt;
+  const T dt2 = (T)2 * dt;
   const T gam = (T)sp.gamma;
   const T cdisp = sp.disp ? (T)sp.cdisp : (T)0;
-  for (int e = tid; e < 3 * CT * KY; e += NT) {
-    const int c = e % CT, r = (e / CT) % KY, X = e / (CT * KY);
+  const bool eul = sp.euler != 0;
+#pragma unroll 2
+  for (int e = tid; e < CT * KY; e += NT) {
+    const int c = e % CT, r = e / CT;
     const int kx = kx0 + c;
     if (kx > g.K) continue;
     const int ky = g.ky_of_row(r);
-    const int j = pad_idx(g.fft_index_of_row(r));
-    const cplx<T> G = buf[((2 * X) * CT + c) * LD + j];
-    const cplx<T> H = buf[((2 * X + 1) * CT + c) * LD + j];
-    const cplx<T> tend = cscale(mk<T>(G.x - (T)ky * H.y, G.y + (T)ky * H.x), inv_n2);   // G + i ky H
     const long long m = zoff + (long long)r * g.KXP + kx;
     const long long mt = (long long)r * g.KXP + kx;
-    const bool L = g.mask(kx, ky);
-    const T kh2 = (T)(kx * kx + ky * ky);
-    cplx<T>* cur = X == 0 ? st.q : (X == 1 ? st.BR : st.BI);
-    cplx<T>* old = X == 0 ? st.qo : (X == 1 ? st.BRo : st.BIo);
-    const cplx<T> xc = cur[m];
-    const cplx<T> xo = sp.euler ? xc : old[m];
-    cplx<T> xn = mk<T>(0, 0), xf = mk<T>(0, 0);
-    if (L) {
-      if (X == 0) {
-        const T e1 = e1t[mt], e2 = e2t[mt];
-        const cplx<T> dqv = sp.use_dq ? st.dq[m] : mk<T>(0, 0);
-        if (sp.euler) {
-          xn = cscale(cadd(csub(xo, cscale(tend, dt)), cscale(dqv, dt)), e1);
-        } else {
-          xn = cadd(csub(cscale(xo, e2), cscale(cscale(tend, (T)2 * dt), e1)), cscale(cscale(dqv, (T)2 * dt), e2));
-        }
-      } else {
-        const T e1 = e1wt[mt], e2 = e2wt[mt];
-        // BR: tend_BR + c kh2 AI ; BI: tend_BI - c kh2 AR
-        const cplx<T> Av = X == 1 ? st.AI[m] : st.AR[m];
-        const T sgn = X == 1 ? (T)1 : (T)-1;
-        const cplx<T> full = cadd(tend, cscale(Av, sgn * cdisp * kh2));
-        if (sp.euler) {
-          xn = cscale(csub(xo, cscale(full, dt)), e1);
-        } else {
-          xn = csub(cscale(xo, e2), cscale(cscale(full, (T)2 * dt), e1));
-        }
-      }
-      if (sp.euler) {
-        xf = xo;      // old level <- current (main_waqg.f90:232-234)
-      } else {        // Robert-Asselin filter (main_waqg.f90:395-410)
-        xf = cadd(xc, cscale(cadd(csub(xo, cscale(xc, (T)2)), xn), gam));
-      }
-    } else if (sp.euler) {
-      xf = xo;
+    const cplx<T> q0 = st.q[m], r0 = st.BR[m], i0 = st.BI[m];
+    const cplx<T> qo = eul ? q0 : st.qo[m], ro = eul ? r0 : st.BRo[m], io = eul ? i0 : st.BIo[m];
+    const cplx<T> ar = st.AR[m], ai = st.AI[m];
+    const cplx<T> dqv = sp.use_dq ? st.dq[m] : mk<T>(0, 0);
+    const T e1 = e1t[mt], e2 = e2t[mt], e1w = e1wt[mt], e2w = e2wt[mt];
+    const int j = pad_idx(g.fft_index_of_row(r));
+    cplx<T> tq, tr, ti;
+    {
+      const cplx<T> G0 = buf[(0 * CT + c) * LD + j], H0 = buf[(1 * CT + c) * LD + j];
+      const cplx<T> G1 = buf[(2 * CT + c) * LD + j], H1 = buf[(3 * CT + c) * LD + j];
+      const cplx<T> G2 = buf[(4 * CT + c) * LD + j], H2 = buf[(5 * CT + c) * LD + j];
+      const T fky = (T)ky;
+      tq = cscale(mk<T>(G0.x - fky * H0.y, G0.y + fky * H0.x), inv_n2);   // G + i ky H
+      tr = cscale(mk<T>(G1.x - fky * H1.y, G1.y + fky * H1.x), inv_n2);
+      ti = cscale(mk<T>(G2.x - fky * H2.y, G2.y + fky * H2.x), inv_n2);
     }
-    cur[m] = xn;
-    old[m] = xf;
+    cplx<T> qn = mk<T>(0, 0), rn = mk<T>(0, 0), in_ = mk<T>(0, 0);
+    cplx<T> qf = eul ? qo : mk<T>(0, 0), rf = eul ? ro : mk<T>(0, 0), if_ = eul ? io : mk<T>(0, 0);
+    if (g.mask(kx, ky)) {
+      const T ck = cdisp * (T)(kx * kx + ky * ky);
+      const cplx<T> fr = cadd(tr, cscale(ai, ck));     // nBR - 0.5 rBI + c kh2 AI
+      const cplx<T> fi = csub(ti, cscale(ar, ck));     // nBI + 0.5 rBR - c kh2 AR
+      if (eul) {
+        qn = cscale(cadd(csub(qo, cscale(tq, dt)), cscale(dqv, dt)), e1);
+        rn = cscale(csub(ro, cscale(fr, dt)), e1w);
+        in_ = cscale(csub(io, cscale(fi, dt)), e1w);
+      } else {
+        qn = cadd(csub(cscale(qo, e2), cscale(cscale(tq, dt2), e1)), cscale(cscale(dqv, dt2), e2));
+        rn = csub(cscale(ro, e2w), cscale(cscale(fr, dt2), e1w));
+        in_ = csub(cscale(io, e2w), cscale(cscale(fi, dt2), e1w));
+        // Robert-Asselin filter (main_waqg.f90:395-410)
+        qf = cadd(q0, cscale(cadd(csub(qo, cscale(q0, (T)2)), qn), gam));
+        rf = cadd(r0, cscale(cadd(csub(ro, cscale(r0, (T)2)), rn), gam));
+        if_ = cadd(i0, cscale(cadd(csub(io, cscale(i0, (T)2)), in_), gam));
+      }
+    }
+    st.q[m] = qn; st.BR[m] = rn; st.BI[m] = in_;
+    st.qo[m] = qf; st.BRo[m] = rf; st.BIo[m] = if_;
   }
   if (!qw_prep) return;
   __syncthreads();   // this CTA's writes of BR, BI are visible to it after the barrier
@@ -464,95 +465,136 @@ __global__ void k_dissipation(Geom g, double nuz, double dz, const cplx<T>* __re
 // ===========================================================================
 // Phase B: FP64 tridiagonal solves per (kx,ky) column (elliptic.f90:145-460)
 // ===========================================================================
-// fac[idx*n3 + i] = {f_i = dl_i/d'_i, p_i} of DGTSV's elimination for the
-// distinct kh^2 row idx; du[i] = rho_ut(i)*a(i)/rho_st(i).
-//   EXACT (FP64 path): p_i = d'_i, and every operation is the correctly
-//     rounded IEEE operation of DGTSV (no contraction, true division), so
-//     the solve reproduces LAPACK's reference DGTSV bit for bit.
-//   fast (mixed path): p_i = 1/d'_i, fused multiply-adds.
-template <bool EXACT>
-struct Tri {
-  static __device__ __forceinline__ double fwd(double b, double f, double bp) {
-    return EXACT ? __dsub_rn(b, __dmul_rn(f, bp)) : fma(-f, bp, b);
-  }
-  static __device__ __forceinline__ double back(double b, double u, double x, double p) {
-    return EXACT ? __ddiv_rn(__dsub_rn(b, __dmul_rn(u, x)), p) : fma(-u, x, b) * p;
-  }
-  static __device__ __forceinline__ double last(double b, double p) { return EXACT ? __ddiv_rn(b, p) : b * p; }
-};
+// Elimination factors of DGTSV for the distinct kh^2 row idx, one double4
+// per level i:
+//   EXACT (FP64 path): {f_i = dl_i/d'_i, d'_i, -, -}; every operation is the
+//     correctly rounded IEEE operation of DGTSV (no contraction, true
+//     division), so the solve reproduces LAPACK's reference DGTSV bit for bit.
+//   fast (mixed path): {f_i, s/d'_i, u_i/d'_i, -} with s the RHS scaling
+//     (dz^2 or dz^2 Bu) and u_i = rho_ut(i) a(i)/rho_st(i): the forward sweep
+//     runs on the unscaled RHS, c_i = b_i - f_{i-1} c_{i-1}, and the back
+//     substitution is one fused multiply-add on the recurrence,
+//     x_i = fma(-(u_i/d'_i), x_{i+1}, (s/d'_i) c_i).
+// The FP32 <-> FP64 conversions of the mixed path are done with integer
+// operations (exact, round-to-nearest-even like the hardware conversions),
+// which keeps them off the FP64 pipe that bounds this kernel.
+__device__ __forceinline__ double f32_to_f64(float v) {
+  const unsigned b = __float_as_uint(v);
+  const unsigned e = (b >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) return (double)v;              // zero, subnormal, inf, nan: hardware
+  const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
+  return __hiloint2double((int)hi, (int)(b << 29));
+}
+__device__ __forceinline__ float f64_to_f32(double v) {
+  const unsigned hi = (unsigned)__double2hiint(v), lo = (unsigned)__double2loint(v);
+  const int e = (int)((hi >> 20) & 0x7ffu) - 896;
+  if (e <= 0 || e >= 255) return (float)v;                  // zero, subnormal, overflow, inf, nan: hardware
+  unsigned r = (hi & 0x80000000u) | ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+  const unsigned rest = lo & 0x1fffffffu;                   // the 29 dropped mantissa bits
+  if (rest > 0x10000000u || (rest == 0x10000000u && (r & 1u))) r += 1u;   // nearest, ties to even
+  return __uint_as_float(r);
+}
+template <typename T> __device__ __forceinline__ double to64(T v) { return (double)v; }
+template <> __device__ __forceinline__ double to64<float>(float v) { return f32_to_f64(v); }
+template <typename T> __device__ __forceinline__ T from64(double v) { return (T)v; }
+template <> __device__ __forceinline__ float from64<float>(double v) { return f64_to_f32(v); }
+
+// Thread (chain, c) of a CTA runs one real recurrence (chain = 2*rhs +
+// {re, im}; rhs = q*->psi, BR->AR, BI->AI) of column c of TC consecutive
+// columns.  The forward sweep keeps only a checkpoint every kSeg levels (in
+// shared memory); the back substitution recomputes each kSeg-level segment
+// from its checkpoint in registers and then substitutes through it.  One
+// extra FMA per level buys a kernel with no scratch traffic and many warps.
+constexpr int kSeg = 8;
+constexpr int kSolveTC = 32;
+constexpr int kSolveThreads = 6 * kSolveTC;
+
+__host__ __device__ constexpr size_t solve_smem(int n3) {
+  return (size_t)n3 * 8 + (size_t)((n3 + kSeg - 1) / kSeg) * kSolveThreads * 8;
+}
 
 template <typename T>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(kSolveThreads, 3)
 k_solve(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
-        const double2* __restrict__ fac_psi, const double2* __restrict__ fac_A, const double* __restrict__ du,
+        const double4* __restrict__ fac_psi, const double4* __restrict__ fac_A, const double* __restrict__ du,
         const cplx<T>* __restrict__ qs, const cplx<T>* __restrict__ BR, const cplx<T>* __restrict__ BI,
         cplx<T>* __restrict__ psi, cplx<T>* __restrict__ AR, cplx<T>* __restrict__ AI,
-        double2* __restrict__ bscr, int do_psi, int do_A) {
-  using Op = Tri<sizeof(T) == 8>;
-  const long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+        int do_psi, int do_A) {
+  constexpr bool EXACT = sizeof(T) == 8;
+  constexpr int TC = kSolveTC, NTH = kSolveThreads, S = kSeg;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n3 = g.n3;
+  double* du_s = reinterpret_cast<double*>(smem_raw);
+  double* ck = du_s + n3 + threadIdx.x;           // checkpoint of segment j at ck[j*NTH]
+  for (int i = threadIdx.x; i < n3; i += NTH) du_s[i] = du[i];
+  __syncthreads();
+  const int chain = threadIdx.x / TC, c = threadIdx.x % TC;
+  const int rhs_id = chain >> 1, part = chain & 1;
+  if (rhs_id == 0 ? !do_psi : !do_A) return;
+  const long long m = (long long)blockIdx.x * TC + c;
   if (m >= g.plane) return;
   const int kx = (int)(m % g.KXP);
   if (kx > g.K) return;
-  const int n3 = g.n3;
   const long long P = g.plane;
+  const T* rhs = reinterpret_cast<const T*>(rhs_id == 0 ? qs : (rhs_id == 1 ? BR : BI)) + part;
+  T* out = reinterpret_cast<T*>(rhs_id == 0 ? psi : (rhs_id == 1 ? AR : AI)) + part;
   const int idx = tab_idx[m];
   if (idx < 0) {
-    for (int i = 0; i < n3; ++i) {
-      if (do_psi) psi[i * P + m] = mk<T>(0, 0);
-      if (do_A) { AR[i * P + m] = mk<T>(0, 0); AI[i * P + m] = mk<T>(0, 0); }
-    }
+    for (int i = 0; i < n3; ++i) out[2 * (i * P + m)] = (T)0;
     return;
   }
-  if (do_psi) {
-    const double2* F = fac_psi + (long long)idx * n3;
-    const double s = __dmul_rn(dz, dz);
-    cplx<T> v = qs[m];
-    double br = __dmul_rn(s, (double)v.x), bi = __dmul_rn(s, (double)v.y);
-    bscr[m] = make_double2(br, bi);
-    for (int i = 1; i < n3; ++i) {
-      const double f = F[i - 1].x;
-      v = qs[i * P + m];
-      br = Op::fwd(__dmul_rn(s, (double)v.x), f, br);
-      bi = Op::fwd(__dmul_rn(s, (double)v.y), f, bi);
-      bscr[i * P + m] = make_double2(br, bi);
+  const double4* F = (rhs_id == 0 ? fac_psi : fac_A) + (long long)idx * n3;
+  const double s = rhs_id == 0 ? __dmul_rn(dz, dz) : __dmul_rn(__dmul_rn(dz, dz), Bu);
+  const int nseg = (n3 + S - 1) / S;
+  // one forward step: EXACT reproduces DGTSV (scaled RHS), fast runs unscaled
+  auto fwd = [&](double x, double f, T r) -> double {
+    return EXACT ? __dsub_rn(__dmul_rn(s, to64<T>(r)), __dmul_rn(f, x)) : fma(-f, x, to64<T>(r));
+  };
+  // forward sweep, checkpoints only
+  double x = 0.0;
+  for (int j = 0; j < nseg; ++j) {
+    ck[(size_t)j * NTH] = x;
+    T r[S];
+    double f[S];
+#pragma unroll
+    for (int k = 0; k < S; ++k) {
+      const int i = j * S + k;
+      r[k] = i < n3 ? rhs[2 * (i * P + m)] : (T)0;
+      f[k] = (i > 0 && i < n3) ? F[i - 1].x : 0.0;
     }
-    double xr = Op::last(br, F[n3 - 1].y), xi = Op::last(bi, F[n3 - 1].y);
-    psi[(n3 - 1) * P + m] = mk<T>((T)xr, (T)xi);
-    for (int i = n3 - 2; i >= 0; --i) {
-      const double2 b = bscr[i * P + m];
-      const double p = F[i].y, u = du[i];
-      xr = Op::back(b.x, u, xr, p);
-      xi = Op::back(b.y, u, xi, p);
-      psi[i * P + m] = mk<T>((T)xr, (T)xi);
-    }
+#pragma unroll
+    for (int k = 0; k < S; ++k)
+      if (j * S + k < n3) x = fwd(x, f[k], r[k]);
   }
-  if (do_A) {
-    const double2* F = fac_A + (long long)idx * n3;
-    const double s = __dmul_rn(__dmul_rn(dz, dz), Bu);
-    cplx<T> vr = BR[m], vi = BI[m];
-    double a0 = __dmul_rn(s, (double)vr.x), a1 = __dmul_rn(s, (double)vr.y);
-    double b0 = __dmul_rn(s, (double)vi.x), b1 = __dmul_rn(s, (double)vi.y);
-    bscr[m] = make_double2(a0, a1);
-    bscr[n3 * P + m] = make_double2(b0, b1);
-    for (int i = 1; i < n3; ++i) {
-      const double f = F[i - 1].x;
-      vr = BR[i * P + m]; vi = BI[i * P + m];
-      a0 = Op::fwd(__dmul_rn(s, (double)vr.x), f, a0); a1 = Op::fwd(__dmul_rn(s, (double)vr.y), f, a1);
-      b0 = Op::fwd(__dmul_rn(s, (double)vi.x), f, b0); b1 = Op::fwd(__dmul_rn(s, (double)vi.y), f, b1);
-      bscr[i * P + m] = make_double2(a0, a1);
-      bscr[(n3 + i) * P + m] = make_double2(b0, b1);
+  // back substitution, segment by segment from the top
+  double xn = 0.0;      // x_{i+1}
+  for (int j = nseg - 1; j >= 0; --j) {
+    T r[S];
+    double4 fl[S];
+    double fprev[S];
+#pragma unroll
+    for (int k = 0; k < S; ++k) {
+      const int i = j * S + k;
+      r[k] = i < n3 ? rhs[2 * (i * P + m)] : (T)0;
+      fprev[k] = (i > 0 && i < n3) ? F[i - 1].x : 0.0;
+      fl[k] = i < n3 ? F[i] : make_double4(0, 1, 0, 0);
     }
-    const double pn = F[n3 - 1].y;
-    a0 = Op::last(a0, pn); a1 = Op::last(a1, pn); b0 = Op::last(b0, pn); b1 = Op::last(b1, pn);
-    AR[(n3 - 1) * P + m] = mk<T>((T)a0, (T)a1);
-    AI[(n3 - 1) * P + m] = mk<T>((T)b0, (T)b1);
-    for (int i = n3 - 2; i >= 0; --i) {
-      const double2 x = bscr[i * P + m], y = bscr[(n3 + i) * P + m];
-      const double p = F[i].y, u = du[i];
-      a0 = Op::back(x.x, u, a0, p); a1 = Op::back(x.y, u, a1, p);
-      b0 = Op::back(y.x, u, b0, p); b1 = Op::back(y.y, u, b1, p);
-      AR[i * P + m] = mk<T>((T)a0, (T)a1);
-      AI[i * P + m] = mk<T>((T)b0, (T)b1);
+    double v[S];
+    double xc = ck[(size_t)j * NTH];
+#pragma unroll
+    for (int k = 0; k < S; ++k) {
+      if (j * S + k < n3) xc = fwd(xc, fprev[k], r[k]);
+      v[k] = xc;
+    }
+#pragma unroll
+    for (int k = S - 1; k >= 0; --k) {
+      const int i = j * S + k;
+      if (i < n3) {
+        if (i == n3 - 1) xn = EXACT ? __ddiv_rn(v[k], fl[k].y) : fl[k].y * v[k];
+        else if (EXACT) xn = __ddiv_rn(__dsub_rn(v[k], __dmul_rn(du_s[i], xn)), fl[k].y);
+        else xn = fma(-fl[k].z, xn, fl[k].y * v[k]);
+        out[2 * (i * P + m)] = from64<T>(xn);
+      }
     }
   }
 }
