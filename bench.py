@@ -33,9 +33,11 @@ for _p in (str(ROOT), str(PKG)):
         sys.path.insert(0, _p)
 
 FALLBACK_HBM_GBS = 6800.0
-# DRAM bytes per launch of the dominant kernel from an ncu capture
-# (dram__bytes_read.sum + dram__bytes_write.sum); None until captured.
-MEASURED_TRAFFIC = {}
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum, L2 not
+# flushed) of the dominant kernel, from the ncu capture summarised in
+# profiles/dram_per_launch_c2_512x512x32_mixed.md (launch shape identical to
+# the 512^2x256 workload: 11 levels per launch).
+MEASURED_TRAFFIC = {("col_update", "c2_512x512x256_mixed", "mixed"): 49.5e6}
 
 
 # ---------------------------------------------------------------------------
@@ -391,7 +393,8 @@ def main(argv=None):
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-baseline-levels", type=int, default=16)
+    ap.add_argument("--cpu-baseline-levels", type=int, default=64)
+    ap.add_argument("--cpu-baseline-steps", type=int, default=6)
     ap.add_argument("--reference-budget-s", type=float, default=120.0)
     args = ap.parse_args(argv)
     if args.warmup < 3:
@@ -404,11 +407,11 @@ def main(argv=None):
         if out is not None and world == 1 and not args.no_cpu_baseline:
             rc = workload(args)
             workers = os.cpu_count() or 1
-            v, secs = cpu_oracle_rate(rc, args.cpu_baseline_levels, 2, 0, workers)
+            v, secs = cpu_oracle_rate(rc, args.cpu_baseline_levels, args.cpu_baseline_steps, 0, workers)
             out["cpu_baseline"] = {
                 "value": v, "unit": "cell-steps/s", "cores": workers, "kind": "port",
                 "sample": f"oracle on a {rc.n}x{rc.n}x{args.cpu_baseline_levels} slab of {rc.name}, "
-                          f"2 leapfrog steps ({secs:.1f} s)"}
+                          f"{args.cpu_baseline_steps} leapfrog steps ({secs:.1f} s)"}
     if out is not None:
         print(json.dumps(out), flush=True)
 

@@ -163,12 +163,11 @@ __device__ __forceinline__ void load_tw_passes(cplx<T>* tw_s, const cplx<T>* __r
   }
 }
 
-template <typename T, int N, int R, int NS, bool FWD, int BATCH, int NT>
+template <typename T, int N, int R, int NS, bool FWD, int BATCH, int NT, int LD>
 __device__ __forceinline__ void ip_pass(cplx<T>* __restrict__ buf, const cplx<T>* __restrict__ tw) {
   constexpr int NB = N / R;
   constexpr int TASKS = BATCH * NB;
   constexpr int PER = (TASKS + NT - 1) / NT;
-  constexpr int LD = PadLD<N>::value;
   cplx<T> v[PER][R];
   const int tid = threadIdx.x;
 #pragma unroll
@@ -207,20 +206,22 @@ __device__ __forceinline__ void ip_pass(cplx<T>* __restrict__ buf, const cplx<T>
   __syncthreads();
 }
 
-template <typename T, int N, bool FWD, int BATCH, int NT, int NS>
+template <typename T, int N, bool FWD, int BATCH, int NT, int LD, int NS>
 __device__ __forceinline__ void ip_passes(cplx<T>* buf, const cplx<T>* tw) {
   if constexpr (NS < N) {
     constexpr int R = PassRadix<N / NS>::value;
-    ip_pass<T, N, R, NS, FWD, BATCH, NT>(buf, tw);
-    ip_passes<T, N, FWD, BATCH, NT, NS * R>(buf, tw);
+    ip_pass<T, N, R, NS, FWD, BATCH, NT, LD>(buf, tw);
+    ip_passes<T, N, FWD, BATCH, NT, LD, NS * R>(buf, tw);
   }
 }
 
 // All NT threads must call; the data must be visible to all of them (call
-// after a __syncthreads()).  Ends with a __syncthreads().
-template <typename T, int N, bool FWD, int BATCH, int NT>
+// after a __syncthreads()).  Transform b starts at buf + b*LD (LD >= the
+// padded length).  Ends with a __syncthreads().
+template <typename T, int N, bool FWD, int BATCH, int NT, int LD = PadLD<N>::value>
 __device__ __forceinline__ void fft_ip(cplx<T>* buf, const cplx<T>* tw) {
-  ip_passes<T, N, FWD, BATCH, NT, 1>(buf, tw);
+  static_assert(LD >= PadLD<N>::value, "transform stride shorter than the padded transform");
+  ip_passes<T, N, FWD, BATCH, NT, LD, 1>(buf, tw);
 }
 
 }  // namespace qg

@@ -44,7 +44,9 @@ template <typename T, int N> struct Tiles {
   static constexpr int CT = ct0 >= 8 ? 8 : (ct0 >= 1 ? ct0 : 1);
   static constexpr int rt0 = (8192 / CB) / N;
   static constexpr int RT = rt0 >= 2 ? 2 : 1;
-  static constexpr int LD = PadLD<N>::value;
+  // transform stride: odd number of elements, so the CT columns of a tile
+  // that consecutive threads fill and drain fall in different banks
+  static constexpr int LD = PadLD<N>::value + 1;
 };
 constexpr int kColThreads = 256;   // k_col_inv, k_col_update
 constexpr int kThreadsB = 256;     // row kernels, k_col_qw
@@ -53,6 +55,22 @@ constexpr int kThreadsB = 256;     // row kernels, k_col_qw
 template <typename T, int N>
 __device__ __forceinline__ void load_tw(cplx<T>* tw_s, const cplx<T>* __restrict__ tw_g, int nt) {
   load_tw_passes<T, N, 1>(tw_s, tw_g, nt);
+}
+
+// Asynchronous global->shared copies of one complex value (8 or 16 bytes);
+// src_bytes = 0 writes zeros (modes outside the retained set).
+template <typename T>
+__device__ __forceinline__ void cp_async_c(cplx<T>* dst, const cplx<T>* src, bool valid) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  if constexpr (sizeof(cplx<T>) == 8) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(valid ? 8 : 0));
+  } else {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(valid ? 16 : 0));
+  }
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
 
 // ===========================================================================
@@ -72,26 +90,33 @@ k_col_inv(Geom g, int zbase, const cplx<T>* __restrict__ psi, const cplx<T>* __r
   const int kx0 = blockIdx.x * CT;
   load_tw<T, N>(tw, twg, NT);
   const long long zoff = (long long)z * g.plane;
+  // raw columns: psi -> slot 2, q -> 3, BR -> 4, BI -> 5 (asynchronous copies)
 #pragma unroll
   for (int src = 0; src < 4; ++src) {
     const cplx<T>* F = src == 0 ? psi : (src == 1 ? q : (src == 2 ? BR : BI));
+    cplx<T>* slot = buf + (src + 2) * CT * LD;
 #pragma unroll 4
     for (int e = tid; e < CT * N; e += NT) {
       const int c = e % CT, j = e / CT;
       const int kx = kx0 + c;
       const int r = g.row_of_fft_index(j);
       const bool in = kx <= g.K && r >= 0;
-      const cplx<T> sv = in ? F[zoff + (long long)r * g.KXP + kx] : mk<T>(0, 0);
-      const int o = c * LD + pad_idx(j);
-      if (src == 0) {
-        const T ky = in ? (T)g.ky_of_row(r) : (T)0;
-        buf[0 * CT * LD + o] = cscale(cmul_mi(sv), ky);                          // u = -i ky psi (derivatives.f90:1309)
-        buf[1 * CT * LD + o] = cscale(cmul_i(sv), (T)kx);                        // v = i kx psi  (derivatives.f90:1310)
-        buf[2 * CT * LD + o] = cscale(sv, -((T)(kx * kx) + ky * ky));            // zeta = -kh^2 psi (derivatives.f90:842)
-      } else {
-        buf[(src + 2) * CT * LD + o] = sv;
-      }
+      cp_async_c<T>(slot + c * LD + pad_idx(j), in ? F + zoff + (long long)r * g.KXP + kx : F, in);
     }
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  // u = -i ky psi (derivatives.f90:1309), v = i kx psi (1310), zeta = -kh^2 psi (842)
+  for (int e = tid; e < CT * N; e += NT) {
+    const int c = e % CT, j = e / CT;
+    const int r = g.row_of_fft_index(j);
+    const T ky = r >= 0 ? (T)g.ky_of_row(r) : (T)0;
+    const T kx = (T)(kx0 + c);
+    const int o = c * LD + pad_idx(j);
+    const cplx<T> sv = buf[2 * CT * LD + o];
+    buf[0 * CT * LD + o] = cscale(cmul_mi(sv), ky);
+    buf[1 * CT * LD + o] = cscale(cmul_i(sv), kx);
+    buf[2 * CT * LD + o] = cscale(sv, -(kx * kx + ky * ky));
   }
   __syncthreads();
   if (kx0 == 0) {    // realit (fft.f90:88-107) on the kx=0 column of each field
@@ -103,8 +128,8 @@ k_col_inv(Geom g, int zbase, const cplx<T>* __restrict__ psi, const cplx<T>* __r
     __syncthreads();
   }
   // two groups of three fields keep a thread's butterflies in registers
-  fft_ip<T, N, false, 3 * CT, NT>(buf, tw);
-  fft_ip<T, N, false, 3 * CT, NT>(buf + 3 * CT * LD, tw);
+  fft_ip<T, N, false, 3 * CT, NT, LD>(buf, tw);
+  fft_ip<T, N, false, 3 * CT, NT, LD>(buf + 3 * CT * LD, tw);
 #pragma unroll 4
   for (int e = tid; e < 6 * CT * N; e += NT) {
     const int c = e % CT, y = (e / CT) % N, f = e / (CT * N);
@@ -164,7 +189,7 @@ k_row_main(Geom g, StepParams sp, cplx<T>* __restrict__ S, const cplx<T>* __rest
     bA[(rr * 3 + p) * LD + pad_idx(k)] = pack_spec<T>(X, Y, k, N, K);
   }
   __syncthreads();
-  fft_ip<T, N, false, 3 * RT, NT>(bA, tw);
+  fft_ip<T, N, false, 3 * RT, NT, LD>(bA, tw);
   // products: (u q, v q), (u br, v br), (u bi, v bi), (zeta br, zeta bi)
 #pragma unroll 4
   for (int e = tid; e < RT * N; e += NT) {
@@ -179,7 +204,7 @@ k_row_main(Geom g, StepParams sp, cplx<T>* __restrict__ S, const cplx<T>* __rest
     bC[(rr * 4 + 3) * LD + px] = mk<T>(zq.x * bb.x, zq.x * bb.y);
   }
   __syncthreads();
-  fft_ip<T, N, true, 4 * RT, NT>(bC, tw);
+  fft_ip<T, N, true, 4 * RT, NT, LD>(bC, tw);
   const T adv = sp.adv ? (T)1 : (T)0;
   const T half = sp.refr ? (T)0.5 : (T)0;
   for (int e = tid; e < RT * (K + 1); e += NT) {
@@ -228,11 +253,12 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
   for (int e = tid; e < 6 * CT * N; e += NT) {
     const int c = e % CT, y = (e / CT) % N, h = e / (CT * N);
     const int kx = kx0 + c;
-    buf[(h * CT + c) * LD + pad_idx(y)] = kx <= g.K ? S[scr_off(zb, h, y, N, g.KXP) + kx] : mk<T>(0, 0);
+    cp_async_c<T>(buf + (h * CT + c) * LD + pad_idx(y), S + scr_off(zb, h, y, N, g.KXP) + kx, kx <= g.K);
   }
+  cp_async_wait_all();
   __syncthreads();
-  fft_ip<T, N, true, 3 * CT, NT>(buf, tw);
-  fft_ip<T, N, true, 3 * CT, NT>(buf + 3 * CT * LD, tw);
+  fft_ip<T, N, true, 3 * CT, NT, LD>(buf, tw);
+  fft_ip<T, N, true, 3 * CT, NT, LD>(buf + 3 * CT * LD, tw);
   // tendencies and time update (main_waqg.f90:237-264, 362-415): one mode
   // (column c, row r) per iteration, all of its loads issued together
   const T inv_n2 = (T)1 / ((T)N * (T)N);
@@ -293,16 +319,22 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
   __syncthreads();   // this CTA's writes of BR, BI are visible to it after the barrier
   // y-inverse FFTs of BR, i ky BR, BI, i ky BI at n+1 (compute_qw, derivatives.f90:929-957)
 #pragma unroll 4
-  for (int e = tid; e < 4 * CT * N; e += NT) {
+  for (int e = tid; e < 2 * CT * N; e += NT) {
     const int c = e % CT, j = (e / CT) % N, f = e / (CT * N);
     const int kx = kx0 + c;
     const int r = g.row_of_fft_index(j);
-    cplx<T> v = mk<T>(0, 0);
-    if (kx <= g.K && r >= 0) {
-      const cplx<T> s = (f < 2 ? st.BR : st.BI)[zoff + (long long)r * g.KXP + kx];
-      v = (f & 1) ? cscale(cmul_i(s), (T)g.ky_of_row(r)) : s;
-    }
-    buf[(f * CT + c) * LD + pad_idx(j)] = v;
+    const bool in = kx <= g.K && r >= 0;
+    const cplx<T>* F = f == 0 ? st.BR : st.BI;
+    cp_async_c<T>(buf + (2 * f * CT + c) * LD + pad_idx(j), in ? F + zoff + (long long)r * g.KXP + kx : F, in);
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  for (int e = tid; e < 2 * CT * N; e += NT) {
+    const int c = e % CT, j = (e / CT) % N, f = e / (CT * N);
+    const int r = g.row_of_fft_index(j);
+    const T ky = r >= 0 ? (T)g.ky_of_row(r) : (T)0;
+    const int o = c * LD + pad_idx(j);
+    buf[(2 * f + 1) * CT * LD + o] = cscale(cmul_i(buf[2 * f * CT * LD + o]), ky);
   }
   __syncthreads();
   if (kx0 == 0) {
@@ -313,8 +345,8 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
     }
     __syncthreads();
   }
-  fft_ip<T, N, false, 2 * CT, NT>(buf, tw);
-  fft_ip<T, N, false, 2 * CT, NT>(buf + 2 * CT * LD, tw);
+  fft_ip<T, N, false, 2 * CT, NT, LD>(buf, tw);
+  fft_ip<T, N, false, 2 * CT, NT, LD>(buf + 2 * CT * LD, tw);
 #pragma unroll 4
   for (int e = tid; e < 4 * CT * N; e += NT) {
     const int c = e % CT, y = (e / CT) % N, f = e / (CT * N);
@@ -362,7 +394,7 @@ k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
     bA[(rr * 3 + p) * LD + pad_idx(k)] = v;
   }
   __syncthreads();
-  fft_ip<T, N, false, 3 * RT, NT>(bA, tw);
+  fft_ip<T, N, false, 3 * RT, NT, LD>(bA, tw);
 #pragma unroll 4
   for (int e = tid; e < RT * N; e += NT) {
     const int x = e % N, rr = e / N;
@@ -375,7 +407,7 @@ k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
     bC[rr * LD + px] = mk<T>(p1, p2);
   }
   __syncthreads();
-  fft_ip<T, N, true, RT, NT>(bC, tw);
+  fft_ip<T, N, true, RT, NT, LD>(bC, tw);
   for (int e = tid; e < RT * (K + 1); e += NT) {
     const int k = e % (K + 1), rr = e / (K + 1);
     const int y = y0 + rr;
@@ -407,10 +439,11 @@ k_col_qw(Geom g, StepParams sp, int zbase, const cplx<T>* __restrict__ q, cplx<T
   for (int e = tid; e < 2 * CT * N; e += NT) {
     const int c = e % CT, y = (e / CT) % N, h = e / (CT * N);
     const int kx = kx0 + c;
-    buf[(h * CT + c) * LD + pad_idx(y)] = kx <= g.K ? S[scr_off(zb, h, y, N, g.KXP) + kx] : mk<T>(0, 0);
+    cp_async_c<T>(buf + (h * CT + c) * LD + pad_idx(y), S + scr_off(zb, h, y, N, g.KXP) + kx, kx <= g.K);
   }
+  cp_async_wait_all();
   __syncthreads();
-  fft_ip<T, N, true, 2 * CT, NT>(buf, tw);
+  fft_ip<T, N, true, 2 * CT, NT, LD>(buf, tw);
   const T inv_n2 = (T)1 / ((T)N * (T)N);
   const T s = (T)sp.Ro * (T)sp.W2F;
   const long long zoff = (long long)z * g.plane;
