@@ -33,11 +33,12 @@ for _p in (str(ROOT), str(PKG)):
         sys.path.insert(0, _p)
 
 FALLBACK_HBM_GBS = 6800.0
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum, L2 not
-# flushed) of the dominant kernel, from the ncu capture summarised in
-# profiles/dram_per_launch_c2_512x512x32_mixed.md (launch shape identical to
-# the 512^2x256 workload: 11 levels per launch).
-MEASURED_TRAFFIC = {("col_update", "c2_512x512x256_mixed", "mixed"): 49.5e6}
+# DRAM bytes per level of a launch (dram__bytes_read.sum + dram__bytes_write.sum,
+# L2 not flushed) of the dominant kernel, from the ncu capture summarised in
+# profiles/dram_per_launch_c2_512x512x32_mixed.md (512^2 levels, 11 levels per
+# launch: 49.5 MB).  The traffic of a launch grows with the levels it covers,
+# so the roofline entry scales it by the levels per launch of the run.
+MEASURED_TRAFFIC_PER_LEVEL = {("col_update", 512, "mixed"): 49.5e6 / 11}
 
 
 # ---------------------------------------------------------------------------
@@ -185,7 +186,7 @@ def run_ours(args, world, rank, local):
     precision = args.precision or rc.precision
     ic = make_initial_condition(rc)
     params = model_parameters(rc, ic.delt)
-    sim = qgybj.Simulation(params, precision, device=local)
+    sim = qgybj.Simulation(params, precision, device=local, levels_per_batch=rc.levels_per_batch)
     sim.set_state("psi", ic.psi)
     sim.set_state("BR", ic.BR)
     sim.set_state("BI", ic.BI)
@@ -256,7 +257,7 @@ def run_ours(args, world, rank, local):
     # FP64 GPU step on the same workload (the metric compares the two)
     fp64 = None
     if not args.no_fp64 and precision == "mixed":
-        sim64 = qgybj.Simulation(params, "fp64", device=local)
+        sim64 = qgybj.Simulation(params, "fp64", device=local, levels_per_batch=CONFIGS["c1"].levels_per_batch)
         sim64.set_state("psi", ic.psi); sim64.set_state("BR", ic.BR); sim64.set_state("BI", ic.BI)
         sim64.init_state(True, True)
         sim64.steps_async(2, True)
@@ -292,7 +293,8 @@ def run_ours(args, world, rank, local):
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                          "algorithmic_bytes_per_launch": ab[dom], "ms_per_launch": dom_ms,
-                         "traffic": MEASURED_TRAFFIC.get((dom, rc.name, precision))},
+                         "traffic": (MEASURED_TRAFFIC_PER_LEVEL[(dom, n, precision)] * sim_batch(sim)
+                                     if (dom, n, precision) in MEASURED_TRAFFIC_PER_LEVEL else None)},
             "step_roofline": {"bytes_per_step": ab["step"], "achieved": ab["step"] / (step_ms / 1e3) / 1e9,
                               "frac": ab["step"] / (step_ms / 1e3) / 1e9 / peak, "unit": "GB/s",
                               "bytes_per_step_dense_layout": ab["step_dense"],
@@ -316,6 +318,89 @@ def workload(args):
     if args.n or args.n3:
         rc = scaled(rc, args.n or rc.n, args.n3 or rc.n3)
     return rc
+
+
+def run_ensemble(args, world, rank, local):
+    """The 64-member uneven ensemble (24 at 64^2x32, 24 at 128^2x64, 16 at
+    256^2x128, mixed precision) advanced by one graph launch per step, against
+    the same members run one after another, each with its own graph."""
+    import torch
+
+    import qgybj
+    from qgybj.config import ensemble_members, make_initial_condition, model_parameters
+
+    dist = dist_setup(world, "nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    members = ensemble_members()[: args.members or None]
+    ics = [make_initial_condition(rc) for rc in members]
+    params = [model_parameters(rc, ic.delt) for rc, ic in zip(members, ics)]
+    tuned = {}
+    for rc, p in zip(members, params):
+        if (rc.n, rc.n3) not in tuned:
+            tuned[(rc.n, rc.n3)] = qgybj.autotune(p, "mixed", local, nsteps=3)
+    lpb = [tuned[(rc.n, rc.n3)]["levels_per_batch"] for rc in members]
+    cells = sum(rc.n * rc.n * rc.n3 for rc in members)
+
+    def init(sim, ic):
+        sim.set_state("psi", ic.psi); sim.set_state("BR", ic.BR); sim.set_state("BI", ic.BI)
+        sim.init_state(True, True)
+
+    ens = qgybj.Ensemble(params, "mixed", local, levels_per_batch=lpb)
+    for sim, ic in zip(ens.members, ics):
+        init(sim, ic)
+    ens.step(args.warmup, True)
+    ens.synchronize()
+    stream = torch.cuda.ExternalStream(ens.stream(), device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(local)
+    barrier(dist)
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.25)
+    e0.record(stream)
+    ens.step(args.steps, False)
+    e1.record(stream)
+    ens.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier(dist)
+    ms = reduce_max(dist, e0.elapsed_time(e1), device=dev)
+    launches = 0
+    for sim in ens.members:
+        launches += sum(c for _, c in sim.profile_step(False).values())
+    ens.close()
+    # the same members one after another
+    seq_ms = 0.0
+    for p, ic, l in zip(params, ics, lpb):
+        sim = qgybj.Simulation(p, "mixed", local, levels_per_batch=l)
+        init(sim, ic)
+        sim.steps_async(args.warmup, True)
+        sim.synchronize()
+        st = torch.cuda.ExternalStream(sim.stream(), device=dev)
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(st)
+        sim.steps_async(args.steps, False)
+        a1.record(st)
+        sim.synchronize()
+        seq_ms += a0.elapsed_time(a1)
+        sim.close()
+    if rank != 0:
+        return None
+    value = whole_job_value(world, cells, args.steps, ms / 1e3)
+    return {
+        "metric": "cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": f"c3_ensemble_{len(members)}_members", "members": len(members),
+                   "sizes": {f"{n}x{n}x{n3}": sum(1 for rc in members if (rc.n, rc.n3) == (n, n3))
+                             for (n, n3) in tuned},
+                   "levels_per_batch": {f"{n}x{n}x{n3}": t["levels_per_batch"] for (n, n3), t in tuned.items()},
+                   "precision": "mixed", "parallelism": f"replicas{world}"},
+        "sequential_value": cells * args.steps / (seq_ms / 1e3),
+        "ensemble_over_sequential": seq_ms / (ms / world),
+        "gpu_launches": launches * args.steps, "clocks": clk, "e2e": None,
+    }
 
 
 def sim_batch(sim) -> int:
@@ -396,12 +481,15 @@ def main(argv=None):
     ap.add_argument("--cpu-baseline-levels", type=int, default=64)
     ap.add_argument("--cpu-baseline-steps", type=int, default=6)
     ap.add_argument("--reference-budget-s", type=float, default=120.0)
+    ap.add_argument("--members", type=int, default=0, help="c3: first M ensemble members only")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3
     world, rank, local = dist_env()
     if args.impl == "reference":
         out = run_reference(args, world, rank, local)
+    elif args.config == "c3":
+        out = run_ensemble(args, world, rank, local)
     else:
         out = run_ours(args, world, rank, local)
         if out is not None and world == 1 and not args.no_cpu_baseline:

@@ -62,7 +62,7 @@ enum qg_field {
  * the step reads (parameters_test1.f90) plus the base state of
  * init_base_state (init.f90:177-264).  Arrays are copied by qg_create. */
 typedef struct qg_config {
-  int n1, n2, n3;          /* resolution; n1 == n2, a power of two in [16,1024]; 2 <= n3 <= 4096 */
+  int n1, n2, n3;          /* resolution; n1 == n2, a power of two in [16,1024]; 2 <= n3 <= 1024 */
   int precision;           /* enum qg_precision                                        */
   int device;              /* CUDA device ordinal                                      */
   /* physics switches (parameters_test1.f90:22-29) */
@@ -178,6 +178,38 @@ int qg_compute_qw(qg_handle* h, const double* BRk, const double* BIk, double* qw
 int qg_psi_solver(qg_handle* h, const double* qstar, double* psik);
 /* elliptic.f90:346-460: all n3 levels; ck may be NULL. */
 int qg_A_solver_ybj_plus(qg_handle* h, const double* bk, double* ak, double* ck);
+
+/* ---- ensembles and tuning (no counterpart in the reference) -------------- */
+
+/* An ensemble of independent runs, possibly of different sizes and
+ * parameters, advanced together: one CUDA graph per step kind forks every
+ * member's step onto the member's own stream and joins them, so one graph
+ * launch advances all members, which then run concurrently on the GPU.
+ * Members are ordinary handles (set/get/init/diagnostics through
+ * qg_ensemble_member); all members must use the same device. */
+typedef struct qg_ensemble qg_ensemble;
+int qg_ensemble_create(const qg_config* cfgs, int nmembers, qg_ensemble** out);
+int qg_ensemble_member(qg_ensemble* e, int member, qg_handle** h);
+/* nsteps steps of every member (the first forward Euler when euler_first=1);
+ * asynchronous, like qg_steps_async. */
+int qg_ensemble_step(qg_ensemble* e, int nsteps, int euler_first);
+int qg_ensemble_synchronize(qg_ensemble* e);
+int qg_ensemble_get_stream(qg_ensemble* e, void** stream);
+int qg_ensemble_destroy(qg_ensemble* e);
+const char* qg_ensemble_last_error(const qg_ensemble* e);
+
+/* Autotuner: times candidate phase-A batch depths (levels per batch: the L2
+ * footprint of the (kx,y) scratch planes and the wave count of the column
+ * kernels) on a handle built from cfg and reports the fastest.  The state
+ * content does not change the cost, so the candidates run on a zero state. */
+typedef struct qg_tuning {
+  int levels_per_batch;      /* fastest candidate                          */
+  double ms_per_step;        /* its time per step                          */
+  int ncandidates;           /* candidates timed (<= 16)                   */
+  int candidates[16];        /* their batch depths ...                     */
+  double candidate_ms[16];   /* ... and times per step                     */
+} qg_tuning;
+int qg_autotune(const qg_config* cfg, int nsteps, qg_tuning* out);
 
 /* Allocation-free variant of qg_fft_c2r.  No counterpart in the reference.
  * For callers that cannot allocate device memory: a host whose device memory

@@ -8,6 +8,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <vector>
 #include "engine.h"
 
 struct qg_handle {
@@ -225,7 +226,7 @@ int qg_create(const qg_config* cfg, qg_handle** out) {
   if (c.n1 != c.n2) return fail(nullptr, QG_ERR_UNSUPPORTED, "n1 must equal n2");
   if (!qg::supported_n(c.n1)) return fail(nullptr, QG_ERR_UNSUPPORTED, "n1 must be a power of two in [16,1024]");
   if (c.n3 < 2) return fail(nullptr, QG_ERR_ARG, "n3 must be >= 2");
-  if (c.n3 > 4096) return fail(nullptr, QG_ERR_UNSUPPORTED, "n3 must be <= 4096 (one column's FP64 solve in shared memory)");
+  if (c.n3 > 1024) return fail(nullptr, QG_ERR_UNSUPPORTED, "n3 must be <= 1024 (solve checkpoints in shared memory)");
   if (c.precision != QG_PREC_FP64 && c.precision != QG_PREC_MIXED) return fail(nullptr, QG_ERR_ARG, "bad precision");
   if (c.ybj_plus != 1) return fail(nullptr, QG_ERR_UNSUPPORTED, "only the YBJ+ step (ybj_plus=1) is implemented");
   if (!c.a_ell_ut) return fail(nullptr, QG_ERR_ARG, "a_ell_ut is required");
@@ -357,6 +358,183 @@ int qg_A_solver_ybj_plus(qg_handle* h, const double* bk, double* ak, double* ck)
   QG_ENTRY(h);
   if (!bk || !ak) return fail(h, QG_ERR_ARG, "null pointer");
   return fwd(h, h->eng->A_solver(bk, ak, ck));
+}
+
+// ---- ensembles ----------------------------------------------------------------
+struct qg_ensemble {
+  std::vector<qg_handle*> members;
+  cudaStream_t master = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> join;
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+  std::string err;
+};
+
+static int ens_fail(qg_ensemble* e, int code, const std::string& msg) {
+  if (e) e->err = msg;
+  return code;
+}
+
+#define ENS_CK(call)                                                                       \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess) return ens_fail(e, QG_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+int qg_ensemble_destroy(qg_ensemble* e) {
+  if (!e) return QG_ERR_ARG;
+  if (e->master) cudaStreamSynchronize(e->master);
+  for (auto& g : e->gexec) if (g) cudaGraphExecDestroy(g);
+  for (auto* h : e->members) qg_destroy(h);
+  for (auto ev : e->join) cudaEventDestroy(ev);
+  if (e->fork) cudaEventDestroy(e->fork);
+  if (e->master) cudaStreamDestroy(e->master);
+  delete e;
+  return QG_OK;
+}
+
+int qg_ensemble_create(const qg_config* cfgs, int nmembers, qg_ensemble** out) {
+  if (!cfgs || !out || nmembers <= 0) return fail(nullptr, QG_ERR_ARG, "qg_ensemble_create: bad arguments");
+  *out = nullptr;
+  for (int m = 1; m < nmembers; ++m)
+    if (cfgs[m].device != cfgs[0].device) return fail(nullptr, QG_ERR_ARG, "ensemble members must share one device");
+  qg_ensemble* e = new qg_ensemble();
+  for (int m = 0; m < nmembers; ++m) {
+    qg_config c = cfgs[m];
+    c.use_graphs = 0;          // members are replayed through the ensemble graph
+    qg_handle* h = nullptr;
+    int rc = qg_create(&c, &h);
+    if (rc) {
+      const std::string msg = "member " + std::to_string(m) + ": " + g_create_err;
+      qg_ensemble_destroy(e);
+      return fail(nullptr, rc, msg);
+    }
+    e->members.push_back(h);
+  }
+  if (cudaSetDevice(cfgs[0].device) != cudaSuccess || cudaStreamCreateWithFlags(&e->master, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming) != cudaSuccess) {
+    qg_ensemble_destroy(e);
+    return fail(nullptr, QG_ERR_CUDA, "qg_ensemble_create: stream/event creation failed");
+  }
+  e->join.resize(nmembers);
+  for (auto& ev : e->join) cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+  *out = e;
+  return QG_OK;
+}
+
+int qg_ensemble_member(qg_ensemble* e, int member, qg_handle** h) {
+  if (!e || !h || member < 0 || member >= (int)e->members.size()) return ens_fail(e, QG_ERR_ARG, "bad member index");
+  *h = e->members[member];
+  return QG_OK;
+}
+
+static int ens_capture(qg_ensemble* e, int euler) {
+  cudaGraph_t graph = nullptr;
+  ENS_CK(cudaStreamBeginCapture(e->master, cudaStreamCaptureModeThreadLocal));
+  int rc = QG_OK;
+  for (size_t m = 0; m < e->members.size() && !rc; ++m) {
+    cudaStream_t ms = (cudaStream_t)e->members[m]->eng->stream();
+    if (cudaEventRecord(e->fork, e->master) != cudaSuccess || cudaStreamWaitEvent(ms, e->fork, 0) != cudaSuccess) {
+      rc = QG_ERR_CUDA;
+      e->err = "ensemble fork failed";
+      break;
+    }
+    rc = e->members[m]->eng->enqueue(euler);
+    if (rc) { e->err = "member " + std::to_string(m) + ": " + e->members[m]->eng->err; break; }
+    if (cudaEventRecord(e->join[m], ms) != cudaSuccess || cudaStreamWaitEvent(e->master, e->join[m], 0) != cudaSuccess) {
+      rc = QG_ERR_CUDA;
+      e->err = "ensemble join failed";
+    }
+  }
+  cudaError_t ce = cudaStreamEndCapture(e->master, &graph);
+  if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
+  if (ce != cudaSuccess) return ens_fail(e, QG_ERR_CUDA, std::string("ensemble capture: ") + cudaGetErrorString(ce));
+  ce = cudaGraphInstantiate(&e->gexec[euler], graph, 0);
+  cudaGraphDestroy(graph);
+  if (ce != cudaSuccess) return ens_fail(e, QG_ERR_CUDA, std::string("ensemble instantiate: ") + cudaGetErrorString(ce));
+  return QG_OK;
+}
+
+int qg_ensemble_step(qg_ensemble* e, int nsteps, int euler_first) {
+  if (!e || nsteps < 0) return ens_fail(e, QG_ERR_ARG, "bad arguments");
+  e->err.clear();
+  for (int i = 0; i < nsteps; ++i) {
+    const int k = (euler_first && i == 0) ? 1 : 0;
+    if (!e->gexec[k]) {
+      int rc = ens_capture(e, k);
+      if (rc) return rc;
+    }
+    ENS_CK(cudaGraphLaunch(e->gexec[k], e->master));
+  }
+  return QG_OK;
+}
+
+int qg_ensemble_synchronize(qg_ensemble* e) {
+  if (!e) return QG_ERR_ARG;
+  ENS_CK(cudaStreamSynchronize(e->master));
+  return QG_OK;
+}
+
+int qg_ensemble_get_stream(qg_ensemble* e, void** stream) {
+  if (!e || !stream) return ens_fail(e, QG_ERR_ARG, "null argument");
+  *stream = (void*)e->master;
+  return QG_OK;
+}
+
+const char* qg_ensemble_last_error(const qg_ensemble* e) { return e ? e->err.c_str() : ""; }
+
+// ---- autotuner -------------------------------------------------------------
+int qg_autotune(const qg_config* cfg, int nsteps, qg_tuning* out) {
+  if (!cfg || !out || nsteps <= 0) return fail(nullptr, QG_ERR_ARG, "qg_autotune: bad arguments");
+  std::memset(out, 0, sizeof *out);
+  qg_config c = *cfg;
+  c.use_graphs = 1;
+  qg_handle* h = nullptr;
+  int rc = qg_create(&c, &h);
+  if (rc) return rc;
+  // candidate depths: powers of two and the depths whose column-kernel grids
+  // fill an integral number of waves best, capped by a 96 MB scratch budget
+  std::vector<int> cand;
+  const int n = c.n1, n3 = c.n3;
+  const size_t cbytes = c.precision == QG_PREC_FP64 ? 16 : 8;
+  const int K = (int)((float)(int)((float)n / 3.0f + 0.5f) - 0.5f);
+  const size_t per_level = (size_t)6 * n * (((K + 1 + 7) / 8) * 8) * cbytes;
+  const int zmax = (int)std::max<size_t>(1, std::min<size_t>((size_t)n3, (size_t)(96u << 20) / per_level));
+  for (int z : {1, 2, 3, 4, 6, 8, 11, 13, 16, 20, 24, 32, 48, 64})
+    if (z <= zmax && (int)cand.size() < 16) cand.push_back(z);
+  cudaStream_t st = (cudaStream_t)h->eng->stream();
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  double best = 1e300;
+  int bestz = cand.empty() ? 1 : cand[0];
+  for (int z : cand) {
+    rc = h->eng->set_batch_levels(z);
+    if (!rc) rc = h->eng->steps_async(2, 1);          // warm-up, graph capture
+    if (!rc) rc = h->eng->synchronize();
+    if (rc) break;
+    cudaEventRecord(a, st);
+    rc = h->eng->steps_async(nsteps, 0);
+    cudaEventRecord(b, st);
+    if (!rc) rc = h->eng->synchronize();
+    if (rc) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    const double per = ms / nsteps;
+    const int zeff = h->eng->batch_levels();
+    out->candidates[out->ncandidates] = zeff;
+    out->candidate_ms[out->ncandidates] = per;
+    out->ncandidates++;
+    if (per < best) { best = per; bestz = zeff; }
+  }
+  std::string err = rc ? h->eng->err : "";
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  qg_destroy(h);
+  if (rc) return fail(nullptr, rc, "qg_autotune: " + err);
+  out->levels_per_batch = bestz;
+  out->ms_per_step = best;
+  return QG_OK;
 }
 
 }  // extern "C"

@@ -34,6 +34,12 @@ struct EngineBase {
   virtual void* stream() = 0;
   virtual int diagnostics(qg_energy* out) = 0;
   virtual int profile_step(int euler, double* ms, int* launches, int nclasses) = 0;
+  // enqueue one step on the engine's stream without synchronising or graph
+  // replay (used when an ensemble captures its members into one graph)
+  virtual int enqueue(int euler) = 0;
+  // levels per phase-A batch: current value and re-selection (drops graphs)
+  virtual int batch_levels() const = 0;
+  virtual int set_batch_levels(int zb) = 0;
   virtual int fft_r2c(const double* rvar, double* kvar, int nz) = 0;
   virtual int fft_c2r(const double* kvar, double* rvar, int nz) = 0;
   virtual int convol_waqg(const double* uk, const double* vk, const double* qk, const double* BRk, const double* BIk,

@@ -114,6 +114,26 @@ class Engine final : public EngineBase {
 
   void* stream() override { return (void*)st; }
 
+  int enqueue(int euler) override { return enqueue_step(euler ? 1 : 0); }
+
+  int batch_levels() const override { return Zb; }
+
+  int set_batch_levels(int zb) override {
+    QG_CK(cudaStreamSynchronize(st));
+    for (auto& x : gexec) if (x) { cudaGraphExecDestroy(x); x = nullptr; }
+    const size_t per_level = (size_t)kNScr * g.n * g.KXP * sizeof(C);
+    zb = std::max(1, std::min(zb, g.n3));
+    const int nb = (g.n3 + zb - 1) / zb;
+    const int nz = (g.n3 + nb - 1) / nb;
+    if (nz > Zb) {
+      cudaFree(S);
+      S = nullptr;
+      QG_CK(cudaMalloc(&S, (size_t)nz * per_level));
+    }
+    Zb = nz;
+    return QG_OK;
+  }
+
   int synchronize() override { QG_CK(cudaStreamSynchronize(st)); return QG_OK; }
 
   // ---- state --------------------------------------------------------------
@@ -424,7 +444,8 @@ class Engine final : public EngineBase {
       QG_CK(cudaFuncSetAttribute(k_col_update<T, NN>, (cudaFuncAttribute)mx, (int)sm_col6<NN>()));
       QG_CK(cudaFuncSetAttribute(k_row_qw<T, NN>, (cudaFuncAttribute)mx, (int)sm_row4<NN>()));
       QG_CK(cudaFuncSetAttribute(k_col_qw<T, NN>, (cudaFuncAttribute)mx, (int)sm_col2<NN>()));
-      QG_CK(cudaFuncSetAttribute(k_solve<T>, (cudaFuncAttribute)mx, (int)solve_smem(g.n3)));
+      // per-function attribute shared by every handle: set it for the deepest supported column
+      QG_CK(cudaFuncSetAttribute(k_solve<T>, (cudaFuncAttribute)mx, (int)solve_smem(kMaxN3)));
       QG_CK(cudaFuncSetAttribute(k_dcol_inv<T, NN>, (cudaFuncAttribute)mx, (int)sm_colinv()));
       QG_CK(cudaFuncSetAttribute(k_dcol_fwd<T, NN>, (cudaFuncAttribute)mx, (int)sm_colinv()));
       QG_CK(cudaFuncSetAttribute(k_drow_c2r<T, NN>, (cudaFuncAttribute)mx, (int)sm_drow()));

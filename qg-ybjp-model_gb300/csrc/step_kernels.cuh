@@ -539,6 +539,7 @@ template <> __device__ __forceinline__ float from64<float>(double v) { return f6
 // from its checkpoint in registers and then substitutes through it.  One
 // extra FMA per level buys a kernel with no scratch traffic and many warps.
 constexpr int kSeg = 8;
+constexpr int kMaxN3 = 1024;      // checkpoints + upper diagonal fit in shared memory up to here
 constexpr int kSolveTC = 32;
 constexpr int kSolveThreads = 6 * kSolveTC;
 

@@ -6,4 +6,4 @@ seeded initial-condition generator, and the Simulation host class.
 """
 from ._lib import LIB_PATH, QgError, lib  # noqa: F401
 from .config import CONFIGS, RunConfig, ensemble_members, make_initial_condition, model_parameters  # noqa: F401
-from .model import Simulation, simulation_for  # noqa: F401
+from .model import Ensemble, Simulation, autotune, make_config, simulation_for  # noqa: F401

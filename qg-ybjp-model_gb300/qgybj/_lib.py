@@ -24,6 +24,8 @@ EXPORTS = (
     "qg_init_state", "qg_step", "qg_steps_async", "qg_synchronize", "qg_get_stream", "qg_diagnostics_fp64",
     "qg_fft_r2c", "qg_fft_c2r", "qg_convol_waqg", "qg_refraction_waqg", "qg_compute_qw", "qg_psi_solver",
     "qg_A_solver_ybj_plus", "qg_profile_step", "qg_fft_c2r_noalloc",
+    "qg_ensemble_create", "qg_ensemble_member", "qg_ensemble_step", "qg_ensemble_synchronize",
+    "qg_ensemble_get_stream", "qg_ensemble_destroy", "qg_ensemble_last_error", "qg_autotune",
 )
 KERNEL_CLASSES = ("dissipation", "col_inv", "row_main", "col_update", "row_qw", "col_qw", "solve")
 
@@ -42,6 +44,11 @@ class QgConfig(C.Structure):
         ("rho_st", C.POINTER(C.c_double)), ("r_2ut", C.POINTER(C.c_double)),
         ("levels_per_batch", C.c_int), ("use_graphs", C.c_int),
     ]
+
+
+class QgTuning(C.Structure):
+    _fields_ = [("levels_per_batch", C.c_int), ("ms_per_step", C.c_double), ("ncandidates", C.c_int),
+                ("candidates", C.c_int * 16), ("candidate_ms", C.c_double * 16)]
 
 
 class QgEnergy(C.Structure):
@@ -82,6 +89,14 @@ def lib() -> C.CDLL:
         "qg_A_solver_ybj_plus": (ip, [vp, vp, vp, vp]),
         "qg_profile_step": (ip, [vp, ip, dp, C.POINTER(C.c_int), ip]),
         "qg_fft_c2r_noalloc": (ip, [vp, vp, ip, ip, vp]),
+        "qg_ensemble_create": (ip, [C.POINTER(QgConfig), ip, C.POINTER(vp)]),
+        "qg_ensemble_member": (ip, [vp, ip, C.POINTER(vp)]),
+        "qg_ensemble_step": (ip, [vp, ip, ip]),
+        "qg_ensemble_synchronize": (ip, [vp]),
+        "qg_ensemble_get_stream": (ip, [vp, C.POINTER(vp)]),
+        "qg_ensemble_destroy": (ip, [vp]),
+        "qg_ensemble_last_error": (C.c_char_p, [vp]),
+        "qg_autotune": (ip, [C.POINTER(QgConfig), ip, C.POINTER(QgTuning)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

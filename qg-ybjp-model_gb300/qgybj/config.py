@@ -107,10 +107,11 @@ class RunConfig:
 # 512^2x256 mixed precision, ensemble members, adjoint case)
 CONFIGS = {
     "c0": RunConfig("c0_64x64x64_fp64", 64, 64, "fp64", steps=200, seed=0, k0=3.0),
+    # levels_per_batch: the choice of qg_autotune on GB300 for these sizes
     "c1": RunConfig("c1_256x256x128_fp64", 256, 128, "fp64", steps=200, seed=1, k0=6.0,
-                    stratification="exponential"),
+                    stratification="exponential", levels_per_batch=32),
     "c2": RunConfig("c2_512x512x256_mixed", 512, 256, "mixed", steps=100, seed=2, k0=8.0,
-                    stratification="exponential"),
+                    stratification="exponential", levels_per_batch=13),
     "c4": RunConfig("c4_128x128x64_fp64", 128, 64, "fp64", steps=50, seed=4, k0=3.0),
 }
 

@@ -13,7 +13,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import FIELDS, QG_PREC_FP64, QG_PREC_MIXED, QgConfig, QgEnergy, check, lib, ptr
+from ._lib import FIELDS, QG_PREC_FP64, QG_PREC_MIXED, QgConfig, QgEnergy, QgError, QgTuning, check, lib, ptr
 from .config import RunConfig, make_initial_condition, model_parameters
 
 
@@ -21,41 +21,62 @@ def _arr(a, n3=None):
     return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
 
 
+def make_config(params: dict, precision: str = "fp64", device: int = 0, levels_per_batch: int = 0,
+                use_graphs: int = 1, flags: dict | None = None):
+    """qg_config of a parameter dict; returns (config, arrays kept alive)."""
+    cfg = QgConfig()
+    check(lib().qg_config_defaults(C.byref(cfg)))
+    cfg.n1, cfg.n2, cfg.n3 = int(params["n1"]), int(params["n2"]), int(params["n3"])
+    cfg.precision = QG_PREC_FP64 if precision == "fp64" else QG_PREC_MIXED
+    cfg.device = device
+    for k in ("dz", "Bu", "Ro", "W2F", "delt", "gamma", "nuh1", "nuh2", "nuh1w", "nuh2w", "nuz"):
+        setattr(cfg, k, float(params.get(k, 0.0)))
+    for k in ("ilap1", "ilap2", "ilap1w", "ilap2w"):
+        setattr(cfg, k, int(params.get(k, 2)))
+    for k, v in (flags or {}).items():
+        setattr(cfg, k, int(v))
+    keep = []
+    for k in ("a_ell_ut", "rho_ut", "rho_st", "r_2ut"):
+        v = params.get(k)
+        if v is not None:
+            a = np.ascontiguousarray(v, dtype=np.float64)
+            keep.append(a)
+            setattr(cfg, k, a.ctypes.data_as(C.POINTER(C.c_double)))
+    cfg.levels_per_batch = levels_per_batch
+    cfg.use_graphs = use_graphs
+    return cfg, keep
+
+
+def autotune(params: dict, precision: str = "mixed", device: int = 0, nsteps: int = 3) -> dict:
+    """qg_autotune: fastest phase-A batch depth for these parameters."""
+    cfg, keep = make_config(params, precision, device)
+    t = QgTuning()
+    check(lib().qg_autotune(C.byref(cfg), int(nsteps), C.byref(t)))
+    return {"levels_per_batch": t.levels_per_batch, "ms_per_step": t.ms_per_step,
+            "candidates": {t.candidates[i]: t.candidate_ms[i] for i in range(t.ncandidates)}}
+
+
 class Simulation:
     def __init__(self, params: dict, precision: str = "fp64", device: int = 0, levels_per_batch: int = 0,
-                 use_graphs: int = 1, flags: dict | None = None):
+                 use_graphs: int = 1, flags: dict | None = None, _handle=None):
         L = lib()
-        cfg = QgConfig()
-        check(L.qg_config_defaults(C.byref(cfg)))
         self.n, self.n3 = int(params["n1"]), int(params["n3"])
-        cfg.n1, cfg.n2, cfg.n3 = int(params["n1"]), int(params["n2"]), int(params["n3"])
-        cfg.precision = QG_PREC_FP64 if precision == "fp64" else QG_PREC_MIXED
-        cfg.device = device
-        for k in ("dz", "Bu", "Ro", "W2F", "delt", "gamma", "nuh1", "nuh2", "nuh1w", "nuh2w", "nuz"):
-            setattr(cfg, k, float(params.get(k, 0.0)))
-        for k in ("ilap1", "ilap2", "ilap1w", "ilap2w"):
-            setattr(cfg, k, int(params.get(k, 2)))
-        for k, v in (flags or {}).items():
-            setattr(cfg, k, int(v))
-        self._keep = []
-        for k in ("a_ell_ut", "rho_ut", "rho_st", "r_2ut"):
-            v = params.get(k)
-            if v is not None:
-                a = np.ascontiguousarray(v, dtype=np.float64)
-                self._keep.append(a)
-                setattr(cfg, k, a.ctypes.data_as(C.POINTER(C.c_double)))
-        cfg.levels_per_batch = levels_per_batch
-        cfg.use_graphs = use_graphs
-        self.cfg = cfg
-        h = C.c_void_p()
-        check(L.qg_create(C.byref(cfg), C.byref(h)))
-        self.h = h
         self.precision = precision
+        if _handle is not None:          # a member handle owned by an Ensemble
+            self.h, self._owned, self._keep = _handle, False, []
+            self.cfg, _ = make_config(params, precision, device, levels_per_batch, use_graphs, flags)
+            return
+        self._owned = True
+        self.cfg, self._keep = make_config(params, precision, device, levels_per_batch, use_graphs, flags)
+        h = C.c_void_p()
+        check(L.qg_create(C.byref(self.cfg), C.byref(h)))
+        self.h = h
 
     # -- lifecycle -------------------------------------------------------------
     def close(self):
         if getattr(self, "h", None):
-            lib().qg_destroy(self.h)
+            if getattr(self, "_owned", True):
+                lib().qg_destroy(self.h)
             self.h = None
 
     def __enter__(self):
@@ -189,3 +210,60 @@ def simulation_for(rc: RunConfig, device: int = 0, precision: str | None = None)
     sim.set_state("BI", ic.BI)
     sim.init_state(apply_sumB=True, q_from_psi=True)
     return sim, ic, params
+
+
+class Ensemble:
+    """Independent runs of possibly different sizes advanced by one CUDA graph
+    launch per step (qg_ensemble_*).  ``members[m]`` is a Simulation view of
+    member m for state I/O; call synchronize() before touching members after
+    step()."""
+
+    def __init__(self, params_list: list[dict], precision: str = "mixed", device: int = 0,
+                 levels_per_batch: list[int] | None = None):
+        L = lib()
+        n = len(params_list)
+        cfgs = (QgConfig * n)()
+        self._keep = []
+        for m, p in enumerate(params_list):
+            lpb = levels_per_batch[m] if levels_per_batch else 0
+            c, keep = make_config(p, precision, device, lpb)
+            cfgs[m] = c
+            self._keep += keep
+        e = C.c_void_p()
+        st = L.qg_ensemble_create(cfgs, n, C.byref(e))
+        if st:
+            raise QgError(st, (L.qg_last_error(None) or b"").decode())
+        self.e = e
+        self.members = []
+        for m, p in enumerate(params_list):
+            h = C.c_void_p()
+            self._ck(L.qg_ensemble_member(self.e, m, C.byref(h)))
+            self.members.append(Simulation(p, precision, device, _handle=h))
+
+    def _ck(self, st):
+        if st:
+            raise QgError(st, (lib().qg_ensemble_last_error(self.e) or b"").decode())
+
+    def step(self, nsteps: int = 1, euler_first: bool = False):
+        self._ck(lib().qg_ensemble_step(self.e, int(nsteps), int(euler_first)))
+
+    def synchronize(self):
+        self._ck(lib().qg_ensemble_synchronize(self.e))
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._ck(lib().qg_ensemble_get_stream(self.e, C.byref(s)))
+        return int(s.value or 0)
+
+    def close(self):
+        if getattr(self, "e", None):
+            for m in self.members:
+                m.h = None
+            lib().qg_ensemble_destroy(self.e)
+            self.e = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -246,3 +246,39 @@ def test_error_statuses():
     # a valid call after errors still works
     sim.step(True)
     sim.close()
+
+
+# --- ensembles and the autotuner ----------------------------------------------------
+def test_ensemble_members_match_standalone_runs():
+    """Uneven members advanced by one graph launch per step give, member by
+    member, bit-identical fields to the same runs made alone."""
+    from qgybj import Ensemble
+    rcs = [scaled(CONFIGS["c0"], 32, 8), scaled(CONFIGS["c1"], 64, 16), scaled(CONFIGS["c0"], 32, 12)]
+    rcs[2].seed = 7
+    ics = [make_initial_condition(rc) for rc in rcs]
+    params = [model_parameters(rc, ic.delt) for rc, ic in zip(rcs, ics)]
+    ens = Ensemble(params, "mixed")
+    for sim, ic in zip(ens.members, ics):
+        sim.set_state("psi", ic.psi); sim.set_state("BR", ic.BR); sim.set_state("BI", ic.BI)
+        sim.init_state(True, True)
+    ens.step(5, euler_first=True)
+    ens.synchronize()
+    for sim, p, ic in zip(ens.members, params, ics):
+        alone = Simulation(p, "mixed")
+        alone.set_state("psi", ic.psi); alone.set_state("BR", ic.BR); alone.set_state("BI", ic.BI)
+        alone.init_state(True, True)
+        alone.steps_async(5, True)
+        alone.synchronize()
+        for f in FIELDS:
+            assert np.array_equal(sim.get_state(f), alone.get_state(f)), f
+        alone.close()
+    ens.close()
+
+
+def test_autotune_picks_a_timed_candidate():
+    from qgybj import autotune
+    rc = scaled(CONFIGS["c1"], 128, 32)
+    ic = make_initial_condition(rc)
+    t = autotune(model_parameters(rc, ic.delt), "mixed", nsteps=2)
+    assert t["levels_per_batch"] in t["candidates"]
+    assert t["ms_per_step"] == min(t["candidates"].values()) > 0
