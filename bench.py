@@ -403,6 +403,65 @@ def run_ensemble(args, world, rank, local):
     }
 
 
+def run_adjoint(args, world, rank, local):
+    """Adjoint-to-forward cost at 128^2x64 FP64 (constant N^2): J after
+    --steps steps and its gradient with respect to (q0, B0) with checkpoints
+    every --ckpt steps, against the forward steps alone on the same handle."""
+    import torch
+
+    import qgybj
+    from qgybj.config import make_initial_condition, model_parameters
+
+    if rank != 0:
+        return None
+    rc = workload(args)
+    ic = make_initial_condition(rc)
+    params = model_parameters(rc, ic.delt)
+    sim = qgybj.Simulation(params, "fp64", local)
+    sim.set_state("psi", ic.psi); sim.set_state("BR", ic.BR); sim.set_state("BI", ic.BI)
+    sim.init_state(True, True)
+    q0, BR0, BI0 = sim.get_state("q"), sim.get_state("BR"), sim.get_state("BI")
+    nsteps, every = args.steps, args.ckpt
+    dev = torch.device("cuda", local)
+    st = torch.cuda.ExternalStream(sim.stream(), device=dev)
+    sim.steps_async(args.warmup, True)
+    sim.synchronize()
+
+    def forward_ms():
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(st)
+        sim.steps_async(1, True)
+        sim.steps_async(nsteps - 1, False)
+        a1.record(st)
+        sim.synchronize()
+        return a0.elapsed_time(a1)
+
+    sim.adjoint_run(q0, BR0, BI0, nsteps, every)            # warm-up: buffers, graphs
+    fwd = min(forward_ms() for _ in range(3))
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.25)
+    reps = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        J, _ = sim.adjoint_run(q0, BR0, BI0, nsteps, every)
+        reps.append((time.perf_counter() - t0) * 1e3)
+    t0 = time.perf_counter()
+    sim.adjoint_run(q0, BR0, BI0, nsteps, every, gradient=False)
+    fwd_api = (time.perf_counter() - t0) * 1e3
+    clk = clocks.stop()
+    sim.close()
+    adj = min(reps)
+    return {
+        "metric": "adjoint/forward time", "value": adj / fwd, "unit": "ratio", "n_gpus": 1,
+        "steps": nsteps, "warmup": args.warmup, "ms_per_step": adj / nsteps, "higher_is_better": False,
+        "scaling": "none", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": f"{rc.name}_adjoint", "checkpoint_every": every, "objective": "LA subvolume"},
+        "forward_ms": fwd, "adjoint_ms": adj, "adjoint_ms_reps": reps, "forward_through_adjoint_api_ms": fwd_api,
+        "J": J, "clocks": clk,
+    }
+
+
 def sim_batch(sim) -> int:
     """Levels per phase-A batch as chosen by the library (same rule)."""
     from qgybj.config import kmax
@@ -482,6 +541,7 @@ def main(argv=None):
     ap.add_argument("--cpu-baseline-steps", type=int, default=6)
     ap.add_argument("--reference-budget-s", type=float, default=120.0)
     ap.add_argument("--members", type=int, default=0, help="c3: first M ensemble members only")
+    ap.add_argument("--ckpt", type=int, default=10, help="c4: checkpoint spacing of the adjoint")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3
@@ -490,6 +550,8 @@ def main(argv=None):
         out = run_reference(args, world, rank, local)
     elif args.config == "c3":
         out = run_ensemble(args, world, rank, local)
+    elif args.config == "c4":
+        out = run_adjoint(args, world, rank, local)
     else:
         out = run_ours(args, world, rank, local)
         if out is not None and world == 1 and not args.no_cpu_baseline:

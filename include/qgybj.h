@@ -179,6 +179,33 @@ int qg_psi_solver(qg_handle* h, const double* qstar, double* psik);
 /* elliptic.f90:346-460: all n3 levels; ck may be NULL. */
 int qg_A_solver_ybj_plus(qg_handle* h, const double* bk, double* ak, double* ck);
 
+/* ---- adjoint (no counterpart in the reference) ---------------------------- */
+
+/* Objective of qg_adjoint_run: J = sum over the subvolume of 1/2 |LA|^2 at the
+ * final step, LA = B + kh^2 A / (4 Bu) (diagnostics.f90:1698-1706) in physical
+ * space; subvolume = the central quarter of the horizontal domain
+ * (x, y in [n/4, 3n/4) grid points) and the levels with zs >= 0.8 (top 20 %). */
+enum { QG_OBJ_LA_SUBVOLUME = 0 };
+
+/* Reverse-mode gradient of J after nsteps (first step forward Euler) with
+ * respect to the initial q, BR and BI (all n3 levels, kvar layout, host or
+ * device pointers).  The forward model is the step with psi and A derived
+ * from (q, B) at every step, including t = 0 (psi0 = psi_solver(q0 - q^w(B0))).
+ * Checkpoints every ckpt_every steps; the forward steps inside a segment are
+ * recomputed with the step kernels, the reverse steps use hand-written
+ * adjoint kernels.  Gradients are with respect to the real and imaginary
+ * parts of the retained (L=1) modes; pass NULL gradients for J alone.
+ * FP64 handles only (QG_ERR_UNSUPPORTED otherwise); requires rho = 1. */
+int qg_adjoint_run(qg_handle* h, const double* q0, const double* BR0, const double* BI0, int nsteps,
+                   int ckpt_every, int objective, double* J, double* grad_q0, double* grad_BR0, double* grad_BI0);
+
+/* One step and its adjoint at the carried state X = (q, q_old, BR, BI,
+ * BR_old, BI_old) (six kvar arrays, all n3 levels): Xn = step(X) and
+ * lX_out = (d step/d X)^T lX.  For tangent-linear/adjoint (dot-product)
+ * checks.  Any of Xn / lX_out may be NULL. */
+int qg_adjoint_step(qg_handle* h, int euler_first, const double* const* X, const double* const* lX,
+                    double* const* Xn, double* const* lX_out);
+
 /* ---- ensembles and tuning (no counterpart in the reference) -------------- */
 
 /* An ensemble of independent runs, possibly of different sizes and

@@ -124,6 +124,8 @@ int build_tables(const qg_config& c, qg::HostTables& t, std::string& err) {
   std::vector<double> a(c.a_ell_ut, c.a_ell_ut + n3), ru(n3, 1.0), rs(n3, 1.0);
   if (c.rho_ut) ru.assign(c.rho_ut, c.rho_ut + n3);
   if (c.rho_st) rs.assign(c.rho_st, c.rho_st + n3);
+  t.rho_unit = true;
+  for (int i = 0; i < n3; ++i) t.rho_unit = t.rho_unit && ru[i] == 1.0 && rs[i] == 1.0;
   t.du.assign(n3, 0.0); t.cu.assign(n3, 0.0); t.cl.assign(n3, 0.0); t.r2.assign(n3, 0.0);
   for (int i = 0; i < n3; ++i) {
     if (i < n3 - 1) t.du[i] = ru[i] * a[i] / rs[i];
@@ -321,6 +323,22 @@ int qg_profile_step(qg_handle* h, int euler_first, double* ms, int* launches, in
   QG_ENTRY(h);
   if (!ms || !launches || nclasses <= 0) return fail(h, QG_ERR_ARG, "null output or nclasses <= 0");
   return fwd(h, h->eng->profile_step(euler_first, ms, launches, nclasses));
+}
+int qg_adjoint_run(qg_handle* h, const double* q0, const double* BR0, const double* BI0, int nsteps, int ckpt_every,
+                   int objective, double* J, double* gq, double* gR, double* gI) {
+  QG_ENTRY(h);
+  if (!q0 || !BR0 || !BI0 || !J || nsteps < 1 || ckpt_every < 1) return fail(h, QG_ERR_ARG, "qg_adjoint_run: bad arguments");
+  if (objective != QG_OBJ_LA_SUBVOLUME) return fail(h, QG_ERR_ARG, "qg_adjoint_run: unknown objective");
+  if ((gq || gR || gI) && !(gq && gR && gI)) return fail(h, QG_ERR_ARG, "qg_adjoint_run: pass all three gradients or none");
+  return fwd(h, h->eng->adjoint_run(q0, BR0, BI0, nsteps, ckpt_every, objective, J, gq, gR, gI));
+}
+int qg_adjoint_step(qg_handle* h, int euler_first, const double* const* X, const double* const* lX, double* const* Xn,
+                    double* const* lXo) {
+  QG_ENTRY(h);
+  if (!X) return fail(h, QG_ERR_ARG, "qg_adjoint_step: null state");
+  for (int i = 0; i < 6; ++i) if (!X[i]) return fail(h, QG_ERR_ARG, "qg_adjoint_step: null state field");
+  if (lXo && !lX) return fail(h, QG_ERR_ARG, "qg_adjoint_step: lX_out needs lX");
+  return fwd(h, h->eng->adjoint_step(euler_first, X, lX, Xn, lXo));
 }
 int qg_fft_r2c(qg_handle* h, const double* rvar, double* kvar, int nz) {
   QG_ENTRY(h);

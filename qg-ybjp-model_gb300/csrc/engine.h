@@ -19,6 +19,7 @@ struct HostTables {
   std::vector<double> du;                   // [n3] upper diagonal rho_ut a / rho_st
   std::vector<double> cu, cl;               // [n3] init_q coefficients of psi(z+1), psi(z-1)
   std::vector<double> r2;                   // [n3] N^2 at za(iz)
+  bool rho_unit = true;                     // rho_ut = rho_st = 1: symmetric vertical operators
 };
 
 struct EngineBase {
@@ -40,6 +41,17 @@ struct EngineBase {
   // levels per phase-A batch: current value and re-selection (drops graphs)
   virtual int batch_levels() const = 0;
   virtual int set_batch_levels(int zb) = 0;
+  // adjoint (FP64 engines only)
+  virtual int adjoint_run(const double* q0, const double* BR0, const double* BI0, int nsteps, int ckpt_every,
+                          int objective, double* J, double* gq, double* gR, double* gI) {
+    err = "the adjoint needs an FP64 handle";
+    return QG_ERR_UNSUPPORTED;
+  }
+  virtual int adjoint_step(int euler, const double* const* X, const double* const* lX, double* const* Xn,
+                           double* const* lXo) {
+    err = "the adjoint needs an FP64 handle";
+    return QG_ERR_UNSUPPORTED;
+  }
   virtual int fft_r2c(const double* rvar, double* kvar, int nz) = 0;
   virtual int fft_c2r(const double* kvar, double* rvar, int nz) = 0;
   virtual int convol_waqg(const double* uk, const double* vk, const double* qk, const double* BRk, const double* BIk,

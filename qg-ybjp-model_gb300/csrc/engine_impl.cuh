@@ -40,7 +40,7 @@ namespace qg {
 enum { F_Q = 0, F_QO, F_BR, F_BI, F_BRO, F_BIO, F_PSI, F_AR, F_AI, F_QSTAR, F_DQ, F_NINT };
 
 template <typename T>
-class Engine final : public EngineBase {
+class Engine : public EngineBase {
   using C = cplx<T>;
 
  public:
@@ -361,7 +361,7 @@ class Engine final : public EngineBase {
     return QG_OK;
   }
 
- private:
+ protected:
   qg_config cfg{};
   Geom g{};
   StepParams sp{};
@@ -502,7 +502,7 @@ class Engine final : public EngineBase {
     return QG_OK;
   }
 
- private:
+ protected:
   // Enqueue one step on st (no synchronisation; graph-capturable).
   int enqueue_step(int euler) {
     StepParams s = sp;

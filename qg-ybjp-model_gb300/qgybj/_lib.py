@@ -26,6 +26,7 @@ EXPORTS = (
     "qg_A_solver_ybj_plus", "qg_profile_step", "qg_fft_c2r_noalloc",
     "qg_ensemble_create", "qg_ensemble_member", "qg_ensemble_step", "qg_ensemble_synchronize",
     "qg_ensemble_get_stream", "qg_ensemble_destroy", "qg_ensemble_last_error", "qg_autotune",
+    "qg_adjoint_run", "qg_adjoint_step",
 )
 KERNEL_CLASSES = ("dissipation", "col_inv", "row_main", "col_update", "row_qw", "col_qw", "solve")
 
@@ -97,6 +98,8 @@ def lib() -> C.CDLL:
         "qg_ensemble_destroy": (ip, [vp]),
         "qg_ensemble_last_error": (C.c_char_p, [vp]),
         "qg_autotune": (ip, [C.POINTER(QgConfig), ip, C.POINTER(QgTuning)]),
+        "qg_adjoint_run": (ip, [vp, vp, vp, vp, ip, ip, ip, dp, vp, vp, vp]),
+        "qg_adjoint_step": (ip, [vp, ip, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

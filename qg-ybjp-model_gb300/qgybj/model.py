@@ -196,6 +196,33 @@ class Simulation:
         self._ck(lib().qg_A_solver_ybj_plus(self.h, ptr(b), ptr(a), ptr(c)))
         return a, c
 
+    # -- adjoint (FP64 handles) ------------------------------------------------------
+    def adjoint_run(self, q0, BR0, BI0, nsteps: int, ckpt_every: int = 10, gradient: bool = True):
+        """J = 1/2 sum over the central quarter and top fifth of |LA|^2 after
+        nsteps from (q0, B0), and its gradient with respect to (q0, BR0, BI0)."""
+        ins = [self._c(a) for a in (q0, BR0, BI0)]
+        J = C.c_double()
+        outs = [np.empty_like(ins[0]) for _ in range(3)] if gradient else [None] * 3
+        self._ck(lib().qg_adjoint_run(self.h, *[ptr(a) for a in ins], int(nsteps), int(ckpt_every), 0, C.byref(J),
+                                      *[ptr(a) for a in outs]))
+        return (J.value, tuple(outs)) if gradient else J.value
+
+    def adjoint_step(self, X, lX=None, euler_first: bool = False, forward: bool = True):
+        """One step from the carried state X = (q, q_old, BR, BI, BR_old, BI_old):
+        returns (next X or None, transpose of the step's Jacobian at X applied to lX or None)."""
+        Xs = [self._c(a) for a in X]
+        Xa = (C.c_void_p * 6)(*[ptr(a) for a in Xs])
+        Xn = [np.empty_like(Xs[0]) for _ in range(6)] if forward else None
+        lo = None
+        if lX is not None:
+            lXs = [self._c(a) for a in lX]
+            la = (C.c_void_p * 6)(*[ptr(a) for a in lXs])
+            lo = [np.empty_like(Xs[0]) for _ in range(6)]
+        self._ck(lib().qg_adjoint_step(self.h, int(euler_first), Xa, la if lX is not None else None,
+                                       (C.c_void_p * 6)(*[ptr(a) for a in Xn]) if forward else None,
+                                       (C.c_void_p * 6)(*[ptr(a) for a in lo]) if lo is not None else None))
+        return (tuple(Xn) if forward else None), (tuple(lo) if lo is not None else None)
+
 
 def simulation_for(rc: RunConfig, device: int = 0, precision: str | None = None):
     """Handle and initial condition of a run configuration: the
