@@ -105,3 +105,44 @@ def test_adjoint_refuses_mixed_and_vertical_diffusion():
         with pytest.raises(QgError) as e:
             sim.adjoint_run(st.q, st.BR, st.BI, 2, 1)
         assert e.value.status == QG_ERR_UNSUPPORTED
+
+
+def test_c4_full_size_gradient():
+    """128^2 x 64, 50 steps, checkpoints every 10: central differences along
+    8 seeded random unit directions (step 1e-6) and the dot-product test of
+    one step at this size."""
+    from qgybj.config import dealias_mask, make_initial_condition, model_parameters
+    rc = CONFIGS["c4"]
+    ic = make_initial_condition(rc)
+    params = model_parameters(rc, ic.delt)
+    n, nz = rc.n, rc.n3
+    Lb = dealias_mask(n)[None]
+    with Simulation(params, "fp64") as sim:
+        sim.set_state("psi", ic.psi); sim.set_state("BR", ic.BR); sim.set_state("BI", ic.BI)
+        sim.init_state(True, True)
+        q0, BR0, BI0 = sim.get_state("q"), sim.get_state("BR"), sim.get_state("BI")
+        J, g = sim.adjoint_run(q0, BR0, BI0, rc.steps, 10)
+        errs = []
+        for k in range(8):
+            d = tuple(random_masked(n, nz, 1000 + 3 * k + i) for i in range(3))
+            nrm = np.sqrt(inner(d, d, Lb))
+            d = tuple(x / nrm for x in d)
+            h = 1e-6
+            Jp = sim.adjoint_run(q0 + h * d[0], BR0 + h * d[1], BI0 + h * d[2], rc.steps, 10, gradient=False)
+            Jm = sim.adjoint_run(q0 - h * d[0], BR0 - h * d[1], BI0 - h * d[2], rc.steps, 10, gradient=False)
+            fd = (Jp - Jm) / (2 * h)
+            ad = inner(d, g, Lb)
+            errs.append(abs(fd - ad) / abs(ad))
+        assert max(errs) <= 1e-6, errs
+        # one step: <TL dX, lam> = <dX, ADJ lam>
+        X = (q0, q0, BR0, BI0, BR0, BI0)
+        dX = tuple(random_masked(n, nz, 2000 + i) for i in range(6))
+        lam = tuple(random_masked(n, nz, 3000 + i) for i in range(6))
+        eps = 1e-6
+        for first in (True, False):
+            Xp, _ = sim.adjoint_step(tuple(a + eps * b for a, b in zip(X, dX)), euler_first=first)
+            Xm, _ = sim.adjoint_step(tuple(a - eps * b for a, b in zip(X, dX)), euler_first=first)
+            tl = tuple((p - m) / (2 * eps) for p, m in zip(Xp, Xm))
+            _, lo = sim.adjoint_step(X, lam, euler_first=first, forward=False)
+            lhs, rhs = inner(tl, lam, Lb), inner(dX, lo, Lb)
+            assert abs(lhs - rhs) <= 1e-6 * max(abs(lhs), abs(rhs)), (first, lhs, rhs)
