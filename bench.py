@@ -16,6 +16,7 @@ step (the Fortran reference cannot be built here) on the host cores.
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import math
 import os
@@ -317,6 +318,8 @@ def workload(args):
     rc = CONFIGS[args.config]
     if args.n or args.n3:
         rc = scaled(rc, args.n or rc.n, args.n3 or rc.n3)
+    if getattr(args, "levels_per_batch", 0):
+        rc = dataclasses.replace(rc, levels_per_batch=args.levels_per_batch)
     return rc
 
 
@@ -550,6 +553,7 @@ def main(argv=None):
     ap.add_argument("--reference-budget-s", type=float, default=120.0)
     ap.add_argument("--members", type=int, default=0, help="c3: first M ensemble members only")
     ap.add_argument("--ckpt", type=int, default=10, help="c4: checkpoint spacing of the adjoint")
+    ap.add_argument("--levels-per-batch", type=int, default=0, help="override the phase-A batch depth")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3

@@ -173,7 +173,7 @@ __device__ __forceinline__ double2 pack_xy(double2 X, double2 Y, int k, int K, i
 }
 
 template <int N>
-__global__ void __launch_bounds__(kColThreads, 2)
+__global__ void __launch_bounds__(kColThreads, Tiles<double, N>::MINB)
 k_adj_col_inv(Geom g, AdjP p, int zbase, AdjIn L, const double* __restrict__ e1t, const double* __restrict__ e2t,
               const double* __restrict__ e1wt, const double* __restrict__ e2wt, double2* __restrict__ SA,
               const double2* __restrict__ twg) {
@@ -309,7 +309,7 @@ k_adj_row(Geom g, AdjP p, const double2* __restrict__ SF, double2* __restrict__ 
 }
 
 template <int N>
-__global__ void __launch_bounds__(kColThreads, 2)
+__global__ void __launch_bounds__(kColThreads, Tiles<double, N>::MINB)
 k_adj_col_fwd(Geom g, AdjP p, int zbase, AdjIn L, AdjOut O, const double* __restrict__ e1t,
               const double* __restrict__ e2t, const double* __restrict__ e1wt, const double* __restrict__ e2wt,
               const double2* __restrict__ SA, const double2* __restrict__ twg) {
@@ -374,7 +374,7 @@ k_adj_col_fwd(Geom g, AdjP p, int zbase, AdjIn L, AdjOut O, const double* __rest
 // y-inverse FFTs for the q^w transpose: BR, i ky BR, BI, i ky BI, w', ky^2 w'
 // with w' = w/(2N^2) ((0,0): Re w/N^2), into SF
 template <int N>
-__global__ void __launch_bounds__(kColThreads, 2)
+__global__ void __launch_bounds__(kColThreads, Tiles<double, N>::MINB)
 k_adj_qw_col_inv(Geom g, int zbase, const double2* __restrict__ BR, const double2* __restrict__ BI,
                  const double2* __restrict__ w, double2* __restrict__ SF, const double2* __restrict__ twg) {
   using T = double;
@@ -506,7 +506,7 @@ k_adj_qw_row(Geom g, AdjP p, double2* __restrict__ SF, const double2* __restrict
 
 // final adds: lq += w, lB += A_solver(lA) (+ q^w transpose when with_qw)
 template <int N>
-__global__ void __launch_bounds__(kColThreads, 2)
+__global__ void __launch_bounds__(kColThreads, Tiles<double, N>::MINB)
 k_adj_qw_col_fwd(Geom g, int zbase, int with_qw, double2* __restrict__ lq, double2* __restrict__ lBR,
                  double2* __restrict__ lBI, const double2* __restrict__ w, const double2* __restrict__ lBRa,
                  const double2* __restrict__ lBIa, const double2* __restrict__ SF, const double2* __restrict__ twg) {

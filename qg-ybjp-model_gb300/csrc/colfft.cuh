@@ -1,0 +1,165 @@
+// Column (y-direction) FFTs of a tile of CT spectral columns, interleaved in
+// shared memory, with the first pass fed from registers and the last pass
+// handed back in registers.
+//
+// Shared layout: element j of column c of field f at f*FS + pad_idx(j)*CT + c
+// (FS = PadLD<N>*CT).  Threads take tasks (c, j) with c fastest, so a warp
+// touches CT consecutive columns of 32/CT consecutive rows: global loads
+// and stores of the prologue / epilogue are coalesced row segments, and the
+// shared accesses of every pass hit each bank slot equally often.
+//
+// The passes are the Stockham radix-8/4/2 passes of fft_block.cuh (same
+// order of operations and twiddles, so results are bitwise those of fft_ip):
+//   pass 0 (NS = 1):   v = pro(c, j) -> DFT -> shared
+//   middle passes:     shared -> twiddle, DFT -> shared (in place)
+//   last pass:         shared -> twiddle, DFT -> epi(c, j, v)
+// pro fills v[f][r] with the input at index j + r*N/R0 of field f; epi gets
+// v[f][r] = output at index j + r*NS_last.  Every thread's cp.async copies
+// issued before the call have landed and are visible to the whole CTA when
+// epi runs.  Callers synchronise before reusing the shared buffer after
+// col_fft returns.
+#pragma once
+#include "fft_block.cuh"
+
+namespace qg {
+
+template <int N, int CT> struct ColLay {
+  static constexpr int FS = PadLD<N>::value * CT;
+};
+
+// number of passes and the stride NS of the last one
+template <int N> struct LastNS {
+  static constexpr int calc() {
+    int ns = 1;
+    while (ns * radix_of(N / ns) < N) ns *= radix_of(N / ns);
+    return ns;
+  }
+  static constexpr int value = calc();
+};
+
+// completes this thread's outstanding cp.async copies (staging that a
+// caller issued before col_fft; the barrier after the call publishes them)
+__device__ __forceinline__ void col_cp_wait() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
+template <typename T, int N, int R, int NS, bool FWD, int NF, int CT, int NT, bool LASTMID>
+__device__ __forceinline__ void col_mid_pass(cplx<T>* __restrict__ sm, const cplx<T>* __restrict__ tw) {
+  constexpr int FS = ColLay<N, CT>::FS;
+  constexpr int NB = N / R;
+  constexpr int TASKS = CT * NB;
+  constexpr int PER = (TASKS + NT - 1) / NT;
+  cplx<T> v[PER][NF][R];
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int t = tid + p * NT;
+    if ((TASKS % NT) == 0 || t < TASKS) {
+      const int c = t % CT, j = t / CT;
+#pragma unroll
+      for (int f = 0; f < NF; ++f)
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[p][f][r] = sm[f * FS + pad_idx(j + r * NB) * CT + c];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int t = tid + p * NT;
+    if ((TASKS % NT) == 0 || t < TASKS) {
+      const int c = t % CT, j = t / CT;
+      const int k = j & (NS - 1);
+      constexpr int off = tw_off<N>(NS);
+#pragma unroll
+      for (int f = 0; f < NF; ++f) {
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+          cplx<T> w = tw[off + (r - 1) * NS + k];
+          if (!FWD) w.y = -w.y;
+          v[p][f][r] = cmul(v[p][f][r], w);
+        }
+        dftR<T, R, FWD>(v[p][f]);
+      }
+      const int base = (j - k) * R + k;
+#pragma unroll
+      for (int f = 0; f < NF; ++f)
+#pragma unroll
+        for (int r = 0; r < R; ++r) sm[f * FS + pad_idx(base + r * NS) * CT + c] = v[p][f][r];
+    }
+  }
+  if constexpr (LASTMID) col_cp_wait();
+  __syncthreads();
+}
+
+template <typename T, int N, int NS, bool FWD, int NF, int CT, int NT>
+__device__ __forceinline__ void col_mid_passes(cplx<T>* sm, const cplx<T>* tw) {
+  constexpr int R = radix_of(N / NS);
+  if constexpr (NS < LastNS<N>::value) {
+    col_mid_pass<T, N, R, NS, FWD, NF, CT, NT, (NS * R >= LastNS<N>::value)>(sm, tw);
+    col_mid_passes<T, N, NS * R, FWD, NF, CT, NT>(sm, tw);
+  }
+}
+
+template <typename T, int N, bool FWD, int NF, int CT, int NT, class Pro, class Epi>
+__device__ __forceinline__ void col_fft(cplx<T>* __restrict__ sm, const cplx<T>* __restrict__ tw, Pro pro, Epi epi) {
+  constexpr int FS = ColLay<N, CT>::FS;
+  const int tid = threadIdx.x;
+  // pass 0 (NS = 1): inputs from the prologue
+  {
+    constexpr int R = radix_of(N);
+    constexpr int NB = N / R;
+    constexpr int TASKS = CT * NB;
+    constexpr int PER = (TASKS + NT - 1) / NT;
+#pragma unroll
+    for (int p = 0; p < PER; ++p) {
+      const int t = tid + p * NT;
+      if ((TASKS % NT) == 0 || t < TASKS) {
+        const int c = t % CT, j = t / CT;
+        cplx<T> v[NF][R];
+        pro(c, j, v);
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+          dftR<T, R, FWD>(v[f]);
+#pragma unroll
+          for (int r = 0; r < R; ++r) sm[f * FS + pad_idx(j * R + r) * CT + c] = v[f][r];
+        }
+      }
+    }
+  }
+  if constexpr (radix_of(N) >= LastNS<N>::value) col_cp_wait();   // no middle pass
+  __syncthreads();
+  col_mid_passes<T, N, radix_of(N), FWD, NF, CT, NT>(sm, tw);
+  // last pass: outputs to the epilogue
+  {
+    constexpr int NS = LastNS<N>::value;
+    constexpr int R = N / NS;
+    constexpr int NB = N / R;     // == NS
+    constexpr int TASKS = CT * NB;
+    constexpr int PER = (TASKS + NT - 1) / NT;
+    constexpr int off = tw_off<N>(NS);
+#pragma unroll
+    for (int p = 0; p < PER; ++p) {
+      const int t = tid + p * NT;
+      if ((TASKS % NT) == 0 || t < TASKS) {
+        const int c = t % CT, j = t / CT;
+        cplx<T> v[NF][R];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+#pragma unroll
+          for (int r = 0; r < R; ++r) v[f][r] = sm[f * FS + pad_idx(j + r * NB) * CT + c];
+#pragma unroll
+          for (int r = 1; r < R; ++r) {
+            cplx<T> w = tw[off + (r - 1) * NS + j];
+            if (!FWD) w.y = -w.y;
+            v[f][r] = cmul(v[f][r], w);
+          }
+          dftR<T, R, FWD>(v[f]);
+        }
+        epi(c, j, v);
+      }
+    }
+  }
+}
+
+}  // namespace qg

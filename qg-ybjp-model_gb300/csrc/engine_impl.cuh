@@ -428,8 +428,11 @@ class Engine : public EngineBase {
   }
 
   // shared memory of the step kernels (twiddles + padded transforms)
+  // column kernels on the interleaved tile (colfft.cuh): NF fields in flight
+  template <int NN> static constexpr size_t sm_ci(int nf) {
+    return (size_t)(NN + nf * ColLay<NN, Tiles<T, NN>::CT>::FS) * sizeof(C);
+  }
   template <int NN> static constexpr size_t sm_col6() { return (size_t)(NN + 6 * Tiles<T, NN>::CT * Tiles<T, NN>::LD) * sizeof(C); }
-  template <int NN> static constexpr size_t sm_col2() { return (size_t)(NN + 2 * Tiles<T, NN>::CT * Tiles<T, NN>::LD) * sizeof(C); }
   template <int NN> static constexpr size_t sm_row7() { return (size_t)(NN + 7 * Tiles<T, NN>::RT * Tiles<T, NN>::LD) * sizeof(C); }
   template <int NN> static constexpr size_t sm_row4() { return (size_t)(NN + 4 * Tiles<T, NN>::RT * Tiles<T, NN>::LD) * sizeof(C); }
   // shared memory of the dense (routine-level) kernels
@@ -439,11 +442,11 @@ class Engine : public EngineBase {
   int set_smem_attrs() {
     const int mx = cudaFuncAttributeMaxDynamicSharedMemorySize;
     QG_SWITCH_N(g.n, {
-      QG_CK(cudaFuncSetAttribute(k_col_inv<T, NN>, (cudaFuncAttribute)mx, (int)sm_col6<NN>()));
+      QG_CK(cudaFuncSetAttribute(k_col_inv<T, NN>, (cudaFuncAttribute)mx, (int)sm_ci<NN>(3)));
       QG_CK(cudaFuncSetAttribute(k_row_main<T, NN>, (cudaFuncAttribute)mx, (int)sm_row7<NN>()));
-      QG_CK(cudaFuncSetAttribute(k_col_update<T, NN>, (cudaFuncAttribute)mx, (int)sm_col6<NN>()));
+      QG_CK(cudaFuncSetAttribute(k_col_update<T, NN>, (cudaFuncAttribute)mx, (int)UpdLay<T, NN>::bytes()));
       QG_CK(cudaFuncSetAttribute(k_row_qw<T, NN>, (cudaFuncAttribute)mx, (int)sm_row4<NN>()));
-      QG_CK(cudaFuncSetAttribute(k_col_qw<T, NN>, (cudaFuncAttribute)mx, (int)sm_col2<NN>()));
+      QG_CK(cudaFuncSetAttribute(k_col_qw<T, NN>, (cudaFuncAttribute)mx, (int)sm_ci<NN>(2)));
       // per-function attribute shared by every handle: set it for the deepest supported column
       QG_CK(cudaFuncSetAttribute(k_solve<T>, (cudaFuncAttribute)mx, (int)solve_smem(kMaxN3)));
       QG_CK(cudaFuncSetAttribute(k_dcol_inv<T, NN>, (cudaFuncAttribute)mx, (int)sm_colinv()));
@@ -520,7 +523,7 @@ class Engine : public EngineBase {
       QG_SWITCH_N(g.n, {
         const dim3 gc(g.KXP / Tiles<T, NN>::CT, zc), gr(g.n / Tiles<T, NN>::RT, zc);
         if (int rc0 = pbeg(QG_K_COL_INV)) return rc0;
-        k_col_inv<T, NN><<<gc, kColThreads, sm_col6<NN>(), st>>>(g, z0, F[F_PSI], F[F_Q], F[F_BR], F[F_BI], S, tw);
+        k_col_inv<T, NN><<<gc, kColThreads, sm_ci<NN>(3), st>>>(g, z0, F[F_PSI], F[F_Q], F[F_BR], F[F_BI], S, tw);
         QG_LAUNCHED();
         if (int rc0 = pend()) return rc0;
         if (int rc0 = pbeg(QG_K_ROW_MAIN)) return rc0;
@@ -528,7 +531,7 @@ class Engine : public EngineBase {
         QG_LAUNCHED();
         if (int rc0 = pend()) return rc0;
         if (int rc0 = pbeg(QG_K_COL_UPDATE)) return rc0;
-        k_col_update<T, NN><<<gc, kColThreads, sm_col6<NN>(), st>>>(g, s, z0, sptr, e1, e2, e1w, e2w, S, tw,
+        k_col_update<T, NN><<<gc, kColThreads, UpdLay<T, NN>::bytes(), st>>>(g, s, z0, sptr, e1, e2, e1w, e2w, S, tw,
                                                                 need_qw ? 1 : 0);
         QG_LAUNCHED();
         if (int rc0 = pend()) return rc0;
@@ -538,7 +541,7 @@ class Engine : public EngineBase {
           QG_LAUNCHED();
           if (int rc0 = pend()) return rc0;
           if (int rc0 = pbeg(QG_K_COL_QW)) return rc0;
-          k_col_qw<T, NN><<<gc, kThreadsB, sm_col2<NN>(), st>>>(g, s, z0, F[F_Q], F[F_QSTAR], S, tw);
+          k_col_qw<T, NN><<<gc, kThreadsB, sm_ci<NN>(2), st>>>(g, s, z0, F[F_Q], F[F_QSTAR], S, tw);
           QG_LAUNCHED();
           if (int rc0 = pend()) return rc0;
         }

@@ -12,6 +12,7 @@
 #pragma once
 #include "common.cuh"
 #include "fft_block.cuh"
+#include "colfft.cuh"
 
 namespace qg {
 
@@ -44,9 +45,20 @@ template <typename T, int N> struct Tiles {
   static constexpr int CT = ct0 >= 8 ? 8 : (ct0 >= 1 ? ct0 : 1);
   static constexpr int rt0 = (8192 / CB) / N;
   static constexpr int RT = rt0 >= 2 ? 2 : 1;
-  // transform stride: odd number of elements, so the CT columns of a tile
-  // that consecutive threads fill and drain fall in different banks
-  static constexpr int LD = PadLD<N>::value + 1;
+  // transform stride.  A warp filling or draining a column tile touches CT
+  // columns x (32/CT) consecutive rows; with LD = 32/CT modulo the elements
+  // of one 128-byte shared-memory wavefront (SLOTS), the columns' row runs
+  // interleave and every bank slot is hit equally often (no replays beyond
+  // the access width)
+  static constexpr int SLOTS = 128 / CB;
+  static constexpr int RW = 32 / CT;
+  static constexpr int P0 = PadLD<N>::value;
+  static constexpr int LD = P0 + ((RW % SLOTS) - (P0 % SLOTS) + SLOTS) % SLOTS;
+  // CTAs per SM that the shared memory of a six-field column tile allows
+  // (228 KB per SM, 1 KB reserved per CTA), the column kernels' occupancy target
+  static constexpr int SM6 = (N + 6 * CT * LD) * CB;
+  static constexpr int mb0 = 233472 / (SM6 + 1024);
+  static constexpr int MINB = mb0 >= 4 ? 4 : (mb0 >= 1 ? mb0 : 1);
 };
 constexpr int kColThreads = 256;   // k_col_inv, k_col_update
 constexpr int kThreadsB = 256;     // row kernels, k_col_qw
@@ -76,65 +88,68 @@ __device__ __forceinline__ void cp_async_wait_all() {
 // ===========================================================================
 // Phase A, kernel 1: y-inverse FFTs of the six fields needed in physical space
 // ===========================================================================
+// one column entry of a field at FFT index idx, realit (fft.f90:88-107)
+// applied: at kx = 0 the entries of negative ky are the conjugates of the
+// positive ones.  `row` is the compact row the value comes from (-1: zero),
+// `cj` whether it is conjugated.
+__device__ __forceinline__ void col_src(const Geom& g, int kx, int idx, int& row, bool& cj) {
+  cj = kx == 0 && idx > g.n / 2;
+  row = kx <= g.K ? g.row_of_fft_index(cj ? g.n - idx : idx) : -1;
+}
+
 template <typename T, int N>
-__global__ void __launch_bounds__(kColThreads, 2)
+__global__ void __launch_bounds__(kColThreads, Tiles<T, N>::MINB)
 k_col_inv(Geom g, int zbase, const cplx<T>* __restrict__ psi, const cplx<T>* __restrict__ q,
           const cplx<T>* __restrict__ BR, const cplx<T>* __restrict__ BI, cplx<T>* __restrict__ S,
           const cplx<T>* __restrict__ twg) {
-  constexpr int CT = Tiles<T, N>::CT, LD = Tiles<T, N>::LD, NT = kColThreads;
+  constexpr int CT = Tiles<T, N>::CT, NT = kColThreads;
+  constexpr int R0 = radix_of(N), NB0 = N / R0, NSL = LastNS<N>::value, RL = N / NSL;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* buf = tw + N;                       // [6][CT][LD]
-  const int tid = threadIdx.x;
+  cplx<T>* sm = tw + N;                        // [3][FS]
   const int zb = blockIdx.y, z = zbase + zb;
   const int kx0 = blockIdx.x * CT;
   load_tw<T, N>(tw, twg, NT);
+  __syncthreads();
   const long long zoff = (long long)z * g.plane;
-  // raw columns: psi -> slot 2, q -> 3, BR -> 4, BI -> 5 (asynchronous copies)
-#pragma unroll
-  for (int src = 0; src < 4; ++src) {
-    const cplx<T>* F = src == 0 ? psi : (src == 1 ? q : (src == 2 ? BR : BI));
-    cplx<T>* slot = buf + (src + 2) * CT * LD;
-#pragma unroll 4
-    for (int e = tid; e < CT * N; e += NT) {
-      const int c = e % CT, j = e / CT;
-      const int kx = kx0 + c;
-      const int r = g.row_of_fft_index(j);
-      const bool in = kx <= g.K && r >= 0;
-      cp_async_c<T>(slot + c * LD + pad_idx(j), in ? F + zoff + (long long)r * g.KXP + kx : F, in);
-    }
-  }
-  cp_async_wait_all();
-  __syncthreads();
   // u = -i ky psi (derivatives.f90:1309), v = i kx psi (1310), zeta = -kh^2 psi (842)
-  for (int e = tid; e < CT * N; e += NT) {
-    const int c = e % CT, j = e / CT;
-    const int r = g.row_of_fft_index(j);
-    const T ky = r >= 0 ? (T)g.ky_of_row(r) : (T)0;
-    const T kx = (T)(kx0 + c);
-    const int o = c * LD + pad_idx(j);
-    const cplx<T> sv = buf[2 * CT * LD + o];
-    buf[0 * CT * LD + o] = cscale(cmul_mi(sv), ky);
-    buf[1 * CT * LD + o] = cscale(cmul_i(sv), kx);
-    buf[2 * CT * LD + o] = cscale(sv, -(kx * kx + ky * ky));
-  }
-  __syncthreads();
-  if (kx0 == 0) {    // realit (fft.f90:88-107) on the kx=0 column of each field
-    for (int e = tid; e < 6 * (N / 2 - 1); e += NT) {
-      const int f = e / (N / 2 - 1), j = 1 + e % (N / 2 - 1);
-      cplx<T>* col = buf + f * CT * LD;
-      col[pad_idx(N - j)] = cconj(col[pad_idx(j)]);
+  auto pro_psi = [&](int c, int j, cplx<T> (&v)[3][R0]) {
+    const int kx = kx0 + c;
+#pragma unroll
+    for (int r = 0; r < R0; ++r) {
+      int row; bool cj;
+      col_src(g, kx, j + r * NB0, row, cj);
+      const cplx<T> sv = row >= 0 ? psi[zoff + (long long)row * g.KXP + kx] : mk<T>(0, 0);
+      const T ky = row >= 0 ? (T)g.ky_of_row(row) : (T)0;
+      const T fkx = (T)kx;
+      cplx<T> a = cscale(cmul_mi(sv), ky), b = cscale(cmul_i(sv), fkx), d = cscale(sv, -(fkx * fkx + ky * ky));
+      if (cj) { a = cconj(a); b = cconj(b); d = cconj(d); }
+      v[0][r] = a; v[1][r] = b; v[2][r] = d;
     }
-    __syncthreads();
-  }
-  // two groups of three fields keep a thread's butterflies in registers
-  fft_ip<T, N, false, 3 * CT, NT, LD>(buf, tw);
-  fft_ip<T, N, false, 3 * CT, NT, LD>(buf + 3 * CT * LD, tw);
-#pragma unroll 4
-  for (int e = tid; e < 6 * CT * N; e += NT) {
-    const int c = e % CT, y = (e / CT) % N, f = e / (CT * N);
-    S[scr_off(zb, f, y, N, g.KXP) + kx0 + c] = buf[(f * CT + c) * LD + pad_idx(y)];
-  }
+  };
+  auto pro_raw = [&](int c, int j, cplx<T> (&v)[3][R0]) {
+    const int kx = kx0 + c;
+#pragma unroll
+    for (int r = 0; r < R0; ++r) {
+      int row; bool cj;
+      col_src(g, kx, j + r * NB0, row, cj);
+      const long long m = zoff + (long long)row * g.KXP + kx;
+      cplx<T> a = row >= 0 ? q[m] : mk<T>(0, 0), b = row >= 0 ? BR[m] : mk<T>(0, 0), d = row >= 0 ? BI[m] : mk<T>(0, 0);
+      if (cj) { a = cconj(a); b = cconj(b); d = cconj(d); }
+      v[0][r] = a; v[1][r] = b; v[2][r] = d;
+    }
+  };
+  auto epi = [&](int f0) {
+    return [&, f0](int c, int j, cplx<T> (&v)[3][RL]) {
+#pragma unroll
+      for (int f = 0; f < 3; ++f)
+#pragma unroll
+        for (int r = 0; r < RL; ++r) S[scr_off(zb, f0 + f, j + r * NSL, N, g.KXP) + kx0 + c] = v[f][r];
+    };
+  };
+  col_fft<T, N, false, 3, CT, NT>(sm, tw, pro_psi, epi(0));
+  __syncthreads();
+  col_fft<T, N, false, 3, CT, NT>(sm, tw, pro_raw, epi(3));
 }
 
 // Hermitian-extended packed spectrum X + iY of two real rows from their
@@ -235,32 +250,47 @@ template <typename T> struct StateP {
 // ===========================================================================
 // Phase A, kernel 3: y-forward FFTs, time update, y-inverse FFTs for q^w
 // ===========================================================================
+// Shared memory: twiddles | two interleaved transforms | the tile's state of
+// the variable being updated (3 complex fields, staged by cp.async while its
+// tendencies are transformed) | B^{n+1} (2 complex fields) | 2 IF tables.
+template <typename T, int N> struct UpdLay {
+  static constexpr int CT = Tiles<T, N>::CT;
+  static constexpr int KYM = 2 * ((N + 2) / 3) + 1;     // >= KY for this n
+  static constexpr int FE = CT * KYM;                   // entries per staged field
+  static constexpr size_t bytes() {
+    return (size_t)(N + 2 * ColLay<N, CT>::FS + 5 * FE) * sizeof(cplx<T>) + (size_t)2 * FE * sizeof(T);
+  }
+};
+
+template <typename T>
+__device__ __forceinline__ void cp_async_s(T* dst, const T* src, bool valid) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  if constexpr (sizeof(T) == 4) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(valid ? 4 : 0));
+  } else {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(valid ? 8 : 0));
+  }
+}
+
 template <typename T, int N>
-__global__ void __launch_bounds__(kColThreads, 2)
+__global__ void __launch_bounds__(kColThreads, Tiles<T, N>::MINB)
 k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict__ e1t, const T* __restrict__ e2t,
              const T* __restrict__ e1wt, const T* __restrict__ e2wt, cplx<T>* __restrict__ S,
              const cplx<T>* __restrict__ twg, int qw_prep) {
-  constexpr int CT = Tiles<T, N>::CT, LD = Tiles<T, N>::LD, NT = kColThreads;
+  using L = UpdLay<T, N>;
+  constexpr int CT = Tiles<T, N>::CT, NT = kColThreads, FE = L::FE;
+  constexpr int R0 = radix_of(N), NB0 = N / R0, NSL = LastNS<N>::value, RL = N / NSL;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* buf = tw + N;                 // [6][CT][LD]
+  cplx<T>* sm = tw + N;                          // [2][FS]
+  cplx<T>* stg = sm + 2 * ColLay<N, CT>::FS;     // [3][FE]: x, x_old, third (dq / AI / AR)
+  cplx<T>* bnew = stg + 3 * FE;                  // [2][FE]: BR, BI at n+1
+  T* tab = reinterpret_cast<T*>(bnew + 2 * FE);  // [2][FE]: e1, e2 or e1w, e2w
   const int tid = threadIdx.x;
   const int zb = blockIdx.y, z = zbase + zb;
   const int kx0 = blockIdx.x * CT;
   const int KY = g.KY;
   load_tw<T, N>(tw, twg, NT);
-#pragma unroll 4
-  for (int e = tid; e < 6 * CT * N; e += NT) {
-    const int c = e % CT, y = (e / CT) % N, h = e / (CT * N);
-    const int kx = kx0 + c;
-    cp_async_c<T>(buf + (h * CT + c) * LD + pad_idx(y), S + scr_off(zb, h, y, N, g.KXP) + kx, kx <= g.K);
-  }
-  cp_async_wait_all();
-  __syncthreads();
-  fft_ip<T, N, true, 3 * CT, NT, LD>(buf, tw);
-  fft_ip<T, N, true, 3 * CT, NT, LD>(buf + 3 * CT * LD, tw);
-  // tendencies and time update (main_waqg.f90:237-264, 362-415): one mode
-  // (column c, row r) per iteration, all of its loads issued together
   const T inv_n2 = (T)1 / ((T)N * (T)N);
   const long long zoff = (long long)z * g.plane;
   const T dt = (T)sp.delt;
@@ -268,90 +298,131 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
   const T gam = (T)sp.gamma;
   const T cdisp = sp.disp ? (T)sp.cdisp : (T)0;
   const bool eul = sp.euler != 0;
-#pragma unroll 2
-  for (int e = tid; e < CT * KY; e += NT) {
-    const int c = e % CT, r = e / CT;
-    const int kx = kx0 + c;
-    if (kx > g.K) continue;
-    const int ky = g.ky_of_row(r);
-    const long long m = zoff + (long long)r * g.KXP + kx;
-    const long long mt = (long long)r * g.KXP + kx;
-    const cplx<T> q0 = st.q[m], r0 = st.BR[m], i0 = st.BI[m];
-    const cplx<T> qo = eul ? q0 : st.qo[m], ro = eul ? r0 : st.BRo[m], io = eul ? i0 : st.BIo[m];
-    const cplx<T> ar = st.AR[m], ai = st.AI[m];
-    const cplx<T> dqv = sp.use_dq ? st.dq[m] : mk<T>(0, 0);
-    const T e1 = e1t[mt], e2 = e2t[mt], e1w = e1wt[mt], e2w = e2wt[mt];
-    const int j = pad_idx(g.fft_index_of_row(r));
-    cplx<T> tq, tr, ti;
-    {
-      const cplx<T> G0 = buf[(0 * CT + c) * LD + j], H0 = buf[(1 * CT + c) * LD + j];
-      const cplx<T> G1 = buf[(2 * CT + c) * LD + j], H1 = buf[(3 * CT + c) * LD + j];
-      const cplx<T> G2 = buf[(4 * CT + c) * LD + j], H2 = buf[(5 * CT + c) * LD + j];
-      const T fky = (T)ky;
-      tq = cscale(mk<T>(G0.x - fky * H0.y, G0.y + fky * H0.x), inv_n2);   // G + i ky H
-      tr = cscale(mk<T>(G1.x - fky * H1.y, G1.y + fky * H1.x), inv_n2);
-      ti = cscale(mk<T>(G2.x - fky * H2.y, G2.y + fky * H2.x), inv_n2);
-    }
-    cplx<T> qn = mk<T>(0, 0), rn = mk<T>(0, 0), in_ = mk<T>(0, 0);
-    cplx<T> qf = eul ? qo : mk<T>(0, 0), rf = eul ? ro : mk<T>(0, 0), if_ = eul ? io : mk<T>(0, 0);
-    if (g.mask(kx, ky)) {
-      const T ck = cdisp * (T)(kx * kx + ky * ky);
-      const cplx<T> fr = cadd(tr, cscale(ai, ck));     // nBR - 0.5 rBI + c kh2 AI
-      const cplx<T> fi = csub(ti, cscale(ar, ck));     // nBI + 0.5 rBR - c kh2 AR
-      if (eul) {
-        qn = cscale(cadd(csub(qo, cscale(tq, dt)), cscale(dqv, dt)), e1);
-        rn = cscale(csub(ro, cscale(fr, dt)), e1w);
-        in_ = cscale(csub(io, cscale(fi, dt)), e1w);
-      } else {
-        qn = cadd(csub(cscale(qo, e2), cscale(cscale(tq, dt2), e1)), cscale(cscale(dqv, dt2), e2));
-        rn = csub(cscale(ro, e2w), cscale(cscale(fr, dt2), e1w));
-        in_ = csub(cscale(io, e2w), cscale(cscale(fi, dt2), e1w));
-        // Robert-Asselin filter (main_waqg.f90:395-410)
-        qf = cadd(q0, cscale(cadd(csub(qo, cscale(q0, (T)2)), qn), gam));
-        rf = cadd(r0, cscale(cadd(csub(ro, cscale(r0, (T)2)), rn), gam));
-        if_ = cadd(i0, cscale(cadd(csub(io, cscale(i0, (T)2)), in_), gam));
+  // staged entry (c, row) at row*CT + c
+  auto stage = [&](int which) {
+    const cplx<T>* X = which == 0 ? st.q : (which == 1 ? st.BR : st.BI);
+    const cplx<T>* Xo = which == 0 ? st.qo : (which == 1 ? st.BRo : st.BIo);
+    const cplx<T>* X3 = which == 0 ? st.dq : (which == 1 ? st.AI : st.AR);
+    const bool need3 = which != 0 || sp.use_dq;
+    for (int e = tid; e < CT * KY; e += NT) {
+      const int c = e % CT, row = e / CT;
+      const int kx = kx0 + c;
+      const bool in = kx <= g.K;
+      const long long m = zoff + (long long)row * g.KXP + kx;
+      cp_async_c<T>(stg + e, in ? X + m : X, in);
+      if (!eul) cp_async_c<T>(stg + FE + e, in ? Xo + m : Xo, in);
+      if (need3) cp_async_c<T>(stg + 2 * FE + e, in ? X3 + m : X3, in);
+      if (which < 2) {
+        const long long mt = (long long)row * g.KXP + kx;
+        const T* t1 = which == 0 ? e1t : e1wt;
+        const T* t2 = which == 0 ? e2t : e2wt;
+        cp_async_s<T>(tab + e, in ? t1 + mt : t1, in);
+        cp_async_s<T>(tab + FE + e, in ? t2 + mt : t2, in);
       }
     }
-    st.q[m] = qn; st.BR[m] = rn; st.BI[m] = in_;
-    st.qo[m] = qf; st.BRo[m] = rf; st.BIo[m] = if_;
-  }
+  };
+  // tendencies G + i ky H of (q, BR, BI) from the (G, H) plane pairs 0-1, 2-3, 4-5
+  auto pro_planes = [&](int h0) {
+    return [&, h0](int c, int j, cplx<T> (&v)[2][R0]) {
+      const int kx = kx0 + c;
+#pragma unroll
+      for (int r = 0; r < R0; ++r) {
+        const int y = j + r * NB0;
+        const bool in = kx <= g.K;
+        v[0][r] = in ? S[scr_off(zb, h0, y, N, g.KXP) + kx] : mk<T>(0, 0);
+        v[1][r] = in ? S[scr_off(zb, h0 + 1, y, N, g.KXP) + kx] : mk<T>(0, 0);
+      }
+    };
+  };
+  // time update (main_waqg.f90:237-264, 362-415) of one variable
+  // (which = 0 q, 1 BR, 2 BI), one mode per output index
+  auto epi_update = [&](int which) {
+    return [&, which](int c, int j, cplx<T> (&v)[2][RL]) {
+      const int kx = kx0 + c;
+      if (kx > g.K) return;
+      cplx<T>* X = which == 0 ? st.q : (which == 1 ? st.BR : st.BI);
+      cplx<T>* Xo = which == 0 ? st.qo : (which == 1 ? st.BRo : st.BIo);
+#pragma unroll
+      for (int r = 0; r < RL; ++r) {
+        const int row = g.row_of_fft_index(j + r * NSL);
+        if (row < 0) continue;
+        const int ky = g.ky_of_row(row);
+        const int e = row * CT + c;
+        const long long m = zoff + (long long)row * g.KXP + kx;
+        const T fky = (T)ky;
+        const cplx<T> G = v[0][r], H = v[1][r];
+        const cplx<T> tnd = cscale(mk<T>(G.x - fky * H.y, G.y + fky * H.x), inv_n2);   // G + i ky H
+        const cplx<T> x0 = stg[e];
+        const cplx<T> xo = eul ? x0 : stg[FE + e];
+        cplx<T> xn = mk<T>(0, 0), xf = eul ? xo : mk<T>(0, 0);
+        if (g.mask(kx, ky)) {
+          if (which == 0) {
+            const cplx<T> dqv = sp.use_dq ? stg[2 * FE + e] : mk<T>(0, 0);
+            const T e1 = tab[e], e2 = tab[FE + e];
+            if (eul) {
+              xn = cscale(cadd(csub(xo, cscale(tnd, dt)), cscale(dqv, dt)), e1);
+            } else {
+              xn = cadd(csub(cscale(xo, e2), cscale(cscale(tnd, dt2), e1)), cscale(cscale(dqv, dt2), e2));
+            }
+          } else {
+            const T e1w = tab[e], e2w = tab[FE + e];
+            const T ck = cdisp * (T)(kx * kx + ky * ky);
+            // nBR - 0.5 rBI + c kh2 AI ; nBI + 0.5 rBR - c kh2 AR
+            const cplx<T> a3 = stg[2 * FE + e];
+            const cplx<T> fr = which == 1 ? cadd(tnd, cscale(a3, ck)) : csub(tnd, cscale(a3, ck));
+            if (eul) {
+              xn = cscale(csub(xo, cscale(fr, dt)), e1w);
+            } else {
+              xn = csub(cscale(xo, e2w), cscale(cscale(fr, dt2), e1w));
+            }
+          }
+          // Robert-Asselin filter (main_waqg.f90:395-410)
+          if (!eul) xf = cadd(x0, cscale(cadd(csub(xo, cscale(x0, (T)2)), xn), gam));
+        }
+        X[m] = xn;
+        Xo[m] = xf;
+        if (which > 0) bnew[(which - 1) * FE + e] = xn;
+      }
+    };
+  };
+  stage(0);
+  col_fft<T, N, true, 2, CT, NT>(sm, tw, pro_planes(0), epi_update(0));
+  __syncthreads();
+  stage(1);
+  col_fft<T, N, true, 2, CT, NT>(sm, tw, pro_planes(2), epi_update(1));
+  __syncthreads();
+  stage(2);
+  col_fft<T, N, true, 2, CT, NT>(sm, tw, pro_planes(4), epi_update(2));
   if (!qw_prep) return;
-  __syncthreads();   // this CTA's writes of BR, BI are visible to it after the barrier
-  // y-inverse FFTs of BR, i ky BR, BI, i ky BI at n+1 (compute_qw, derivatives.f90:929-957)
-#pragma unroll 4
-  for (int e = tid; e < 2 * CT * N; e += NT) {
-    const int c = e % CT, j = (e / CT) % N, f = e / (CT * N);
-    const int kx = kx0 + c;
-    const int r = g.row_of_fft_index(j);
-    const bool in = kx <= g.K && r >= 0;
-    const cplx<T>* F = f == 0 ? st.BR : st.BI;
-    cp_async_c<T>(buf + (2 * f * CT + c) * LD + pad_idx(j), in ? F + zoff + (long long)r * g.KXP + kx : F, in);
-  }
-  cp_async_wait_all();
   __syncthreads();
-  for (int e = tid; e < 2 * CT * N; e += NT) {
-    const int c = e % CT, j = (e / CT) % N, f = e / (CT * N);
-    const int r = g.row_of_fft_index(j);
-    const T ky = r >= 0 ? (T)g.ky_of_row(r) : (T)0;
-    const int o = c * LD + pad_idx(j);
-    buf[(2 * f + 1) * CT * LD + o] = cscale(cmul_i(buf[2 * f * CT * LD + o]), ky);
-  }
+  // y-inverse FFTs of B and i ky B at n+1 (compute_qw, derivatives.f90:929-957)
+  auto pro_B = [&](int which) {
+    return [&, which](int c, int j, cplx<T> (&v)[2][R0]) {
+      const int kx = kx0 + c;
+      const cplx<T>* X = bnew + (which - 1) * FE;
+#pragma unroll
+      for (int r = 0; r < R0; ++r) {
+        int row; bool cj;
+        col_src(g, kx, j + r * NB0, row, cj);
+        const cplx<T> b = row >= 0 ? X[row * CT + c] : mk<T>(0, 0);
+        const T ky = row >= 0 ? (T)g.ky_of_row(row) : (T)0;
+        cplx<T> b0 = b, b1 = cscale(cmul_i(b), ky);
+        if (cj) { b0 = cconj(b0); b1 = cconj(b1); }
+        v[0][r] = b0; v[1][r] = b1;
+      }
+    };
+  };
+  auto epi_store = [&](int f0) {
+    return [&, f0](int c, int j, cplx<T> (&v)[2][RL]) {
+#pragma unroll
+      for (int f = 0; f < 2; ++f)
+#pragma unroll
+        for (int r = 0; r < RL; ++r) S[scr_off(zb, f0 + f, j + r * NSL, N, g.KXP) + kx0 + c] = v[f][r];
+    };
+  };
+  col_fft<T, N, false, 2, CT, NT>(sm, tw, pro_B(1), epi_store(0));
   __syncthreads();
-  if (kx0 == 0) {
-    for (int e = tid; e < 4 * (N / 2 - 1); e += NT) {
-      const int f = e / (N / 2 - 1), j = 1 + e % (N / 2 - 1);
-      cplx<T>* col = buf + f * CT * LD;
-      col[pad_idx(N - j)] = cconj(col[pad_idx(j)]);
-    }
-    __syncthreads();
-  }
-  fft_ip<T, N, false, 2 * CT, NT, LD>(buf, tw);
-  fft_ip<T, N, false, 2 * CT, NT, LD>(buf + 2 * CT * LD, tw);
-#pragma unroll 4
-  for (int e = tid; e < 4 * CT * N; e += NT) {
-    const int c = e % CT, y = (e / CT) % N, f = e / (CT * N);
-    S[scr_off(zb, f, y, N, g.KXP) + kx0 + c] = buf[(f * CT + c) * LD + pad_idx(y)];
-  }
+  col_fft<T, N, false, 2, CT, NT>(sm, tw, pro_B(2), epi_store(2));
 }
 
 // ===========================================================================
@@ -426,42 +497,47 @@ template <typename T, int N>
 __global__ void __launch_bounds__(kThreadsB)
 k_col_qw(Geom g, StepParams sp, int zbase, const cplx<T>* __restrict__ q, cplx<T>* __restrict__ qstar,
          const cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
-  constexpr int CT = Tiles<T, N>::CT, LD = Tiles<T, N>::LD, NT = kThreadsB;
+  constexpr int CT = Tiles<T, N>::CT, NT = kThreadsB;
+  constexpr int R0 = radix_of(N), NB0 = N / R0, NSL = LastNS<N>::value, RL = N / NSL;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* buf = tw + N;                 // [2][CT][LD]
-  const int tid = threadIdx.x;
+  cplx<T>* sm = tw + N;                 // [2][FS]
   const int zb = blockIdx.y, z = zbase + zb;
   const int kx0 = blockIdx.x * CT;
-  const int KY = g.KY;
   load_tw<T, N>(tw, twg, NT);
-#pragma unroll 4
-  for (int e = tid; e < 2 * CT * N; e += NT) {
-    const int c = e % CT, y = (e / CT) % N, h = e / (CT * N);
-    const int kx = kx0 + c;
-    cp_async_c<T>(buf + (h * CT + c) * LD + pad_idx(y), S + scr_off(zb, h, y, N, g.KXP) + kx, kx <= g.K);
-  }
-  cp_async_wait_all();
   __syncthreads();
-  fft_ip<T, N, true, 2 * CT, NT, LD>(buf, tw);
   const T inv_n2 = (T)1 / ((T)N * (T)N);
   const T s = (T)sp.Ro * (T)sp.W2F;
   const long long zoff = (long long)z * g.plane;
-  for (int e = tid; e < CT * KY; e += NT) {
-    const int c = e % CT, r = e / CT;
+  auto pro = [&](int c, int j, cplx<T> (&v)[2][R0]) {
     const int kx = kx0 + c;
-    if (kx > g.K) continue;
-    const int ky = g.ky_of_row(r);
-    const int j = pad_idx(g.fft_index_of_row(r));
-    const long long m = zoff + (long long)r * g.KXP + kx;
-    cplx<T> out = mk<T>(0, 0);
-    if (g.mask(kx, ky)) {
-      const cplx<T> R = csub(buf[c * LD + j], cscale(buf[(CT + c) * LD + j], (T)0.25 * (T)ky * (T)ky));
-      const cplx<T> qw = cscale(cscale(R, inv_n2), s);
-      out = csub(q[m], qw);       // q* = q - q^w (main_waqg.f90:430-439)
+#pragma unroll
+    for (int r = 0; r < R0; ++r) {
+      const int y = j + r * NB0;
+      const bool in = kx <= g.K;
+      v[0][r] = in ? S[scr_off(zb, 0, y, N, g.KXP) + kx] : mk<T>(0, 0);
+      v[1][r] = in ? S[scr_off(zb, 1, y, N, g.KXP) + kx] : mk<T>(0, 0);
     }
-    qstar[m] = out;
-  }
+  };
+  auto epi = [&](int c, int j, cplx<T> (&v)[2][RL]) {
+    const int kx = kx0 + c;
+    if (kx > g.K) return;
+#pragma unroll
+    for (int r = 0; r < RL; ++r) {
+      const int row = g.row_of_fft_index(j + r * NSL);
+      if (row < 0) continue;
+      const int ky = g.ky_of_row(row);
+      const long long m = zoff + (long long)row * g.KXP + kx;
+      cplx<T> out = mk<T>(0, 0);
+      if (g.mask(kx, ky)) {
+        const cplx<T> R = csub(v[0][r], cscale(v[1][r], (T)0.25 * (T)ky * (T)ky));
+        const cplx<T> qw = cscale(cscale(R, inv_n2), s);
+        out = csub(q[m], qw);       // q* = q - q^w (main_waqg.f90:430-439)
+      }
+      qstar[m] = out;
+    }
+  };
+  col_fft<T, N, true, 2, CT, NT>(sm, tw, pro, epi);
 }
 
 // q* = q where the feedback is off (no_feedback == 1)
