@@ -434,6 +434,7 @@ class Engine : public EngineBase {
   }
   template <int NN> static constexpr size_t sm_col6() { return (size_t)(NN + 6 * Tiles<T, NN>::CT * Tiles<T, NN>::LD) * sizeof(C); }
   template <int NN> static constexpr size_t sm_row7() { return (size_t)(NN + 7 * Tiles<T, NN>::RT * Tiles<T, NN>::LD) * sizeof(C); }
+  template <int NN> static constexpr size_t sm_row3() { return (size_t)(NN + 3 * Tiles<T, NN>::RT * Tiles<T, NN>::LD) * sizeof(C); }
   template <int NN> static constexpr size_t sm_row4() { return (size_t)(NN + 4 * Tiles<T, NN>::RT * Tiles<T, NN>::LD) * sizeof(C); }
   // shared memory of the dense (routine-level) kernels
   size_t sm_colinv() const { return (size_t)(g.n + 2 * Tile<T>::CT * (g.n + 1)) * sizeof(C); }
@@ -443,9 +444,9 @@ class Engine : public EngineBase {
     const int mx = cudaFuncAttributeMaxDynamicSharedMemorySize;
     QG_SWITCH_N(g.n, {
       QG_CK(cudaFuncSetAttribute(k_col_inv<T, NN>, (cudaFuncAttribute)mx, (int)sm_ci<NN>(3)));
-      QG_CK(cudaFuncSetAttribute(k_row_main<T, NN>, (cudaFuncAttribute)mx, (int)sm_row7<NN>()));
+      QG_CK(cudaFuncSetAttribute(k_row_main<T, NN>, (cudaFuncAttribute)mx, (int)sm_row4<NN>()));
       QG_CK(cudaFuncSetAttribute(k_col_update<T, NN>, (cudaFuncAttribute)mx, (int)UpdLay<T, NN>::bytes()));
-      QG_CK(cudaFuncSetAttribute(k_row_qw<T, NN>, (cudaFuncAttribute)mx, (int)sm_row4<NN>()));
+      QG_CK(cudaFuncSetAttribute(k_row_qw<T, NN>, (cudaFuncAttribute)mx, (int)sm_row3<NN>()));
       QG_CK(cudaFuncSetAttribute(k_col_qw<T, NN>, (cudaFuncAttribute)mx, (int)sm_ci<NN>(2)));
       // per-function attribute shared by every handle: set it for the deepest supported column
       QG_CK(cudaFuncSetAttribute(k_solve<T>, (cudaFuncAttribute)mx, (int)solve_smem(kMaxN3)));
@@ -527,7 +528,7 @@ class Engine : public EngineBase {
         QG_LAUNCHED();
         if (int rc0 = pend()) return rc0;
         if (int rc0 = pbeg(QG_K_ROW_MAIN)) return rc0;
-        k_row_main<T, NN><<<gr, kThreadsB, sm_row7<NN>(), st>>>(g, s, S, tw);
+        k_row_main<T, NN><<<gr, kThreadsB, sm_row4<NN>(), st>>>(g, s, S, tw);
         QG_LAUNCHED();
         if (int rc0 = pend()) return rc0;
         if (int rc0 = pbeg(QG_K_COL_UPDATE)) return rc0;
@@ -537,7 +538,7 @@ class Engine : public EngineBase {
         if (int rc0 = pend()) return rc0;
         if (need_qw) {
           if (int rc0 = pbeg(QG_K_ROW_QW)) return rc0;
-          k_row_qw<T, NN><<<gr, kThreadsB, sm_row4<NN>(), st>>>(g, S, tw);
+          k_row_qw<T, NN><<<gr, kThreadsB, sm_row3<NN>(), st>>>(g, S, tw);
           QG_LAUNCHED();
           if (int rc0 = pend()) return rc0;
           if (int rc0 = pbeg(QG_K_COL_QW)) return rc0;

@@ -39,6 +39,16 @@ __device__ __forceinline__ void realit_col(cplx<T>* col, int n) {
 
 // Tile shapes: CT columns per column-kernel CTA (6*CT transforms ~100 KB of
 // shared memory), RT rows per row-kernel CTA.
+// CTAs per SM the register budgets of the FP32 kernels target (FP64
+// kernels: at most 2); shared memory caps them further per shape
+constexpr int kRowMinB = 4;        // k_row_main, k_row_qw
+constexpr int kColInvMinB = 2;     // k_col_inv
+constexpr int kColQwMinB = 4;      // k_col_qw
+__host__ __device__ constexpr int smem_ctas(int bytes) {
+  return 233472 / (bytes + 1024) >= 4 ? 4 : (233472 / (bytes + 1024) >= 1 ? 233472 / (bytes + 1024) : 1);
+}
+__host__ __device__ constexpr int imin(int a, int b) { return a < b ? a : b; }
+
 template <typename T, int N> struct Tiles {
   static constexpr int CB = (int)sizeof(cplx<T>);
   static constexpr int ct0 = (16384 / CB) / N;
@@ -59,6 +69,10 @@ template <typename T, int N> struct Tiles {
   static constexpr int SM6 = (N + 6 * CT * LD) * CB;
   static constexpr int mb0 = 233472 / (SM6 + 1024);
   static constexpr int MINB = mb0 >= 4 ? 4 : (mb0 >= 1 ? mb0 : 1);
+  static constexpr int FSC = PadLD<N>::value * CT;   // interleaved column tile (colfft.cuh)
+  static constexpr int RMINB = imin(CB == 8 ? kRowMinB : 2, smem_ctas((N + 4 * RT * LD) * CB));
+  static constexpr int CIMINB = imin(CB == 8 ? kColInvMinB : 2, smem_ctas((N + 3 * FSC) * CB));
+  static constexpr int CQMINB = imin(CB == 8 ? kColQwMinB : 2, smem_ctas((N + 2 * FSC) * CB));
 };
 constexpr int kColThreads = 256;   // k_col_inv, k_col_update
 constexpr int kThreadsB = 256;     // row kernels, k_col_qw
@@ -98,7 +112,7 @@ __device__ __forceinline__ void col_src(const Geom& g, int kx, int idx, int& row
 }
 
 template <typename T, int N>
-__global__ void __launch_bounds__(kColThreads, Tiles<T, N>::MINB)
+__global__ void __launch_bounds__(kColThreads, Tiles<T, N>::CIMINB)
 k_col_inv(Geom g, int zbase, const cplx<T>* __restrict__ psi, const cplx<T>* __restrict__ q,
           const cplx<T>* __restrict__ BR, const cplx<T>* __restrict__ BI, cplx<T>* __restrict__ S,
           const cplx<T>* __restrict__ twg) {
@@ -183,13 +197,13 @@ __device__ __forceinline__ void unpack_pad(const cplx<T>* F, int k, int n, cplx<
 // Phase A, kernel 2: rows — physical products of convol_waqg / refraction_waqg
 // ===========================================================================
 template <typename T, int N>
-__global__ void __launch_bounds__(kThreadsB)
+__global__ void __launch_bounds__(kThreadsB, Tiles<T, N>::RMINB)
 k_row_main(Geom g, StepParams sp, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
   constexpr int RT = Tiles<T, N>::RT, LD = Tiles<T, N>::LD, NT = kThreadsB;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* bA = tw + N;                 // [RT][3][LD]: (u,v), (zeta,q), (br,bi)
-  cplx<T>* bC = bA + 3 * RT * LD;       // [RT][4][LD]: products
+  // [4][RT][LD]: (u,v), (zeta,q), (br,bi); then, in place, the 4 products
+  cplx<T>* bA = tw + N;
   const int tid = threadIdx.x;
   const int zb = blockIdx.y;
   const int y0 = blockIdx.x * RT;
@@ -201,7 +215,7 @@ k_row_main(Geom g, StepParams sp, cplx<T>* __restrict__ S, const cplx<T>* __rest
     const int y = y0 + rr;
     const cplx<T>* X = S + scr_off(zb, 2 * p, y, N, g.KXP);
     const cplx<T>* Y = S + scr_off(zb, 2 * p + 1, y, N, g.KXP);
-    bA[(rr * 3 + p) * LD + pad_idx(k)] = pack_spec<T>(X, Y, k, N, K);
+    bA[(p * RT + rr) * LD + pad_idx(k)] = pack_spec<T>(X, Y, k, N, K);
   }
   __syncthreads();
   fft_ip<T, N, false, 3 * RT, NT, LD>(bA, tw);
@@ -210,26 +224,26 @@ k_row_main(Geom g, StepParams sp, cplx<T>* __restrict__ S, const cplx<T>* __rest
   for (int e = tid; e < RT * N; e += NT) {
     const int x = e % N, rr = e / N;
     const int px = pad_idx(x);
-    const cplx<T> uv = bA[(rr * 3 + 0) * LD + px];
-    const cplx<T> zq = bA[(rr * 3 + 1) * LD + px];
-    const cplx<T> bb = bA[(rr * 3 + 2) * LD + px];
-    bC[(rr * 4 + 0) * LD + px] = mk<T>(uv.x * zq.y, uv.y * zq.y);
-    bC[(rr * 4 + 1) * LD + px] = mk<T>(uv.x * bb.x, uv.y * bb.x);
-    bC[(rr * 4 + 2) * LD + px] = mk<T>(uv.x * bb.y, uv.y * bb.y);
-    bC[(rr * 4 + 3) * LD + px] = mk<T>(zq.x * bb.x, zq.x * bb.y);
+    const cplx<T> uv = bA[(0 * RT + rr) * LD + px];
+    const cplx<T> zq = bA[(1 * RT + rr) * LD + px];
+    const cplx<T> bb = bA[(2 * RT + rr) * LD + px];
+    bA[(0 * RT + rr) * LD + px] = mk<T>(uv.x * zq.y, uv.y * zq.y);
+    bA[(1 * RT + rr) * LD + px] = mk<T>(uv.x * bb.x, uv.y * bb.x);
+    bA[(2 * RT + rr) * LD + px] = mk<T>(uv.x * bb.y, uv.y * bb.y);
+    bA[(3 * RT + rr) * LD + px] = mk<T>(zq.x * bb.x, zq.x * bb.y);
   }
   __syncthreads();
-  fft_ip<T, N, true, 4 * RT, NT, LD>(bC, tw);
+  fft_ip<T, N, true, 4 * RT, NT, LD>(bA, tw);
   const T adv = sp.adv ? (T)1 : (T)0;
   const T half = sp.refr ? (T)0.5 : (T)0;
   for (int e = tid; e < RT * (K + 1); e += NT) {
     const int k = e % (K + 1), rr = e / (K + 1);
     const int y = y0 + rr;
     cplx<T> uq, vq, ubr, vbr, ubi, vbi, zbr, zbi;
-    unpack_pad<T>(bC + (rr * 4 + 0) * LD, k, N, uq, vq);
-    unpack_pad<T>(bC + (rr * 4 + 1) * LD, k, N, ubr, vbr);
-    unpack_pad<T>(bC + (rr * 4 + 2) * LD, k, N, ubi, vbi);
-    unpack_pad<T>(bC + (rr * 4 + 3) * LD, k, N, zbr, zbi);
+    unpack_pad<T>(bA + (0 * RT + rr) * LD, k, N, uq, vq);
+    unpack_pad<T>(bA + (1 * RT + rr) * LD, k, N, ubr, vbr);
+    unpack_pad<T>(bA + (2 * RT + rr) * LD, k, N, ubi, vbi);
+    unpack_pad<T>(bA + (3 * RT + rr) * LD, k, N, zbr, zbi);
     const T kx = (T)k;
     // G = i kx F(uX) (+- refraction), H = F(vX); tendency = F_y(G) + i ky F_y(H)
     S[scr_off(zb, 0, y, N, g.KXP) + k] = cscale(cmul_i(uq), kx * adv);
@@ -429,13 +443,12 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
 // Phase A, kernel 4: rows — products of compute_qw
 // ===========================================================================
 template <typename T, int N>
-__global__ void __launch_bounds__(kThreadsB)
+__global__ void __launch_bounds__(kThreadsB, Tiles<T, N>::RMINB)
 k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
   constexpr int RT = Tiles<T, N>::RT, LD = Tiles<T, N>::LD, NT = kThreadsB;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* bA = tw + N;               // [RT][3][LD]
-  cplx<T>* bC = bA + 3 * RT * LD;     // [RT][LD]
+  cplx<T>* bA = tw + N;               // [3][RT][LD]; then, in place, (P1, P2) in the first RT
   const int tid = threadIdx.x;
   const int zb = blockIdx.y;
   const int y0 = blockIdx.x * RT;
@@ -462,7 +475,7 @@ k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
       const cplx<T> a = cscale(cmul_i(sBR[kk]), (T)kk), b = cscale(cmul_i(sBI[kk]), (T)kk);
       v = k <= K ? mk<T>(a.x - b.y, a.y + b.x) : mk<T>(a.x + b.y, b.x - a.y);
     }
-    bA[(rr * 3 + p) * LD + pad_idx(k)] = v;
+    bA[(p * RT + rr) * LD + pad_idx(k)] = v;
   }
   __syncthreads();
   fft_ip<T, N, false, 3 * RT, NT, LD>(bA, tw);
@@ -470,20 +483,20 @@ k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
   for (int e = tid; e < RT * N; e += NT) {
     const int x = e % N, rr = e / N;
     const int px = pad_idx(x);
-    const cplx<T> b = bA[(rr * 3 + 0) * LD + px];    // (br, bi)
-    const cplx<T> bx = bA[(rr * 3 + 1) * LD + px];   // (brx, bix)
-    const cplx<T> by = bA[(rr * 3 + 2) * LD + px];   // (bry, biy)
+    const cplx<T> b = bA[(0 * RT + rr) * LD + px];    // (br, bi)
+    const cplx<T> bx = bA[(1 * RT + rr) * LD + px];   // (brx, bix)
+    const cplx<T> by = bA[(2 * RT + rr) * LD + px];   // (bry, biy)
     const T p1 = by.x * bx.y - bx.x * by.y;           // BRy BIx - BRx BIy (derivatives.f90:973)
     const T p2 = b.x * b.x + b.y * b.y;               // BR^2 + BI^2     (derivatives.f90:996)
-    bC[rr * LD + px] = mk<T>(p1, p2);
+    bA[rr * LD + px] = mk<T>(p1, p2);
   }
   __syncthreads();
-  fft_ip<T, N, true, RT, NT, LD>(bC, tw);
+  fft_ip<T, N, true, RT, NT, LD>(bA, tw);
   for (int e = tid; e < RT * (K + 1); e += NT) {
     const int k = e % (K + 1), rr = e / (K + 1);
     const int y = y0 + rr;
     cplx<T> P1, P2;
-    unpack_pad<T>(bC + rr * LD, k, N, P1, P2);
+    unpack_pad<T>(bA + rr * LD, k, N, P1, P2);
     const T qk = (T)0.25 * (T)(k * k);
     S[scr_off(zb, 0, y, N, g.KXP) + k] = csub(P1, cscale(P2, qk));
     S[scr_off(zb, 1, y, N, g.KXP) + k] = P2;
@@ -494,7 +507,7 @@ k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
 // Phase A, kernel 5: y-forward FFTs of the q^w planes, q* = q - q^w
 // ===========================================================================
 template <typename T, int N>
-__global__ void __launch_bounds__(kThreadsB)
+__global__ void __launch_bounds__(kThreadsB, Tiles<T, N>::CQMINB)
 k_col_qw(Geom g, StepParams sp, int zbase, const cplx<T>* __restrict__ q, cplx<T>* __restrict__ qstar,
          const cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
   constexpr int CT = Tiles<T, N>::CT, NT = kThreadsB;
