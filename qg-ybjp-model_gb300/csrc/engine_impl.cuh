@@ -87,7 +87,7 @@ class Engine : public EngineBase {
       return QG_OK;
     };
     if ((rc = upd(&du, t.du)) || (rc = upd(&cu, t.cu)) || (rc = upd(&cl, t.cl)) || (rc = upd(&r2, t.r2))) return rc;
-    QG_CK(cudaMalloc(&diag_part, (size_t)g.n3 * kNDiag * sizeof(double)));
+    QG_CK(cudaMalloc(&diag_part, (size_t)g.n3 * kDiagChunks * kNDiag * sizeof(double)));
     QG_CK(cudaMalloc(&diag_out, kNDiag * sizeof(double)));
     QG_CK(cudaMallocHost(&diag_host, kNDiag * sizeof(double)));
     // phase-A batching: keep the scratch planes of one batch L2-sized
@@ -222,9 +222,9 @@ class Engine : public EngineBase {
   }
 
   int diagnostics(qg_energy* out) override {
-    k_diag_level<T><<<g.n3, 256, 0, st>>>(g, cfg.dz, cfg.Bu, r2, F[F_BR], F[F_BI], F[F_AR], F[F_AI], F[F_PSI], diag_part);
+    k_diag_level<T><<<dim3(kDiagChunks, g.n3), 256, 0, st>>>(g, cfg.dz, cfg.Bu, r2, F[F_BR], F[F_BI], F[F_AR], F[F_AI], F[F_PSI], diag_part);
     QG_LAUNCHED();
-    k_diag_sum<<<1, 32, 0, st>>>(g.n3, diag_part, diag_out);
+    k_diag_sum<<<1, 32 * kNDiag, 0, st>>>(g.n3, diag_part, diag_out);
     QG_LAUNCHED();
     QG_CK(cudaMemcpyAsync(diag_host, diag_out, kNDiag * sizeof(double), cudaMemcpyDeviceToHost, st));
     QG_CK(cudaStreamSynchronize(st));

@@ -845,43 +845,61 @@ __global__ void k_init_q(Geom g, double dz, const double* __restrict__ cu, const
 // FP64 diagnostics: per-level partial sums, then a fixed-order vertical sum
 // ===========================================================================
 constexpr int kNDiag = 7;
+constexpr int kDiagChunks = 32;    // CTAs per level: the level's modes in 32 contiguous ranges
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_diag_level(Geom g, double dz, double Bu, const double* __restrict__ r2, const cplx<T>* __restrict__ BR,
              const cplx<T>* __restrict__ BI, const cplx<T>* __restrict__ AR, const cplx<T>* __restrict__ AI,
              const cplx<T>* __restrict__ psi, double* __restrict__ part) {
   __shared__ double red[kNDiag][256];
-  const int z = blockIdx.x;
+  const int z = blockIdx.y, chunk = blockIdx.x;
   const long long zo = (long long)z * g.plane;
+  const long long per = (g.plane + kDiagChunks - 1) / kDiagChunks;
+  const long long m0 = chunk * per, m1 = m0 + per < g.plane ? m0 + per : g.plane;
   const bool top = (z == g.n3 - 1);
   const double rz = r2[z];
   double acc[kNDiag] = {0, 0, 0, 0, 0, 0, 0};
-  for (long long m = threadIdx.x; m < g.plane; m += blockDim.x) {
-    const int r = (int)(m / g.KXP), kx = (int)(m % g.KXP);
+  for (long long m = m0 + threadIdx.x; m < m1; m += blockDim.x) {
+    const int mi = (int)m, r = mi / g.KXP, kx = mi - r * g.KXP;
     const int ky = g.ky_of_row(r);
     if (!g.mask(kx, ky)) continue;
-    const double kh2 = (double)(kx * kx + ky * ky);
+    // exact int -> double without a conversion instruction: (2^52 + k) - 2^52
+    const double kh2 = __hiloint2double(0x43300000, kx * kx + ky * ky) - 4503599627370496.0;
     const double w00 = (kx == 0 && ky == 0) ? 0.5 : 1.0;
-    const cplx<T> br = BR[zo + m], bi = BI[zo + m], ar = AR[zo + m], ai = AI[zo + m], p = psi[zo + m];
-    const double b2 = (double)br.x * br.x + (double)br.y * br.y + (double)bi.x * bi.x + (double)bi.y * bi.y;
+    // widen once per value (exact; FP32 inputs convert with integer operations)
+    const cplx<T> brc = BR[zo + m], bic = BI[zo + m], arc = AR[zo + m], aic = AI[zo + m], pc = psi[zo + m];
+    const double brx = to64<T>(brc.x), bry = to64<T>(brc.y), bix = to64<T>(bic.x), biy = to64<T>(bic.y);
+    const double arx = to64<T>(arc.x), ary = to64<T>(arc.y), aix = to64<T>(aic.x), aiy = to64<T>(aic.y);
+    const double px = to64<T>(pc.x), py = to64<T>(pc.y);
+    const double b2 = brx * brx + bry * bry + bix * bix + biy * biy;
     acc[0] += w00 * b2;
     double c2 = 0.0, pz2 = 0.0;
     if (!top) {
+      // C = A_z and b ~ psi_z: differences (f(z+1) - f(z)), scaled by 1/dz^2 below
       const cplx<T> ar1 = AR[zo + g.plane + m], ai1 = AI[zo + g.plane + m], p1 = psi[zo + g.plane + m];
-      const double crx = ((double)ar1.x - ar.x) / dz, cry = ((double)ar1.y - ar.y) / dz;
-      const double cix = ((double)ai1.x - ai.x) / dz, ciy = ((double)ai1.y - ai.y) / dz;
+      const double crx = to64<T>(ar1.x) - arx, cry = to64<T>(ar1.y) - ary;
+      const double cix = to64<T>(ai1.x) - aix, ciy = to64<T>(ai1.y) - aiy;
       c2 = crx * crx + cry * cry + cix * cix + ciy * ciy;
-      const double bx = ((double)p1.x - p.x) / dz, by = ((double)p1.y - p.y) / dz;
+      const double bx = to64<T>(p1.x) - px, by = to64<T>(p1.y) - py;
       pz2 = bx * bx + by * by;
     }
-    acc[1] += (0.5 / (rz * Bu)) * kh2 * c2;
-    const double a2 = (double)ar.x * ar.x + (double)ar.y * ar.y + (double)ai.x * ai.x + (double)ai.y * ai.y;
-    acc[2] += (1.0 / 8.0) * (1.0 / (Bu * Bu)) * kh2 * kh2 * a2;
-    const double ps2 = (double)p.x * p.x + (double)p.y * p.y;
-    acc[3] += kh2 * ps2;
-    acc[4] += w00 * (Bu / rz) * pz2;
-    acc[5] += 2.0 * kh2 * kh2 * ps2;
-    acc[6] += 2.0 * kh2 * pz2;
+    acc[1] += kh2 * c2;
+    const double a2 = arx * arx + ary * ary + aix * aix + aiy * aiy;
+    acc[2] += (kh2 * kh2) * a2;
+    const double t = kh2 * (px * px + py * py);
+    acc[3] += t;
+    acc[4] += w00 * pz2;
+    acc[5] += kh2 * t;
+    acc[6] += kh2 * pz2;
+  }
+  // constant factors of each sum (per level)
+  {
+    const double inv_dz2 = 1.0 / (dz * dz);
+    acc[1] *= (0.5 / (rz * Bu)) * inv_dz2;
+    acc[2] *= (1.0 / 8.0) * (1.0 / (Bu * Bu));
+    acc[4] *= (Bu / rz) * inv_dz2;
+    acc[5] *= 2.0;
+    acc[6] *= 2.0 * inv_dz2;
   }
   for (int k = 0; k < kNDiag; ++k) red[k][threadIdx.x] = acc[k];
   __syncthreads();
@@ -890,15 +908,22 @@ k_diag_level(Geom g, double dz, double Bu, const double* __restrict__ r2, const 
       for (int k = 0; k < kNDiag; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + s];
     __syncthreads();
   }
-  if (threadIdx.x < kNDiag) part[z * kNDiag + threadIdx.x] = red[threadIdx.x][0];
+  if (threadIdx.x < kNDiag) part[((long long)z * kDiagChunks + chunk) * kNDiag + threadIdx.x] = red[threadIdx.x][0];
 }
 
+// one warp per quantity: lane l sums levels l, l+32, ... (each level's
+// chunks in order), then a fixed butterfly over the lanes; mean over levels
 static __global__ void k_diag_sum(int n3, const double* __restrict__ part, double* __restrict__ out) {
-  if (threadIdx.x < kNDiag) {
-    double s = 0.0;
-    for (int z = 0; z < n3; ++z) s += part[z * kNDiag + threadIdx.x];
-    out[threadIdx.x] = s / n3;
+  const int k = threadIdx.x / 32, lane = threadIdx.x % 32;
+  if (k >= kNDiag) return;
+  double s = 0.0;
+  for (int z = lane; z < n3; z += 32) {
+    double lv = 0.0;
+    for (int c = 0; c < kDiagChunks; ++c) lv += part[((long long)z * kDiagChunks + c) * kNDiag + k];
+    s += lv;
   }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) out[k] = s / n3;
 }
 
 }  // namespace qg
