@@ -174,6 +174,18 @@ int qg_refraction_waqg(qg_handle* h, const double* BRk, const double* BIk, const
                        double* rBRk, double* rBIk, int nz);
 /* derivatives.f90:906-1032 */
 int qg_compute_qw(qg_handle* h, const double* BRk, const double* BIk, double* qwk, int nz);
+/* Output path: the real-space FP32 fields of the netCDF dumps, interior
+ * levels level0 .. level0+nlev-1, layout out[z][y][x] (x fastest, the
+ * Fortran psi_clean(n1,n2,n3h0) / BR_clean order).
+ * qg_dump_psi replaces IO_ncf.f90:35-58 (ncdump_psi): out = real(psi * U_scale * L_scale),
+ * the product taken left to right in FP64 and rounded to FP32.
+ * qg_dump_la replaces IO_ncf.f90:137-146 (ncdump_la): out = real(B * Uw_scale) for the
+ * real and imaginary parts of B; with la != 0 the YBJ+ conversion
+ * LA = B + 0.25*kh2*A/Bu on the retained modes is applied first
+ * (diagnostics.f90:1698-1727).  Pass the scales as the host holds them
+ * (the reference's Uw_scale = 2.5e-5 is a single-precision literal). */
+int qg_dump_psi(qg_handle* h, float* out, int level0, int nlev, double U_scale, double L_scale);
+int qg_dump_la(qg_handle* h, float* outR, float* outI, int level0, int nlev, double Uw_scale, int la);
 /* elliptic.f90:145-247: all n3 levels, z-major layout (no transpose). */
 int qg_psi_solver(qg_handle* h, const double* qstar, double* psik);
 /* elliptic.f90:346-460: all n3 levels; ck may be NULL. */

@@ -453,6 +453,26 @@ class Model:
             s = self.step(s, first and i == 0)
         return s
 
+    # -- output path: real-space FP32 fields of the netCDF dumps -------------
+    def dump_psi(self, psik: np.ndarray, U_scale: float, L_scale: float) -> np.ndarray:
+        """ncdump_psi (IO_ncf.f90:35-58): c2r of psi, times U_scale*L_scale
+        (left to right in FP64), rounded to FP32; [nz][n2][n1], x fastest."""
+        r = self.fft_c2r(psik)
+        return ((r * U_scale) * L_scale).astype(np.float32)
+
+    def la_from_b(self, Bk: np.ndarray, Ak: np.ndarray) -> np.ndarray:
+        """YBJ+ B -> LA on the retained modes (diagnostics.f90:1698-1727):
+        LA = B + 0.25*kh2*A/Bu, evaluated left to right; zero where L=0."""
+        return np.where(self.Lb, Bk + ((0.25 * self.kh2f) * Ak) / self.p.Bu, 0)
+
+    def dump_la(self, BRk, BIk, ARk, AIk, Uw_scale: float, la: bool):
+        """ncdump_la (IO_ncf.f90:137-158): c2r of BR and BI (or of LA when
+        `la`), times Uw_scale, rounded to FP32; [nz][n2][n1] each."""
+        if la:
+            BRk, BIk = self.la_from_b(BRk, ARk), self.la_from_b(BIk, AIk)
+        return ((self.fft_c2r(BRk) * Uw_scale).astype(np.float32),
+                (self.fft_c2r(BIk) * Uw_scale).astype(np.float32))
+
     # -- FP64 diagnostics (diagnostics.f90) ---------------------------------
     def diagnostics(self, s: "State") -> dict:
         """Domain-integrated energies and enstrophy.

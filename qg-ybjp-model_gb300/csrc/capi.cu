@@ -367,6 +367,16 @@ int qg_compute_qw(qg_handle* h, const double* BRk, const double* BIk, double* qw
   if (!BRk || !BIk || !qwk) return fail(h, QG_ERR_ARG, "null pointer");
   return fwd(h, h->eng->compute_qw(BRk, BIk, qwk, nz));
 }
+int qg_dump_psi(qg_handle* h, float* out, int level0, int nlev, double U_scale, double L_scale) {
+  QG_ENTRY(h);
+  if (!out) return fail(h, QG_ERR_ARG, "qg_dump_psi: null pointer");
+  return fwd(h, h->eng->dump_real(0, out, nullptr, level0, nlev, U_scale, L_scale));
+}
+int qg_dump_la(qg_handle* h, float* outR, float* outI, int level0, int nlev, double Uw_scale, int la) {
+  QG_ENTRY(h);
+  if (!outR || !outI) return fail(h, QG_ERR_ARG, "qg_dump_la: null pointer");
+  return fwd(h, h->eng->dump_real(la ? 2 : 1, outR, outI, level0, nlev, Uw_scale, 1.0));
+}
 int qg_psi_solver(qg_handle* h, const double* qstar, double* psik) {
   QG_ENTRY(h);
   if (!qstar || !psik) return fail(h, QG_ERR_ARG, "null pointer");

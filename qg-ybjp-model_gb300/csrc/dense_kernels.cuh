@@ -229,4 +229,28 @@ __global__ void k_phys_pad(int n, long long tot, const T* __restrict__ in, doubl
   }
 }
 
+// Output path (netCDF dumps).  YBJ+ B -> LA on the retained modes
+// (diagnostics.f90:1698-1727): LA = B + 0.25*kh2*A/Bu, left to right; 0 elsewhere.
+static __global__ void k_dense_la(int n, int kmax2, long long tot, const double2* __restrict__ B,
+                                  const double2* __restrict__ A, double Bu, double2* __restrict__ out) {
+  for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < tot; m += (long long)gridDim.x * blockDim.x) {
+    int kx, ky, iky; dense_mode(m, n, kx, ky, iky);
+    double2 v = make_double2(0.0, 0.0);
+    if (dense_L(kx, ky, iky, n, kmax2)) {
+      const double c = 0.25 * (double)(kx * kx + ky * ky);
+      const double2 b = B[m], a = A[m];
+      v = make_double2(b.x + (c * a.x) / Bu, b.y + (c * a.y) / Bu);
+    }
+    out[m] = v;
+  }
+}
+
+// dimensional FP32 copy of a physical field: out = float((x * s1) * s2)
+// (IO_ncf.f90:47-52, 139-146: real(field*scale))
+template <typename T>
+__global__ void k_phys_f32(long long tot, const T* __restrict__ in, double s1, double s2, float* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x)
+    out[i] = (float)(((double)in[i] * s1) * s2);
+}
+
 }  // namespace qg

@@ -52,6 +52,8 @@ struct EngineBase {
     err = "the adjoint needs an FP64 handle";
     return QG_ERR_UNSUPPORTED;
   }
+  // real-space FP32 output of the dumps: which = 0 psi (out0), 1 B, 2 LA (out0 = R, out1 = I)
+  virtual int dump_real(int which, float* out0, float* out1, int level0, int nlev, double s1, double s2) = 0;
   virtual int fft_r2c(const double* rvar, double* kvar, int nz) = 0;
   virtual int fft_c2r(const double* kvar, double* rvar, int nz) = 0;
   virtual int convol_waqg(const double* uk, const double* vk, const double* qk, const double* BRk, const double* BIk,

@@ -233,6 +233,36 @@ class Engine : public EngineBase {
     return QG_OK;
   }
 
+  // ---- output path ----------------------------------------------------------
+  int dump_real(int which, float* out0, float* out1, int level0, int nlev, double s1, double s2) override {
+    if (level0 < 0 || nlev <= 0 || level0 + nlev > g.n3) { err = "bad level range"; return QG_ERR_ARG; }
+    int rc = prep_dense(nlev);
+    if (rc) return rc;
+    const long long tot = (long long)nlev * g.n * (g.n / 2 + 1), np = (long long)nlev * g.n * g.n;
+    float* o32 = reinterpret_cast<float*>(dstage);        // nlev*n*(n+2) doubles hold nlev*n*n floats
+    const int nf = which == 0 ? 1 : 2;
+    for (int c = 0; c < nf; ++c) {
+      const C* src = which == 0 ? F[F_PSI] : (c == 0 ? F[F_BR] : F[F_BI]);
+      k_compact_to_dense<T><<<grid_for(tot), 256, 0, st>>>(g, level0, nlev, src, D[0], 0, cfg.dz);
+      QG_LAUNCHED();
+      const double2* spec = D[0];
+      if (which == 2) {
+        k_compact_to_dense<T><<<grid_for(tot), 256, 0, st>>>(g, level0, nlev, c == 0 ? F[F_AR] : F[F_AI], D[1], 0,
+                                                            cfg.dz);
+        QG_LAUNCHED();
+        k_dense_la<<<grid_for(tot), 256, 0, st>>>(g.n, g.kmax2, tot, D[0], D[1], cfg.Bu, D[2]);
+        QG_LAUNCHED();
+        spec = D[2];
+      }
+      if ((rc = d_c2r(spec, P[0], nlev))) return rc;
+      k_phys_f32<T><<<grid_for(np), 256, 0, st>>>(np, P[0], s1, s2, o32);
+      QG_LAUNCHED();
+      QG_CK(cudaMemcpyAsync(c == 0 ? out0 : out1, o32, (size_t)np * sizeof(float), cudaMemcpyDefault, st));
+      QG_CK(cudaStreamSynchronize(st));
+    }
+    return QG_OK;
+  }
+
   // ---- routine-level drop-ins ---------------------------------------------
   int fft_r2c(const double* rvar, double* kvar, int nz) override {
     int rc = prep_dense(nz);

@@ -26,7 +26,7 @@ EXPORTS = (
     "qg_A_solver_ybj_plus", "qg_profile_step", "qg_fft_c2r_noalloc",
     "qg_ensemble_create", "qg_ensemble_member", "qg_ensemble_step", "qg_ensemble_synchronize",
     "qg_ensemble_get_stream", "qg_ensemble_destroy", "qg_ensemble_last_error", "qg_autotune",
-    "qg_adjoint_run", "qg_adjoint_step",
+    "qg_adjoint_run", "qg_adjoint_step", "qg_dump_psi", "qg_dump_la",
 )
 KERNEL_CLASSES = ("dissipation", "col_inv", "row_main", "col_update", "row_qw", "col_qw", "solve")
 
@@ -100,6 +100,8 @@ def lib() -> C.CDLL:
         "qg_autotune": (ip, [C.POINTER(QgConfig), ip, C.POINTER(QgTuning)]),
         "qg_adjoint_run": (ip, [vp, vp, vp, vp, ip, ip, ip, dp, vp, vp, vp]),
         "qg_adjoint_step": (ip, [vp, ip, vp, vp, vp, vp]),
+        "qg_dump_psi": (ip, [vp, vp, ip, ip, C.c_double, C.c_double]),
+        "qg_dump_la": (ip, [vp, vp, vp, ip, ip, C.c_double, ip]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -196,6 +196,33 @@ class Simulation:
         self._ck(lib().qg_A_solver_ybj_plus(self.h, ptr(b), ptr(a), ptr(c)))
         return a, c
 
+    # -- output path (the netCDF dumps' real-space FP32 fields) ----------------------
+    def dump_psi(self, U_scale: float, L_scale: float, level0: int = 0, nlev: int | None = None):
+        """psi in physical space, dimensional, float32 [nz][n][n] (ncdump_psi)."""
+        nlev = self.n3 - level0 if nlev is None else nlev
+        out = np.empty((nlev, self.n, self.n), dtype=np.float32)
+        self._ck(lib().qg_dump_psi(self.h, ptr(out), level0, nlev, float(U_scale), float(L_scale)))
+        return out
+
+    def dump_la(self, Uw_scale: float, la: bool = False, level0: int = 0, nlev: int | None = None):
+        """Real and imaginary wave fields in physical space, float32 (ncdump_la:
+        B; with la=True the YBJ+ LA = B + kh^2 A/(4 Bu))."""
+        nlev = self.n3 - level0 if nlev is None else nlev
+        outR = np.empty((nlev, self.n, self.n), dtype=np.float32)
+        outI = np.empty_like(outR)
+        self._ck(lib().qg_dump_la(self.h, ptr(outR), ptr(outI), level0, nlev, float(Uw_scale), int(la)))
+        return outR, outI
+
+    def write_dumps(self, directory, count: int, time: float, U_scale: float, L_scale: float, Uw_scale: float):
+        """psiNNN and laNNN dumps as ncdump_psi / ncdump_la write them (raw
+        binary + JSON sidecar, qgybj.io); returns the two .bin paths."""
+        from .io import dump_time_seconds, write_dump
+        ts = dump_time_seconds(time, L_scale, U_scale)
+        p1 = write_dump(directory, "psi", count, {"psi": self.dump_psi(U_scale, L_scale)}, ts)
+        lr, li = self.dump_la(Uw_scale)
+        p2 = write_dump(directory, "la", count, {"LAr": lr, "LAi": li}, ts)
+        return p1, p2
+
     # -- adjoint (FP64 handles) ------------------------------------------------------
     def adjoint_run(self, q0, BR0, BI0, nsteps: int, ckpt_every: int = 10, gradient: bool = True):
         """J = 1/2 sum over the central quarter and top fifth of |LA|^2 after

@@ -219,6 +219,44 @@ def _params(n=32, n3=8):
     return model_parameters(rc, ic.delt)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_output_dumps(precision, tmp_path):
+    """qg_dump_psi / qg_dump_la (ncdump_psi, ncdump_la; LA conversion of the
+    slice diagnostics) against the oracle applied to the handle's own
+    spectral state: float32 outputs, rel. L2 <= 1e-7 (FP64) / 2e-6 (mixed)."""
+    from qgybj.io import read_dump
+    rc = scaled(CONFIGS["c0"], 32, 8)
+    model, st, sim = pair(rc, precision)
+    sim.step(True)
+    for _ in range(3):
+        sim.step()
+    tol = 1e-7 if precision == "fp64" else 2e-6
+    U, L, Uw = 0.25, float(np.float32(6.28318530718 * 5e4)) / (2 * np.pi), float(np.float32(2.5e-5))
+    psi, BR, BI = sim.get_state("psi"), sim.get_state("BR"), sim.get_state("BI")
+    AR, AI = sim.get_state("AR"), sim.get_state("AI")
+    got = sim.dump_psi(U, L)
+    assert got.dtype == np.float32 and got.shape == (8, 32, 32)
+    assert rel_l2(got.astype(np.float64), model.dump_psi(psi, U, L).astype(np.float64)) <= tol
+    for la in (False, True):
+        gr, gi = sim.dump_la(Uw, la)
+        er, ei = model.dump_la(BR, BI, AR, AI, Uw, la)
+        assert rel_l2(gr.astype(np.float64), er.astype(np.float64)) <= tol
+        assert rel_l2(gi.astype(np.float64), ei.astype(np.float64)) <= tol
+    # a level sub-range is the same slice of the full dump
+    part = sim.dump_psi(U, L, level0=2, nlev=3)
+    assert np.array_equal(part, got[2:5])
+    # files
+    p1, p2 = sim.write_dumps(tmp_path, 0, 1.5, U, L, Uw)
+    d, t = read_dump(p1)
+    assert np.array_equal(d["psi"], got) and t == float(np.float32(1.5 * L / U))
+    d, _ = read_dump(p2)
+    assert np.array_equal(d["LAr"], sim.dump_la(Uw)[0])
+    with pytest.raises(QgError) as e:
+        sim.dump_psi(U, L, level0=6, nlev=3)
+    assert e.value.status == QG_ERR_ARG
+    sim.close()
+
+
 def test_error_statuses():
     p = _params()
     with pytest.raises(QgError) as e:

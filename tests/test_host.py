@@ -104,3 +104,20 @@ def test_ensemble_members():
     assert sizes.count((64, 32)) == 24 and sizes.count((128, 64)) == 24 and sizes.count((256, 128)) == 16
     assert all(0.05 <= r.Ro <= 0.2 and 0.05 <= r.wave_depth <= 0.2 for r in m)
     assert len({r.seed for r in m}) == 64
+
+
+def test_dump_files_round_trip(tmp_path):
+    """qgybj.io writes psiNNN/laNNN dumps as float32 [z][y][x] plus a JSON
+    sidecar (names and time as the netCDF files carry them) and reads them back."""
+    from qgybj.io import dump_time_seconds, read_dump, write_dump
+    rng = np.random.default_rng(3)
+    a, b = rng.standard_normal((4, 8, 8)).astype(np.float32), rng.standard_normal((4, 8, 8)).astype(np.float32)
+    ts = dump_time_seconds(12.5, 5e4, 0.25)
+    assert ts == float(np.float32(12.5 * 5e4 / 0.25))
+    p = write_dump(tmp_path, "la", 7, {"LAr": a, "LAi": b}, ts)
+    assert p.name == "la007.out.bin"
+    got, t = read_dump(p)
+    assert t == ts and list(got) == ["LAr", "LAi"]
+    assert np.array_equal(got["LAr"], a) and np.array_equal(got["LAi"], b)
+    with pytest.raises(ValueError):
+        write_dump(tmp_path, "x", 0, {"a": a, "b": b[:2]}, ts)

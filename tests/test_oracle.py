@@ -274,3 +274,36 @@ def test_diagnostics_wave_energy_of_uniform_wave():
     prof = ic.BR[:, 0, 0].real
     assert abs(d["wke"] - 0.5 * np.mean(prof ** 2)) < 1e-14
     assert d["ke"] > 0 and d["zeta2"] > 0
+
+
+# --- output path (netCDF dumps) --------------------------------------------------
+def test_dump_single_mode_layout_and_scaling():
+    """A single (kx=1, ky=0) mode dumps as 2 Re(a e^{ix}) times the scales,
+    varying along the last (x) axis, in float32 (IO_ncf.f90:47-52)."""
+    m, s, ic, p = small_model(16, 2)
+    n = 16
+    k = np.zeros((2, n, n // 2 + 1), dtype=complex)
+    k[:, 0, 1] = 0.5 - 0.25j
+    U, L = 0.25, 5e4
+    out = m.dump_psi(k, U, L)
+    assert out.dtype == np.float32 and out.shape == (2, n, n)
+    x = 2 * np.pi * np.arange(n) / n
+    exp = (2 * (0.5 * np.cos(x) + 0.25 * np.sin(x)) * U * L).astype(np.float32)
+    assert np.allclose(out[0, 3], exp, rtol=1e-6, atol=1e-3)
+    assert np.array_equal(out[0, 0], out[0, 5])          # no y dependence
+
+
+def test_la_from_b_adds_a_on_retained_modes_only():
+    """LA = B + 0.25 kh2 A / Bu where L=1 and 0 elsewhere (diagnostics.f90:1698-1727)."""
+    m, s, ic, p = small_model(32, 2)
+    B = random_masked(32, 2, 5, masked=False)
+    A = random_masked(32, 2, 6, masked=False)
+    la = m.la_from_b(B, A)
+    Lb = m.Lb
+    kh2 = m.kh2f
+    assert np.array_equal(la[:, ~Lb], np.zeros_like(la[:, ~Lb]))
+    assert np.allclose(la[:, Lb], (B + 0.25 * kh2 * A / m.p.Bu)[:, Lb], rtol=0, atol=1e-14)
+    # kh = 0: LA = B (horizontally uniform waves are their own LA)
+    assert la[0, 0, 0] == B[0, 0, 0]
+    R, I = m.dump_la(B * Lb, B * Lb, A * Lb, A * Lb, 2.5e-5, la=False)
+    assert np.array_equal(R, I)
