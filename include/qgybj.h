@@ -186,6 +186,18 @@ int qg_compute_qw(qg_handle* h, const double* BRk, const double* BIk, double* qw
  * (the reference's Uw_scale = 2.5e-5 is a single-precision literal). */
 int qg_dump_psi(qg_handle* h, float* out, int level0, int nlev, double U_scale, double L_scale);
 int qg_dump_la(qg_handle* h, float* outR, float* outI, int level0, int nlev, double Uw_scale, int la);
+/* Omega equation (the vertical-velocity diagnostic, main_waqg.f90:164-167),
+ * all n3 interior levels, dense spectral layout.
+ * qg_omega_eqn_rhs replaces derivatives.f90:1469-1586: rhs = r2c(2 J(psi_z, lap psi)),
+ * psi_z and the interpolated psi on the unstaggered level between z and z+1
+ * (0 and psi(top) at the top level).
+ * qg_omega_equation replaces elliptic.f90:463-567: per column with kh2 != 0 and
+ * L = 1 the tridiagonal system of the n3-1 unstaggered levels (DGTSV order,
+ * FP64); w at the top level and in every other column is 0.
+ * qg_omega: both, from the handle's resident psi. */
+int qg_omega_eqn_rhs(qg_handle* h, const double* psik, double* rhs);
+int qg_omega_equation(qg_handle* h, const double* rhs, double* wk);
+int qg_omega(qg_handle* h, double* wk);
 /* elliptic.f90:145-247: all n3 levels, z-major layout (no transpose). */
 int qg_psi_solver(qg_handle* h, const double* qstar, double* psik);
 /* elliptic.f90:346-460: all n3 levels; ck may be NULL. */

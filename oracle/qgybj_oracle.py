@@ -473,6 +473,53 @@ class Model:
         return ((self.fft_c2r(BRk) * Uw_scale).astype(np.float32),
                 (self.fft_c2r(BIk) * Uw_scale).astype(np.float32))
 
+    # -- omega equation (vertical velocity diagnostic) ----------------------
+    def omega_eqn_rhs(self, psik):
+        """derivatives.f90:1469-1586: rhs = r2c(2 (bx xy - by xx)) with
+        bx, by = i kx, i ky psi_z; xx, xy = -i kx, -i ky kh2 psi_avg on the
+        unstaggered level between z and z+1 (psi_z = 0, psi_avg = psi at the top)."""
+        g, Lb, dz = self.grid, self.Lb, self.p.dz
+        kx, ky, kh2 = g.kx, g.ky, self.kh2f
+        rz = np.zeros_like(psik)
+        rz[:-1] = np.where(Lb, (psik[1:] - psik[:-1]) / dz, 0)
+        bx = np.where(Lb, 1j * kx * rz, 0)
+        by = np.where(Lb, 1j * ky * rz, 0)
+        xx = np.zeros_like(psik)
+        xy = np.zeros_like(psik)
+        xx[:-1] = np.where(Lb, -1j * kx * kh2 * 0.5 * (psik[1:] + psik[:-1]), 0)
+        xy[:-1] = np.where(Lb, -1j * ky * kh2 * 0.5 * (psik[1:] + psik[:-1]), 0)
+        xx[-1] = np.where(Lb, -1j * kx * kh2 * psik[-1], 0)
+        xy[-1] = np.where(Lb, -1j * ky * kh2 * psik[-1], 0)
+        bxr, byr, xxr, xyr = (self.fft_c2r(a) for a in (bx, by, xx, xy))
+        return self.fft_r2c(2.0 * (bxr * xyr - byr * xxr))
+
+    def omega_equation(self, rhs):
+        """elliptic.f90:463-567: per column (kh2 != 0, L = 1) the n3-1
+        unstaggered levels, d = -(rho_ut(rho_st1 + rho_st0)/(rho_st1 rho_st0)
+        + dz^2 kh2/a), du = rho_ut(iz+1)/rho_st(iz+1), dl = rho_ut(iz-1)/rho_st(iz),
+        rhs dz^2 q, DGTSV; w = 0 at the top level and elsewhere."""
+        p, g = self.p, self.grid
+        n3, dz = p.n3, p.dz
+        a = np.asarray(p.a_ell_ut, dtype=np.float64)
+        ru = np.asarray(p.rho_ut, dtype=np.float64) * np.ones(n3)
+        rs = np.asarray(p.rho_st, dtype=np.float64) * np.ones(n3)
+        w = np.zeros_like(rhs)
+        act = self.Lb & (g.kh2 != 0)
+        if n3 < 2 or not act.any():
+            return w
+        kh2 = g.kh2[act].astype(np.float64)
+        m = n3 - 1
+        t1 = (ru[:m] * (rs[1:] + rs[:m])) / (rs[1:] * rs[:m])
+        d = np.stack([-(t1[i] + ((dz * dz) * kh2) / a[i]) for i in range(m)])
+        du = np.array([ru[i + 1] / rs[i + 1] for i in range(m - 1)])[:, None] * np.ones_like(kh2)
+        dl = np.array([ru[i] / rs[i + 1] for i in range(m - 1)])[:, None] * np.ones_like(kh2)
+        br = (dz * dz) * rhs[:m].real[:, act]
+        bi = (dz * dz) * rhs[:m].imag[:, act]
+        xr = dgtsv_nopivot(dl.copy(), d.copy(), du.copy(), br)
+        xi = dgtsv_nopivot(dl.copy(), d.copy(), du.copy(), bi)
+        w[:m][:, act] = xr + 1j * xi
+        return w
+
     # -- FP64 diagnostics (diagnostics.f90) ---------------------------------
     def diagnostics(self, s: "State") -> dict:
         """Domain-integrated energies and enstrophy.

@@ -124,6 +124,11 @@ int build_tables(const qg_config& c, qg::HostTables& t, std::string& err) {
   std::vector<double> a(c.a_ell_ut, c.a_ell_ut + n3), ru(n3, 1.0), rs(n3, 1.0);
   if (c.rho_ut) ru.assign(c.rho_ut, c.rho_ut + n3);
   if (c.rho_st) rs.assign(c.rho_st, c.rho_st + n3);
+  t.om_t1.assign(n3, 0.0); t.om_du.assign(n3, 0.0); t.om_dl.assign(n3, 0.0); t.om_a = a;
+  for (int i = 0; i + 1 < n3; ++i) {
+    t.om_t1[i] = (ru[i] * (rs[i + 1] + rs[i])) / (rs[i + 1] * rs[i]);
+    if (i + 2 < n3) { t.om_du[i] = ru[i + 1] / rs[i + 1]; t.om_dl[i] = ru[i] / rs[i + 1]; }
+  }
   t.rho_unit = true;
   for (int i = 0; i < n3; ++i) t.rho_unit = t.rho_unit && ru[i] == 1.0 && rs[i] == 1.0;
   t.du.assign(n3, 0.0); t.cu.assign(n3, 0.0); t.cl.assign(n3, 0.0); t.r2.assign(n3, 0.0);
@@ -376,6 +381,21 @@ int qg_dump_la(qg_handle* h, float* outR, float* outI, int level0, int nlev, dou
   QG_ENTRY(h);
   if (!outR || !outI) return fail(h, QG_ERR_ARG, "qg_dump_la: null pointer");
   return fwd(h, h->eng->dump_real(la ? 2 : 1, outR, outI, level0, nlev, Uw_scale, 1.0));
+}
+int qg_omega_eqn_rhs(qg_handle* h, const double* psik, double* rhs) {
+  QG_ENTRY(h);
+  if (!psik || !rhs) return fail(h, QG_ERR_ARG, "qg_omega_eqn_rhs: null pointer");
+  return fwd(h, h->eng->omega_eqn_rhs(psik, rhs));
+}
+int qg_omega_equation(qg_handle* h, const double* rhs, double* wk) {
+  QG_ENTRY(h);
+  if (!rhs || !wk) return fail(h, QG_ERR_ARG, "qg_omega_equation: null pointer");
+  return fwd(h, h->eng->omega_equation(rhs, wk));
+}
+int qg_omega(qg_handle* h, double* wk) {
+  QG_ENTRY(h);
+  if (!wk) return fail(h, QG_ERR_ARG, "qg_omega: null pointer");
+  return fwd(h, h->eng->omega_from_state(wk));
 }
 int qg_psi_solver(qg_handle* h, const double* qstar, double* psik) {
   QG_ENTRY(h);

@@ -253,4 +253,96 @@ __global__ void k_phys_f32(long long tot, const T* __restrict__ in, double s1, d
     out[i] = (float)(((double)in[i] * s1) * s2);
 }
 
+// Omega equation right-hand side, spectral part (derivatives.f90:1489-1560):
+// psi_z at the unstaggered level between z and z+1 (0 at the top level),
+// bx = i kx psi_z, by = i ky psi_z, xx = -i kx kh2 psi_avg, xy = -i ky kh2
+// psi_avg with psi_avg = (psi(z+1) + psi(z))/2, psi at the top level itself.
+static __global__ void k_omega_spec(int n, int n3, int kmax2, double dz, const double2* __restrict__ psi,
+                                    double2* __restrict__ bx, double2* __restrict__ by, double2* __restrict__ xx,
+                                    double2* __restrict__ xy) {
+  const long long per = (long long)n * (n / 2 + 1), tot = per * n3;
+  for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < tot; m += (long long)gridDim.x * blockDim.x) {
+    int kx, ky, iky; dense_mode(m, n, kx, ky, iky);
+    const bool top = m / per == n3 - 1;
+    double2 vbx = make_double2(0.0, 0.0), vby = vbx, vxx = vbx, vxy = vbx;
+    if (dense_L(kx, ky, iky, n, kmax2)) {
+      const double2 p0 = psi[m];
+      const double fkx = (double)kx, fky = (double)ky, kh2 = (double)(kx * kx + ky * ky);
+      if (!top) {
+        const double2 p1 = psi[m + per];
+        const double2 rz = make_double2((p1.x - p0.x) / dz, (p1.y - p0.y) / dz);
+        vbx = make_double2(-fkx * rz.y, fkx * rz.x);        // i kx psi_z
+        vby = make_double2(-fky * rz.y, fky * rz.x);        // i ky psi_z
+        const double2 sm = make_double2(p1.x + p0.x, p1.y + p0.y);
+        const double cx = fkx * kh2 * 0.5, cy = fky * kh2 * 0.5;   // -i kx kh2 0.5 (psi1 + psi0)
+        vxx = make_double2(cx * sm.y, -cx * sm.x);
+        vxy = make_double2(cy * sm.y, -cy * sm.x);
+      } else {
+        const double cx = fkx * kh2, cy = fky * kh2;
+        vxx = make_double2(cx * p0.y, -cx * p0.x);
+        vxy = make_double2(cy * p0.y, -cy * p0.x);
+      }
+    }
+    bx[m] = vbx; by[m] = vby; xx[m] = vxx; xy[m] = vxy;
+  }
+}
+
+// physical part: rhsr = 2 (bx xy - by xx)  (derivatives.f90:1569-1577)
+template <typename T>
+__global__ void k_omega_phys(long long tot, const T* __restrict__ bx, const T* __restrict__ by, const T* __restrict__ xx,
+                             const T* __restrict__ xy, T* __restrict__ o) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x)
+    o[i] = (T)2 * (bx[i] * xy[i] - by[i] * xx[i]);
+}
+
+// omega_equation (elliptic.f90:463-567): one thread per dense column with
+// kh2 != 0 and L = 1; n3-1 unstaggered levels; DGTSV's elimination order
+// (no interchange: |d| >= 2 >= |dl|) in correctly rounded FP64 operations,
+// the same factorisation for the real and imaginary right-hand sides
+// (dz^2 * rhs).  w at the top level and in every other column is 0.
+// scr: 3 * (n3-1) * per doubles (modified diagonal, two right-hand sides).
+static __global__ void k_omega_solve(int n, int n3, int kmax2, double dz, const double* __restrict__ t1,
+                                     const double* __restrict__ du, const double* __restrict__ dl,
+                                     const double* __restrict__ a, const double2* __restrict__ rhs,
+                                     double* __restrict__ scr, double2* __restrict__ w) {
+  const long long per = (long long)n * (n / 2 + 1);
+  const long long col = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (col >= per) return;
+  int kx, ky, iky; dense_mode(col, n, kx, ky, iky);
+  const int kh2i = kx * kx + ky * ky;
+  if (kh2i == 0 || !dense_L(kx, ky, iky, n, kmax2) || n3 < 2) {
+    for (int z = 0; z < n3; ++z) w[z * per + col] = make_double2(0.0, 0.0);
+    return;
+  }
+  const int m = n3 - 1;
+  const double dz2 = __dmul_rn(dz, dz), kh2 = (double)kh2i, dzk = __dmul_rn(dz2, kh2);
+  double* dd = scr;
+  double* br = scr + (long long)m * per;
+  double* bi = scr + 2LL * m * per;
+  auto diag = [&](int i) { return -__dadd_rn(t1[i], __ddiv_rn(dzk, a[i])); };
+  double dprev = diag(0);
+  double rprev = __dmul_rn(dz2, rhs[col].x), iprev = __dmul_rn(dz2, rhs[col].y);
+  dd[col] = dprev; br[col] = rprev; bi[col] = iprev;
+  for (int i = 0; i + 1 < m; ++i) {
+    const double fact = __ddiv_rn(dl[i], dprev);
+    const double dn = __dsub_rn(diag(i + 1), __dmul_rn(fact, du[i]));
+    const double2 q = rhs[(long long)(i + 1) * per + col];
+    rprev = __dsub_rn(__dmul_rn(dz2, q.x), __dmul_rn(fact, rprev));
+    iprev = __dsub_rn(__dmul_rn(dz2, q.y), __dmul_rn(fact, iprev));
+    dprev = dn;
+    const long long o = (long long)(i + 1) * per + col;
+    dd[o] = dn; br[o] = rprev; bi[o] = iprev;
+  }
+  // back substitution
+  double xr = __ddiv_rn(rprev, dprev), xi = __ddiv_rn(iprev, dprev);
+  w[(long long)(m - 1) * per + col] = make_double2(xr, xi);
+  for (int i = m - 2; i >= 0; --i) {
+    const long long o = (long long)i * per + col;
+    xr = __ddiv_rn(__dsub_rn(br[o], __dmul_rn(du[i], xr)), dd[o]);
+    xi = __ddiv_rn(__dsub_rn(bi[o], __dmul_rn(du[i], xi)), dd[o]);
+    w[o] = make_double2(xr, xi);
+  }
+  w[(long long)m * per + col] = make_double2(0.0, 0.0);
+}
+
 }  // namespace qg

@@ -20,6 +20,9 @@ struct HostTables {
   std::vector<double> cu, cl;               // [n3] init_q coefficients of psi(z+1), psi(z-1)
   std::vector<double> r2;                   // [n3] N^2 at za(iz)
   bool rho_unit = true;                     // rho_ut = rho_st = 1: symmetric vertical operators
+  // omega equation (elliptic.f90:463-567), unstaggered levels iz = 0..n3-2:
+  // d = -(om_t1 + dz^2 kh2 / a), upper om_du, lower om_dl; om_a = a_ell_ut
+  std::vector<double> om_t1, om_du, om_dl, om_a;
 };
 
 struct EngineBase {
@@ -54,6 +57,11 @@ struct EngineBase {
   }
   // real-space FP32 output of the dumps: which = 0 psi (out0), 1 B, 2 LA (out0 = R, out1 = I)
   virtual int dump_real(int which, float* out0, float* out1, int level0, int nlev, double s1, double s2) = 0;
+  // omega equation: right-hand side (derivatives.f90:1469-1586), solve
+  // (elliptic.f90:463-567), and w from the resident psi
+  virtual int omega_eqn_rhs(const double* psik, double* rhs) = 0;
+  virtual int omega_equation(const double* rhs, double* wk) = 0;
+  virtual int omega_from_state(double* wk) = 0;
   virtual int fft_r2c(const double* rvar, double* kvar, int nz) = 0;
   virtual int fft_c2r(const double* kvar, double* rvar, int nz) = 0;
   virtual int convol_waqg(const double* uk, const double* vk, const double* qk, const double* BRk, const double* BIk,

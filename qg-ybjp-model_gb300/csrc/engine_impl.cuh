@@ -68,6 +68,14 @@ class Engine : public EngineBase {
     };
     int rc;
     if ((rc = up(&e1, t.e1)) || (rc = up(&e2, t.e2)) || (rc = up(&e1w, t.e1w)) || (rc = up(&e2w, t.e2w))) return rc;
+    {
+      const std::vector<double>* om[4] = {&t.om_t1, &t.om_du, &t.om_dl, &t.om_a};
+      double** dst[4] = {&om_t1, &om_du, &om_dl, &om_a};
+      for (int k = 0; k < 4; ++k) {
+        QG_CK(cudaMalloc(dst[k], (size_t)g.n3 * sizeof(double)));
+        QG_CK(cudaMemcpy(*dst[k], om[k]->data(), (size_t)g.n3 * sizeof(double), cudaMemcpyHostToDevice));
+      }
+    }
     std::vector<C> twh(g.n);
     for (int m = 0; m < g.n; ++m) twh[m] = mk<T>((T)t.tw[2 * m], (T)t.tw[2 * m + 1]);
     QG_CK(cudaMalloc(&tw, g.n * sizeof(C)));
@@ -263,6 +271,58 @@ class Engine : public EngineBase {
     return QG_OK;
   }
 
+  // ---- omega equation (the vertical-velocity diagnostic) ---------------------
+  // right-hand side from the dense psi in D[0] into D[5]
+  int omega_rhs_dev() {
+    const long long tot = (long long)g.n3 * g.n * (g.n / 2 + 1), pt = (long long)g.n3 * g.n * g.n;
+    k_omega_spec<<<grid_for(tot), 256, 0, st>>>(g.n, g.n3, g.kmax2, cfg.dz, D[0], D[1], D[2], D[3], D[4]);
+    QG_LAUNCHED();
+    int rc;
+    for (int k = 0; k < 4; ++k)
+      if ((rc = d_c2r(D[1 + k], P[k], g.n3))) return rc;
+    k_omega_phys<T><<<grid_for(pt), 256, 0, st>>>(pt, P[0], P[1], P[2], P[3], P[4]);
+    QG_LAUNCHED();
+    return d_r2c(P[4], D[5], g.n3);
+  }
+  // w from the dense right-hand side in `rhs` into D[1]
+  int omega_solve_dev(const double2* rhs) {
+    const long long per = (long long)g.n * (g.n / 2 + 1);
+    if (!om_scr) QG_CK(cudaMalloc(&om_scr, (size_t)3 * (g.n3 > 1 ? g.n3 - 1 : 1) * per * sizeof(double)));
+    k_omega_solve<<<(unsigned)((per + 127) / 128), 128, 0, st>>>(g.n, g.n3, g.kmax2, cfg.dz, om_t1, om_du, om_dl, om_a,
+                                                                 rhs, om_scr, D[1]);
+    QG_LAUNCHED();
+    return QG_OK;
+  }
+  int omega_eqn_rhs(const double* psik, double* rhs) override {
+    int rc = prep_dense(g.n3);
+    if (rc) return rc;
+    QG_CK(cudaMemcpyAsync(D[0], psik, dense_bytes(g.n3), cudaMemcpyDefault, st));
+    if ((rc = omega_rhs_dev())) return rc;
+    QG_CK(cudaMemcpyAsync(rhs, D[5], dense_bytes(g.n3), cudaMemcpyDefault, st));
+    QG_CK(cudaStreamSynchronize(st));
+    return QG_OK;
+  }
+  int omega_equation(const double* rhs, double* wk) override {
+    int rc = prep_dense(g.n3);
+    if (rc) return rc;
+    QG_CK(cudaMemcpyAsync(D[0], rhs, dense_bytes(g.n3), cudaMemcpyDefault, st));
+    if ((rc = omega_solve_dev(D[0]))) return rc;
+    QG_CK(cudaMemcpyAsync(wk, D[1], dense_bytes(g.n3), cudaMemcpyDefault, st));
+    QG_CK(cudaStreamSynchronize(st));
+    return QG_OK;
+  }
+  int omega_from_state(double* wk) override {
+    int rc = prep_dense(g.n3);
+    if (rc) return rc;
+    k_compact_to_dense<T><<<grid_for((long long)g.n3 * g.n * (g.n / 2 + 1)), 256, 0, st>>>(g, 0, g.n3, F[F_PSI], D[0], 0,
+                                                                                          cfg.dz);
+    QG_LAUNCHED();
+    if ((rc = omega_rhs_dev()) || (rc = omega_solve_dev(D[5]))) return rc;
+    QG_CK(cudaMemcpyAsync(wk, D[1], dense_bytes(g.n3), cudaMemcpyDefault, st));
+    QG_CK(cudaStreamSynchronize(st));
+    return QG_OK;
+  }
+
   // ---- routine-level drop-ins ---------------------------------------------
   int fft_r2c(const double* rvar, double* kvar, int nz) override {
     int rc = prep_dense(nz);
@@ -404,6 +464,7 @@ class Engine : public EngineBase {
   double2* bscr = nullptr;
   double *du = nullptr, *cu = nullptr, *cl = nullptr, *r2 = nullptr;
   double *diag_part = nullptr, *diag_out = nullptr, *diag_host = nullptr;
+  double *om_t1 = nullptr, *om_du = nullptr, *om_dl = nullptr, *om_a = nullptr, *om_scr = nullptr;
   C* S = nullptr;
   double2* psi64 = nullptr;
   int Zb = 1;
@@ -423,7 +484,7 @@ class Engine : public EngineBase {
     for (auto& x : gexec) if (x) { cudaGraphExecDestroy(x); x = nullptr; }
     for (auto& p : F) if (p) { cudaFree(p); p = nullptr; }
     void* ps[] = {e1, e2, e1w, e2w, tw, tab_idx, fac_psi, fac_A, bscr, du, cu, cl, r2, diag_part, diag_out, S, stage,
-                  W, dstage, psi64};
+                  W, dstage, psi64, om_t1, om_du, om_dl, om_a, om_scr};
     for (void* p : ps) if (p) cudaFree(p);
     for (auto& p : D) if (p) cudaFree(p);
     for (auto& p : P) if (p) cudaFree(p);

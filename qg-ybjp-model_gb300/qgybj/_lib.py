@@ -27,6 +27,7 @@ EXPORTS = (
     "qg_ensemble_create", "qg_ensemble_member", "qg_ensemble_step", "qg_ensemble_synchronize",
     "qg_ensemble_get_stream", "qg_ensemble_destroy", "qg_ensemble_last_error", "qg_autotune",
     "qg_adjoint_run", "qg_adjoint_step", "qg_dump_psi", "qg_dump_la",
+    "qg_omega_eqn_rhs", "qg_omega_equation", "qg_omega",
 )
 KERNEL_CLASSES = ("dissipation", "col_inv", "row_main", "col_update", "row_qw", "col_qw", "solve")
 
@@ -102,6 +103,9 @@ def lib() -> C.CDLL:
         "qg_adjoint_step": (ip, [vp, ip, vp, vp, vp, vp]),
         "qg_dump_psi": (ip, [vp, vp, ip, ip, C.c_double, C.c_double]),
         "qg_dump_la": (ip, [vp, vp, vp, ip, ip, C.c_double, ip]),
+        "qg_omega_eqn_rhs": (ip, [vp, vp, vp]),
+        "qg_omega_equation": (ip, [vp, vp, vp]),
+        "qg_omega": (ip, [vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -223,6 +223,25 @@ class Simulation:
         p2 = write_dump(directory, "la", count, {"LAr": lr, "LAi": li}, ts)
         return p1, p2
 
+    # -- omega equation (vertical velocity) ------------------------------------------
+    def omega_eqn_rhs(self, psik):
+        p = self._c(psik)
+        out = np.empty_like(p)
+        self._ck(lib().qg_omega_eqn_rhs(self.h, ptr(p), ptr(out)))
+        return out
+
+    def omega_equation(self, rhs):
+        r = self._c(rhs)
+        out = np.empty_like(r)
+        self._ck(lib().qg_omega_equation(self.h, ptr(r), ptr(out)))
+        return out
+
+    def omega(self):
+        """w (spectral, dense layout) from the resident psi."""
+        out = np.empty(self.spectral_shape, dtype=np.complex128)
+        self._ck(lib().qg_omega(self.h, ptr(out)))
+        return out
+
     # -- adjoint (FP64 handles) ------------------------------------------------------
     def adjoint_run(self, q0, BR0, BI0, nsteps: int, ckpt_every: int = 10, gradient: bool = True):
         """J = 1/2 sum over the central quarter and top fifth of |LA|^2 after

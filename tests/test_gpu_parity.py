@@ -257,6 +257,28 @@ def test_output_dumps(precision, tmp_path):
     sim.close()
 
 
+@pytest.mark.parametrize("strat", ["c0", "c1"])
+def test_omega_equation(strat):
+    """qg_omega_eqn_rhs / qg_omega_equation (FP64 drop-ins) and qg_omega (from
+    the resident psi) against the oracle: rhs 1e-12, solve 1e-13 (DGTSV order
+    reproduced), w from the state 1e-12 (constant N^2) / 1e-10 (exponential
+    stratification, whose columns are ill-conditioned at small kh)."""
+    rc = scaled(CONFIGS[strat], 32, 12)
+    model, st, sim = pair(rc, "fp64")
+    sim.step(True)
+    sim.step()
+    psi = sim.get_state("psi")
+    rhs = sim.omega_eqn_rhs(psi)
+    exp_rhs = model.omega_eqn_rhs(psi)
+    assert rel_l2(rhs, exp_rhs) <= 1e-12
+    w = sim.omega_equation(exp_rhs)
+    assert rel_l2(w, model.omega_equation(exp_rhs)) <= 1e-13
+    assert np.abs(w[-1]).max() == 0
+    tol = 1e-12 if strat == "c0" else 1e-10
+    assert rel_l2(sim.omega(), model.omega_equation(exp_rhs)) <= tol
+    sim.close()
+
+
 def test_error_statuses():
     p = _params()
     with pytest.raises(QgError) as e:

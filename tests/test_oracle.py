@@ -307,3 +307,56 @@ def test_la_from_b_adds_a_on_retained_modes_only():
     assert la[0, 0, 0] == B[0, 0, 0]
     R, I = m.dump_la(B * Lb, B * Lb, A * Lb, A * Lb, 2.5e-5, la=False)
     assert np.array_equal(R, I)
+
+
+# --- omega equation ----------------------------------------------------------------
+def test_omega_rhs_two_modes_known_answer():
+    """psi = A(z) cos x + B(z) cos y: 2 J(psi_z, lap psi) = 2 sin x sin y
+    (Abar B' - A' Bbar) with the discrete vertical difference and average, so
+    the (1, +-1) modes carry -/+ c/2 and every other mode is zero."""
+    m, s, ic, p = small_model(16, 6)
+    n, n3, dz = 16, 6, m.p.dz
+    z = np.arange(n3)
+    A = 1.0 + 0.3 * z
+    B = np.cos(0.7 * z)
+    psik = np.zeros((n3, n, n // 2 + 1), dtype=complex)
+    psik[:, 0, 1] = A / 2
+    psik[:, 1, 0] = B / 2
+    rhs = m.omega_eqn_rhs(psik)
+    c = np.zeros(n3)
+    c[:-1] = 0.5 * (A[1:] + A[:-1]) * (B[1:] - B[:-1]) / dz - (A[1:] - A[:-1]) / dz * 0.5 * (B[1:] + B[:-1])
+    assert np.allclose(rhs[:, 1, 1], -0.5 * c, atol=1e-13)
+    assert np.allclose(rhs[:, n - 1, 1], 0.5 * c, atol=1e-13)
+    rest = rhs.copy()
+    rest[:, 1, 1] = 0
+    rest[:, n - 1, 1] = 0
+    assert np.abs(rest).max() < 1e-13
+    # a single horizontal mode has no Jacobian with its own Laplacian
+    only = psik.copy()
+    only[:, 1, 0] = 0
+    assert np.abs(m.omega_eqn_rhs(only)).max() < 1e-13
+
+
+@pytest.mark.parametrize("strat", ["constant", "exponential"])
+def test_omega_equation_inverts_its_operator(strat):
+    """Apply the tridiagonal operator of elliptic.f90:463-567 to a random w
+    (zero at the top level, kh2 != 0, L = 1) and solve it back."""
+    m, s, ic, p = small_model(32, 12, strat)
+    n3, dz = m.p.n3, m.p.dz
+    g = m.grid
+    act = m.Lb & (g.kh2 != 0)
+    w = random_masked(32, n3, 11) * act
+    w[-1] = 0
+    a = np.asarray(m.p.a_ell_ut)
+    kh2 = m.kh2f
+    rhs = np.zeros_like(w)
+    for i in range(n3 - 1):
+        v = -(2.0 + dz * dz * kh2 / a[i]) * w[i]
+        if i > 0:
+            v = v + w[i - 1]
+        if i < n3 - 2:
+            v = v + w[i + 1]
+        rhs[i] = np.where(act, v / (dz * dz), 0)
+    got = m.omega_equation(rhs)
+    assert rel_l2(got, w) < 1e-11
+    assert np.abs(got[-1]).max() == 0
