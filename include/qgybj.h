@@ -120,7 +120,9 @@ int qg_get_state(qg_handle* h, int field, double* kvar, int level0, int nlev);
 
 /* Initialisation sequence of main_waqg.f90:129-147 on the resident state:
  * optional sumB (derivatives.f90:1073-1118), q = init_q(psi) (init.f90:591),
- * old levels = current levels, and A = A_solver_ybj_plus(B). */
+ * old levels = current levels, and A = A_solver_ybj_plus(B) (YBJ+; with
+ * ybj_plus = 0 the A the host set is kept, as the reference keeps the A of
+ * its initial-condition fields). */
 int qg_init_state(qg_handle* h, int apply_sumB, int q_from_psi);
 /* With fixed_flow = 1, q is set to 0 instead (main_waqg.f90:141-146). */
 

@@ -393,8 +393,11 @@ class Model:
             rBR = np.zeros_like(rBR); rBI = np.zeros_like(rBI)
         return nq, nBR, nBI, rBR, rBI, dq, AR, AI
 
-    def invert(self, s: "State") -> "State":
-        """q* = q - q^w, psi and A inversions (main_waqg.f90:421-462)."""
+    def invert(self, s: "State", tend=None) -> "State":
+        """q* = q - q^w, psi and A inversions (main_waqg.f90:421-462).
+        Regular YBJ (ybj_plus = 0): sumB on B^{n+1}, then A from the vertical
+        integral of B and sigma of this step's tendencies `tend` =
+        (nBR, nBI, rBR, rBI) (main_waqg.f90:449-460)."""
         p = self.p
         psi, AR, AI, CR, CI = s.psi, s.AR, s.AI, s.CR, s.CI
         if p.fixed_flow == 0:
@@ -405,9 +408,50 @@ class Model:
             qstar = np.where(self.Lb, s.q - qw, qw)
             psi = self.psi_solver(qstar)
         if p.passive_scalar == 0:
-            AR, CR = self.A_solver_ybj_plus(s.BR)
-            AI, CI = self.A_solver_ybj_plus(s.BI)
+            if p.ybj_plus == 1:
+                AR, CR = self.A_solver_ybj_plus(s.BR)
+                AI, CI = self.A_solver_ybj_plus(s.BI)
+            else:
+                BR, BI = self.sumB(s.BR, s.BI)
+                s = replace(s, BR=BR, BI=BI)
+                sig1, sig2 = self.compute_sigma(*tend)
+                AR, CR = self.compute_A(s.BR, sig1)
+                AI, CI = self.compute_A(s.BI, sig2)
         return replace(s, psi=psi, AR=AR, AI=AI, CR=CR, CI=CI)
+
+    # -- regular YBJ (ybj_plus = 0) ------------------------------------------
+    def compute_sigma(self, nBR, nBI, rBR, rBI):
+        """derivatives.f90:1037-1068: sigma = Bu Ro sum_z ((rBR + 2 nBI)/kh2,
+        (rBI - 2 nBR)/kh2) where kh2 > 0 and L = 1 (vertical integral of A)."""
+        p = self.p
+        sel = self.Lb & (self.grid.kh2 > 0)
+        kh2 = np.where(sel, self.kh2f, 1.0)
+        s1 = np.zeros(nBR.shape[1:], dtype=complex)
+        s2 = np.zeros(nBR.shape[1:], dtype=complex)
+        for z in range(nBR.shape[0]):
+            s1 = s1 + np.where(sel, (rBR[z] + 2 * nBI[z]) / kh2, 0)
+            s2 = s2 + np.where(sel, (rBI[z] - 2 * nBR[z]) / kh2, 0)
+        return s1 * p.Bu * p.Ro, s2 * p.Bu * p.Ro
+
+    def compute_A(self, Bk, sigma):
+        """derivatives.f90:1141-1264: A~(1) = 0, A~(iz) = A~(iz-1) + sumB r_2ut(iz-1) dz^2
+        with sumB the running vertical sum of B; A = A~ + (sigma - sum A~)/n3 where
+        kh2 > 0 and L = 1, else 0; C = A_z (0 at the top)."""
+        p = self.p
+        n3, dz = p.n3, p.dz
+        r2 = np.asarray(p.r_2ut, dtype=np.float64)
+        sel = self.Lb & (self.grid.kh2 > 0)
+        At = np.zeros_like(Bk)
+        sumB = Bk[0].copy()
+        sumA = np.zeros(Bk.shape[1:], dtype=complex)
+        for iz in range(1, n3):
+            At[iz] = At[iz - 1] + sumB * r2[iz - 1] * dz * dz
+            sumA = sumA + At[iz]
+            sumB = sumB + Bk[iz]
+        A = np.where(sel, At + (sigma - sumA) / n3, 0)
+        C = np.zeros_like(A)
+        C[:-1] = (A[1:] - A[:-1]) / dz
+        return A, C
 
     def step_euler(self, s: "State") -> "State":
         """First step, forward Euler (main_waqg.f90:197-317)."""
@@ -423,7 +467,7 @@ class Model:
         Lb = self.Lb
         q, BR, BI = (np.where(Lb, x, 0) for x in (q, BR, BI))
         s2 = replace(s, q=q, BR=BR, BI=BI, qo=qo.copy(), BRo=BRo.copy(), BIo=BIo.copy())
-        return self.invert(s2)
+        return self.invert(s2, (nBR, nBI, rBR, rBI))
 
     def step_leapfrog(self, s: "State") -> "State":
         """Leapfrog + Robert-Asselin filter (main_waqg.f90:326-467)."""
@@ -443,7 +487,7 @@ class Model:
         BRo = np.where(Lb, s.BR + g * (s.BRo - 2 * s.BR + BRt), 0)
         BIo = np.where(Lb, s.BI + g * (s.BIo - 2 * s.BI + BIt), 0)
         s2 = replace(s, q=qt, BR=BRt, BI=BIt, qo=qo, BRo=BRo, BIo=BIo)
-        return self.invert(s2)
+        return self.invert(s2, (nBR, nBI, rBR, rBI))
 
     def step(self, s: "State", first: bool) -> "State":
         return self.step_euler(s) if first else self.step_leapfrog(s)
@@ -620,8 +664,10 @@ def initial_state(model: Model, psik: np.ndarray, BRk: np.ndarray,
     z = np.zeros_like(psik)
     s = State(q=q, qo=q.copy(), BR=BRk.copy(), BI=BIk.copy(), BRo=BRk.copy(), BIo=BIk.copy(),
               psi=psik.copy(), AR=z.copy(), AI=z.copy(), CR=z.copy(), CI=z.copy())
-    if model.p.passive_scalar == 0:
+    if model.p.passive_scalar == 0 and model.p.ybj_plus == 1:
         AR, CR = model.A_solver_ybj_plus(s.BR)
         AI, CI = model.A_solver_ybj_plus(s.BI)
         s = replace(s, AR=AR, AI=AI, CR=CR, CI=CI)
+    # regular YBJ: A at t = 0 is the initial-condition field (zero here unless
+    # the caller sets it), as generate_fields_stag provides it (main_waqg.f90:124-127)
     return s

@@ -235,7 +235,7 @@ int qg_create(const qg_config* cfg, qg_handle** out) {
   if (c.n3 < 2) return fail(nullptr, QG_ERR_ARG, "n3 must be >= 2");
   if (c.n3 > 1024) return fail(nullptr, QG_ERR_UNSUPPORTED, "n3 must be <= 1024 (solve checkpoints in shared memory)");
   if (c.precision != QG_PREC_FP64 && c.precision != QG_PREC_MIXED) return fail(nullptr, QG_ERR_ARG, "bad precision");
-  if (c.ybj_plus != 1) return fail(nullptr, QG_ERR_UNSUPPORTED, "only the YBJ+ step (ybj_plus=1) is implemented");
+  if (c.ybj_plus != 0 && c.ybj_plus != 1) return fail(nullptr, QG_ERR_ARG, "ybj_plus must be 0 or 1");
   if (!c.a_ell_ut) return fail(nullptr, QG_ERR_ARG, "a_ell_ut is required");
   if (!(c.dz > 0) || !(c.Bu > 0) || !(c.Ro > 0)) return fail(nullptr, QG_ERR_ARG, "dz, Bu and Ro must be positive");
   const double sc[] = {c.dz, c.Bu, c.Ro, c.W2F, c.delt, c.gamma, c.nuh1, c.nuh2, c.nuh1w, c.nuh2w, c.nuz};

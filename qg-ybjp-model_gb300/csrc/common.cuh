@@ -57,6 +57,7 @@ struct StepParams {
   int disp;           // 0 when no_dispersion == 1 or passive_scalar == 1
   int use_dq;         // inviscid == 0 && nuz != 0
   int euler;          // forward Euler first step
+  int ybj;            // 1: YBJ+ (A from A_solver_ybj_plus); 0: regular YBJ (A from the vertical integral of B)
 };
 
 }  // namespace qg

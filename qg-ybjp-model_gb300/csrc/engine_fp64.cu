@@ -190,6 +190,7 @@ class AdjEngine final : public Engine<double> {
     // derived from the carried state
     if (!rho_unit) { err = "the adjoint needs rho_ut = rho_st = 1 (symmetric vertical operators)"; return QG_ERR_UNSUPPORTED; }
     if (sp.use_dq) { err = "the adjoint covers the inviscid vertical step (nuz = 0 or inviscid = 1)"; return QG_ERR_UNSUPPORTED; }
+    if (!cfg.ybj_plus) { err = "the adjoint covers the YBJ+ step (ybj_plus = 1)"; return QG_ERR_UNSUPPORTED; }
     if (cfg.fixed_flow || cfg.passive_scalar) {
       err = "the adjoint needs fixed_flow = 0 and passive_scalar = 0";
       return QG_ERR_UNSUPPORTED;

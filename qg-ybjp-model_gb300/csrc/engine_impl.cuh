@@ -58,6 +58,9 @@ class Engine : public EngineBase {
       QG_CK(cudaMalloc(&F[f], fbytes));
       QG_CK(cudaMemsetAsync(F[f], 0, fbytes, st));
     }
+    if (!cfg.ybj_plus && !cfg.passive_scalar) {
+      for (auto& p : sig) { QG_CK(cudaMalloc(&p, fbytes)); QG_CK(cudaMemsetAsync(p, 0, fbytes, st)); }
+    }
     // tables
     std::vector<T> tmp(g.plane);
     auto up = [&](T** d, const std::vector<double>& h) -> int {
@@ -113,6 +116,7 @@ class Engine : public EngineBase {
     sp.disp = (cfg.no_dispersion || cfg.passive_scalar) ? 0 : 1;
     sp.use_dq = (cfg.inviscid == 0 && cfg.nuz != 0.0) ? 1 : 0;
     sp.euler = 0;
+    sp.ybj = cfg.ybj_plus ? 1 : 0;
     need_qw = (!cfg.fixed_flow && !cfg.no_feedback);
     int r0 = set_smem_attrs();
     if (r0) return r0;
@@ -204,7 +208,7 @@ class Engine : public EngineBase {
     QG_CK(cudaMemcpyAsync(F[F_QO], F[F_Q], fbytes, cudaMemcpyDeviceToDevice, st));
     QG_CK(cudaMemcpyAsync(F[F_BRO], F[F_BR], fbytes, cudaMemcpyDeviceToDevice, st));
     QG_CK(cudaMemcpyAsync(F[F_BIO], F[F_BI], fbytes, cudaMemcpyDeviceToDevice, st));
-    if (!cfg.passive_scalar) {
+    if (!cfg.passive_scalar && cfg.ybj_plus) {   // regular YBJ keeps the A the host set
       int rc = launch_solve(F[F_QSTAR], 0, 1);
       if (rc) return rc;
     }
@@ -465,6 +469,7 @@ class Engine : public EngineBase {
   double *du = nullptr, *cu = nullptr, *cl = nullptr, *r2 = nullptr;
   double *diag_part = nullptr, *diag_out = nullptr, *diag_host = nullptr;
   double *om_t1 = nullptr, *om_du = nullptr, *om_dl = nullptr, *om_a = nullptr, *om_scr = nullptr;
+  C* sig[2] = {};     // regular YBJ: per-level sigma terms
   C* S = nullptr;
   double2* psi64 = nullptr;
   int Zb = 1;
@@ -484,7 +489,7 @@ class Engine : public EngineBase {
     for (auto& x : gexec) if (x) { cudaGraphExecDestroy(x); x = nullptr; }
     for (auto& p : F) if (p) { cudaFree(p); p = nullptr; }
     void* ps[] = {e1, e2, e1w, e2w, tw, tab_idx, fac_psi, fac_A, bscr, du, cu, cl, r2, diag_part, diag_out, S, stage,
-                  W, dstage, psi64, om_t1, om_du, om_dl, om_a, om_scr};
+                  W, dstage, psi64, om_t1, om_du, om_dl, om_a, om_scr, sig[0], sig[1]};
     for (void* p : ps) if (p) cudaFree(p);
     for (auto& p : D) if (p) cudaFree(p);
     for (auto& p : P) if (p) cudaFree(p);
@@ -553,6 +558,7 @@ class Engine : public EngineBase {
     StateP<T> p;
     p.q = F[F_Q]; p.qo = F[F_QO]; p.BR = F[F_BR]; p.BI = F[F_BI]; p.BRo = F[F_BRO]; p.BIo = F[F_BIO];
     p.psi = F[F_PSI]; p.AR = F[F_AR]; p.AI = F[F_AI]; p.qstar = F[F_QSTAR]; p.dq = F[F_DQ];
+    p.sig1 = sig[0]; p.sig2 = sig[1];
     return p;
   }
 
@@ -640,8 +646,15 @@ class Engine : public EngineBase {
       });
     }
     if (int rc0 = pbeg(QG_K_SOLVE)) return rc0;
-    int rc = launch_solve(need_qw ? F[F_QSTAR] : F[F_Q], cfg.fixed_flow ? 0 : 1, cfg.passive_scalar ? 0 : 1);
+    int rc = launch_solve(need_qw ? F[F_QSTAR] : F[F_Q], cfg.fixed_flow ? 0 : 1,
+                          (cfg.passive_scalar || !cfg.ybj_plus) ? 0 : 1);
     if (rc) return rc;
+    if (!cfg.ybj_plus && !cfg.passive_scalar) {
+      // regular YBJ: sumB on B^{n+1}, then A from the vertical integral (main_waqg.f90:449-460)
+      k_ybj_A<T><<<(unsigned)((g.plane + 127) / 128), 128, 0, st>>>(g, cfg.dz, cfg.Bu, cfg.Ro, r2, F[F_BR], F[F_BI],
+                                                                    sig[0], sig[1], F[F_AR], F[F_AI]);
+      QG_LAUNCHED();
+    }
     return pend();
   }
 

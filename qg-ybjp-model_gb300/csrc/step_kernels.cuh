@@ -259,6 +259,7 @@ k_row_main(Geom g, StepParams sp, cplx<T>* __restrict__ S, const cplx<T>* __rest
 template <typename T> struct StateP {
   cplx<T>* q; cplx<T>* qo; cplx<T>* BR; cplx<T>* BI; cplx<T>* BRo; cplx<T>* BIo;
   cplx<T>* psi; cplx<T>* AR; cplx<T>* AI; cplx<T>* qstar; const cplx<T>* dq;
+  cplx<T>* sig1; cplx<T>* sig2;   // regular YBJ: per-level terms of sigma (compute_sigma)
 };
 
 // ===========================================================================
@@ -396,6 +397,15 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
         X[m] = xn;
         Xo[m] = xf;
         if (which > 0) bnew[(which - 1) * FE + e] = xn;
+        if (!sp.ybj && which > 0) {
+          // compute_sigma (derivatives.f90:1037-1068) with the tendencies
+          // T_R = nBR - rBI/2, T_I = nBI + rBR/2: (rBR + 2 nBI) = 2 T_I,
+          // (rBI - 2 nBR) = -2 T_R, divided by kh2 where kh2 > 0 and L = 1
+          const int kh2 = kx * kx + ky * ky;
+          cplx<T> sv = mk<T>(0, 0);
+          if (kh2 > 0 && g.mask(kx, ky)) sv = cscale(tnd, (which == 2 ? (T)2 : (T)-2) / (T)kh2);
+          (which == 2 ? st.sig1 : st.sig2)[m] = sv;
+        }
       }
     };
   };
@@ -838,6 +848,76 @@ __global__ void k_init_q(Geom g, double dz, const double* __restrict__ cu, const
       out = mk<T>((T)__ddiv_rn(vr, dz2), (T)__ddiv_rn(vi, dz2));
     }
     q[i] = out;
+  }
+}
+
+// ===========================================================================
+// Regular YBJ (ybj_plus = 0): sumB and compute_A after the update, one thread
+// per retained column, FP64 (derivatives.f90:1073-1118, 1141-1264)
+// ===========================================================================
+template <typename T>
+__global__ void k_ybj_A(Geom g, double dz, double Bu, double Ro, const double* __restrict__ r2, cplx<T>* __restrict__ BR,
+                        cplx<T>* __restrict__ BI, const cplx<T>* __restrict__ sig1, const cplx<T>* __restrict__ sig2,
+                        cplx<T>* __restrict__ AR, cplx<T>* __restrict__ AI) {
+  const long long mcol = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (mcol >= g.plane) return;
+  const int r = (int)(mcol / g.KXP), kx = (int)(mcol % g.KXP);
+  const int ky = g.ky_of_row(r);
+  const int n3 = g.n3;
+  if (kx > g.K) return;
+  if (!(g.mask(kx, ky) && kx * kx + ky * ky > 0)) {
+    for (int z = 0; z < n3; ++z) { AR[z * g.plane + mcol] = mk<T>(0, 0); AI[z * g.plane + mcol] = mk<T>(0, 0); }
+    return;
+  }
+  // sumB: remove the vertical mean of B
+  double sR[2] = {0, 0}, sI[2] = {0, 0}, g1[2] = {0, 0}, g2[2] = {0, 0};
+  for (int z = 0; z < n3; ++z) {
+    const long long m = z * g.plane + mcol;
+    const cplx<T> br = BR[m], bi = BI[m], a = sig1[m], b = sig2[m];
+    sR[0] += to64<T>(br.x); sR[1] += to64<T>(br.y);
+    sI[0] += to64<T>(bi.x); sI[1] += to64<T>(bi.y);
+    g1[0] += to64<T>(a.x); g1[1] += to64<T>(a.y);
+    g2[0] += to64<T>(b.x); g2[1] += to64<T>(b.y);
+  }
+  const double mR[2] = {sR[0] / n3, sR[1] / n3}, mI[2] = {sI[0] / n3, sI[1] / n3};
+  // sigma = sigma * Bu * Ro (derivatives.f90:1066)
+  const double s1[2] = {g1[0] * Bu * Ro, g1[1] * Bu * Ro}, s2[2] = {g2[0] * Bu * Ro, g2[1] * Bu * Ro};
+  // A~(0) = 0, A~(z) = A~(z-1) + sumB r_2ut(z-1) dz dz, sumB the running sum of B
+  double aR[2] = {0, 0}, aI[2] = {0, 0}, bR[2], bI[2], tR[2] = {0, 0}, tI[2] = {0, 0};
+  {
+    const cplx<T> br = BR[mcol], bi = BI[mcol];
+    bR[0] = to64<T>(br.x) - mR[0]; bR[1] = to64<T>(br.y) - mR[1];
+    bI[0] = to64<T>(bi.x) - mI[0]; bI[1] = to64<T>(bi.y) - mI[1];
+    BR[mcol] = mk<T>(from64<T>(bR[0]), from64<T>(bR[1]));
+    BI[mcol] = mk<T>(from64<T>(bI[0]), from64<T>(bI[1]));
+    AR[mcol] = mk<T>(0, 0); AI[mcol] = mk<T>(0, 0);
+  }
+  for (int z = 1; z < n3; ++z) {
+    const long long m = z * g.plane + mcol;
+    const double c = r2[z - 1];
+    for (int k = 0; k < 2; ++k) {
+      aR[k] = aR[k] + bR[k] * c * dz * dz;
+      aI[k] = aI[k] + bI[k] * c * dz * dz;
+      tR[k] += aR[k];
+      tI[k] += aI[k];
+    }
+    AR[m] = mk<T>(from64<T>(aR[0]), from64<T>(aR[1]));
+    AI[m] = mk<T>(from64<T>(aI[0]), from64<T>(aI[1]));
+    const cplx<T> br = BR[m], bi = BI[m];
+    const double nbR[2] = {to64<T>(br.x) - mR[0], to64<T>(br.y) - mR[1]};
+    const double nbI[2] = {to64<T>(bi.x) - mI[0], to64<T>(bi.y) - mI[1]};
+    BR[m] = mk<T>(from64<T>(nbR[0]), from64<T>(nbR[1]));
+    BI[m] = mk<T>(from64<T>(nbI[0]), from64<T>(nbI[1]));
+    for (int k = 0; k < 2; ++k) { bR[k] += nbR[k]; bI[k] += nbI[k]; }
+  }
+  // A = A~ + (sigma - sum A~)/n3
+  const double cR[2] = {(s1[0] - tR[0]) / n3, (s1[1] - tR[1]) / n3};
+  const double cI[2] = {(s2[0] - tI[0]) / n3, (s2[1] - tI[1]) / n3};
+  for (int z = 0; z < n3; ++z) {
+    const long long m = z * g.plane + mcol;
+    const cplx<T> a = AR[m], b = AI[m];
+    AR[m] = mk<T>(from64<T>(to64<T>(a.x) + cR[0]), from64<T>(to64<T>(a.y) + cR[1]));
+    AI[m] = mk<T>(from64<T>(to64<T>(b.x) + cI[0]), from64<T>(to64<T>(b.y) + cI[1]));
   }
 }
 

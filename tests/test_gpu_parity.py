@@ -152,7 +152,7 @@ def test_c0_mixed_100_steps():
 
 @pytest.mark.parametrize("flags", [
     {"linear": 1}, {"no_feedback": 1}, {"fixed_flow": 1}, {"passive_scalar": 1}, {"no_dispersion": 1},
-    {"inviscid": 0, "nuz": 3e-4},
+    {"inviscid": 0, "nuz": 3e-4}, {"ybj_plus": 0}, {"ybj_plus": 0, "linear": 1},
 ])
 def test_physics_switches(flags):
     rc = scaled(CONFIGS["c0"], 32, 8)
@@ -294,8 +294,8 @@ def test_error_statuses():
         Simulation(dict(p, a_ell_ut=-np.ones(8)), "fp64")
     assert e.value.status == QG_ERR_PIVOT
     with pytest.raises(QgError) as e:
-        Simulation(p, "fp64", flags={"ybj_plus": 0})
-    assert e.value.status == QG_ERR_UNSUPPORTED
+        Simulation(p, "fp64", flags={"ybj_plus": 2})
+    assert e.value.status == QG_ERR_ARG
     sim = Simulation(p, "fp64")
     with pytest.raises(QgError) as e:
         sim.set_state("CR", np.zeros((8, 32, 17), complex))

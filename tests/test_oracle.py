@@ -360,3 +360,31 @@ def test_omega_equation_inverts_its_operator(strat):
     got = m.omega_equation(rhs)
     assert rel_l2(got, w) < 1e-11
     assert np.abs(got[-1]).max() == 0
+
+
+# --- regular YBJ (ybj_plus = 0) ----------------------------------------------------
+def test_compute_A_inverts_the_regular_ybj_operator():
+    """compute_A (derivatives.f90:1141-1264) returns A with
+    d/dz (A_z / N^2) = B on the interior levels (discretely) and vertical
+    mean sigma/n3, for B of zero vertical mean (as sumB leaves it)."""
+    m, s, ic, p = small_model(16, 10, "exponential", ybj_plus=0)
+    n3, dz = m.p.n3, m.p.dz
+    r2 = np.asarray(m.p.r_2ut)
+    sel = m.Lb & (m.grid.kh2 > 0)
+    B = random_masked(16, n3, 7) * sel
+    B = B - B.mean(axis=0)
+    sigma = random_masked(16, 1, 8)[0] * sel
+    A, C = m.compute_A(B, sigma)
+    for iz in range(1, n3 - 1):
+        lhs = (A[iz + 1] - A[iz]) / (dz * dz * r2[iz]) - (A[iz] - A[iz - 1]) / (dz * dz * r2[iz - 1])
+        assert np.allclose(np.where(sel, lhs, 0), B[iz], rtol=0, atol=1e-9 * np.abs(B).max())
+    assert np.allclose(A.sum(axis=0), sigma, atol=1e-12 * max(1.0, np.abs(sigma).max()))
+    assert np.abs(A[:, ~sel]).max() == 0
+
+
+def test_regular_ybj_step_keeps_zero_vertical_mean_of_B():
+    m, s, ic, p = small_model(16, 8, ybj_plus=0)
+    s = m.run(s, 3, first=True)
+    sel = m.Lb & (m.grid.kh2 > 0)
+    assert np.abs(s.BR.sum(axis=0)[sel]).max() < 1e-13 * max(1.0, np.abs(s.BR).max())
+    assert np.isfinite(s.AR).all() and np.abs(s.AR).max() > 0
