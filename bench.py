@@ -369,6 +369,23 @@ def run_ensemble(args, world, rank, local):
     ens = qgybj.Ensemble(params, "mixed", local, levels_per_batch=lpb)
     for sim, ic in zip(ens.members, ics):
         init(sim, ic)
+    # concurrent member chains of the step graph: timed choice among a few
+    stream0 = torch.cuda.ExternalStream(ens.stream(), device=dev)
+    lane_ms = {}
+    for lanes in (1, 2, 4, 8, 16, 32, 64):
+        ens.set_lanes(lanes)
+        ens.step(2, True)
+        ens.synchronize()
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(stream0)
+        ens.step(5, False)
+        a1.record(stream0)
+        ens.synchronize()
+        lane_ms[lanes] = a0.elapsed_time(a1) / 5
+    best_lanes = min(lane_ms, key=lane_ms.get)
+    ens.set_lanes(best_lanes)
+    for sim, ic in zip(ens.members, ics):
+        init(sim, ic)
     ens.step(args.warmup, True)
     ens.synchronize()
     stream = torch.cuda.ExternalStream(ens.stream(), device=dev)
@@ -417,6 +434,7 @@ def run_ensemble(args, world, rank, local):
                              for (n, n3) in tuned},
                    "levels_per_batch": {f"{n}x{n}x{n3}": t["levels_per_batch"] for (n, n3), t in tuned.items()},
                    "precision": "mixed", "parallelism": f"replicas{world}"},
+        "lanes": best_lanes, "lanes_ms_per_step": lane_ms,
         "sequential_value": cells * args.steps / (seq_ms / 1e3),
         "ensemble_over_sequential": seq_ms / (ms / world),
         "gpu_launches": launches * args.steps, "clocks": clk, "e2e": None,

@@ -246,6 +246,11 @@ int qg_ensemble_member(qg_ensemble* e, int member, qg_handle** h);
 /* nsteps steps of every member (the first forward Euler when euler_first=1);
  * asynchronous, like qg_steps_async. */
 int qg_ensemble_step(qg_ensemble* e, int nsteps, int euler_first);
+/* Number of member chains the step graph runs concurrently (default 8; 1
+ * runs the members one after another).  Members are dealt to the chains
+ * largest first, each to the chain with the fewest cells so far.  Drops the
+ * captured graphs; results do not depend on it. */
+int qg_ensemble_set_lanes(qg_ensemble* e, int lanes);
 int qg_ensemble_synchronize(qg_ensemble* e);
 int qg_ensemble_get_stream(qg_ensemble* e, void** stream);
 int qg_ensemble_destroy(qg_ensemble* e);

@@ -411,9 +411,11 @@ int qg_A_solver_ybj_plus(qg_handle* h, const double* bk, double* ak, double* ck)
 // ---- ensembles ----------------------------------------------------------------
 struct qg_ensemble {
   std::vector<qg_handle*> members;
+  std::vector<long long> cells;       // n1*n2*n3 of each member (lane balancing)
   cudaStream_t master = nullptr;
   cudaEvent_t fork = nullptr;
   std::vector<cudaEvent_t> join;
+  int lanes = 8;                      // concurrent chains of members in the step graph
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
   std::string err;
 };
@@ -458,6 +460,7 @@ int qg_ensemble_create(const qg_config* cfgs, int nmembers, qg_ensemble** out) {
       return fail(nullptr, rc, msg);
     }
     e->members.push_back(h);
+    e->cells.push_back((long long)cfgs[m].n1 * cfgs[m].n2 * cfgs[m].n3);
   }
   if (cudaSetDevice(cfgs[0].device) != cudaSuccess || cudaStreamCreateWithFlags(&e->master, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming) != cudaSuccess) {
@@ -476,24 +479,40 @@ int qg_ensemble_member(qg_ensemble* e, int member, qg_handle** h) {
   return QG_OK;
 }
 
+// One step of every member as one graph: members are dealt to `lanes`
+// chains (largest first, each to the lane with the fewest cells so far);
+// the chains run concurrently, the members of a chain one after another,
+// which bounds how many members' scratch planes compete for L2 at once.
 static int ens_capture(qg_ensemble* e, int euler) {
   cudaGraph_t graph = nullptr;
+  const int nm = (int)e->members.size();
+  const int L = std::max(1, std::min(e->lanes, nm));
+  std::vector<int> order(nm);
+  for (int m = 0; m < nm; ++m) order[m] = m;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return e->cells[a] > e->cells[b]; });
+  std::vector<long long> load(L, 0);
+  std::vector<int> tail(L, -1);       // last member of each lane (-1: the fork)
   ENS_CK(cudaStreamBeginCapture(e->master, cudaStreamCaptureModeThreadLocal));
   int rc = QG_OK;
-  for (size_t m = 0; m < e->members.size() && !rc; ++m) {
+  if (cudaEventRecord(e->fork, e->master) != cudaSuccess) { rc = QG_ERR_CUDA; e->err = "ensemble fork failed"; }
+  for (int k = 0; k < nm && !rc; ++k) {
+    const int m = order[k];
+    int lane = 0;
+    for (int l = 1; l < L; ++l) if (load[l] < load[lane]) lane = l;
     cudaStream_t ms = (cudaStream_t)e->members[m]->eng->stream();
-    if (cudaEventRecord(e->fork, e->master) != cudaSuccess || cudaStreamWaitEvent(ms, e->fork, 0) != cudaSuccess) {
-      rc = QG_ERR_CUDA;
-      e->err = "ensemble fork failed";
-      break;
-    }
+    cudaEvent_t dep = tail[lane] < 0 ? e->fork : e->join[tail[lane]];
+    if (cudaStreamWaitEvent(ms, dep, 0) != cudaSuccess) { rc = QG_ERR_CUDA; e->err = "ensemble fork failed"; break; }
     rc = e->members[m]->eng->enqueue(euler);
     if (rc) { e->err = "member " + std::to_string(m) + ": " + e->members[m]->eng->err; break; }
-    if (cudaEventRecord(e->join[m], ms) != cudaSuccess || cudaStreamWaitEvent(e->master, e->join[m], 0) != cudaSuccess) {
+    if (cudaEventRecord(e->join[m], ms) != cudaSuccess) { rc = QG_ERR_CUDA; e->err = "ensemble join failed"; break; }
+    tail[lane] = m;
+    load[lane] += e->cells[m];
+  }
+  for (int l = 0; l < L && !rc; ++l)
+    if (tail[l] >= 0 && cudaStreamWaitEvent(e->master, e->join[tail[l]], 0) != cudaSuccess) {
       rc = QG_ERR_CUDA;
       e->err = "ensemble join failed";
     }
-  }
   cudaError_t ce = cudaStreamEndCapture(e->master, &graph);
   if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
   if (ce != cudaSuccess) return ens_fail(e, QG_ERR_CUDA, std::string("ensemble capture: ") + cudaGetErrorString(ce));
@@ -514,6 +533,15 @@ int qg_ensemble_step(qg_ensemble* e, int nsteps, int euler_first) {
     }
     ENS_CK(cudaGraphLaunch(e->gexec[k], e->master));
   }
+  return QG_OK;
+}
+
+int qg_ensemble_set_lanes(qg_ensemble* e, int lanes) {
+  if (!e || lanes < 1) return ens_fail(e, QG_ERR_ARG, "qg_ensemble_set_lanes: lanes must be >= 1");
+  ENS_CK(cudaStreamSynchronize(e->master));
+  for (auto& x : e->gexec)
+    if (x) { cudaGraphExecDestroy(x); x = nullptr; }
+  e->lanes = lanes;
   return QG_OK;
 }
 

@@ -27,7 +27,7 @@ EXPORTS = (
     "qg_ensemble_create", "qg_ensemble_member", "qg_ensemble_step", "qg_ensemble_synchronize",
     "qg_ensemble_get_stream", "qg_ensemble_destroy", "qg_ensemble_last_error", "qg_autotune",
     "qg_adjoint_run", "qg_adjoint_step", "qg_dump_psi", "qg_dump_la",
-    "qg_omega_eqn_rhs", "qg_omega_equation", "qg_omega",
+    "qg_omega_eqn_rhs", "qg_omega_equation", "qg_omega", "qg_ensemble_set_lanes",
 )
 KERNEL_CLASSES = ("dissipation", "col_inv", "row_main", "col_update", "row_qw", "col_qw", "solve")
 
@@ -106,6 +106,7 @@ def lib() -> C.CDLL:
         "qg_omega_eqn_rhs": (ip, [vp, vp, vp]),
         "qg_omega_equation": (ip, [vp, vp, vp]),
         "qg_omega": (ip, [vp, vp]),
+        "qg_ensemble_set_lanes": (ip, [vp, ip]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

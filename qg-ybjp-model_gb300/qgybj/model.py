@@ -320,6 +320,10 @@ class Ensemble:
     def step(self, nsteps: int = 1, euler_first: bool = False):
         self._ck(lib().qg_ensemble_step(self.e, int(nsteps), int(euler_first)))
 
+    def set_lanes(self, lanes: int):
+        """Member chains the step graph runs concurrently (qg_ensemble_set_lanes)."""
+        self._ck(lib().qg_ensemble_set_lanes(self.e, int(lanes)))
+
     def synchronize(self):
         self._ck(lib().qg_ensemble_synchronize(self.e))
 

@@ -321,7 +321,13 @@ def test_ensemble_members_match_standalone_runs():
     for sim, ic in zip(ens.members, ics):
         sim.set_state("psi", ic.psi); sim.set_state("BR", ic.BR); sim.set_state("BI", ic.BI)
         sim.init_state(True, True)
-    ens.step(5, euler_first=True)
+    # steps with different numbers of concurrent member chains
+    ens.set_lanes(1)
+    ens.step(2, euler_first=True)
+    ens.set_lanes(2)
+    ens.step(2)
+    ens.set_lanes(8)
+    ens.step(1)
     ens.synchronize()
     for sim, p, ic in zip(ens.members, params, ics):
         alone = Simulation(p, "mixed")
