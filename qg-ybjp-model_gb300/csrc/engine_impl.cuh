@@ -120,6 +120,12 @@ class Engine : public EngineBase {
     need_qw = (!cfg.fixed_flow && !cfg.no_feedback);
     int r0 = set_smem_attrs();
     if (r0) return r0;
+    // forward values of the column solves; without this scratch the solves
+    // checkpoint and recompute instead (k_solve)
+    if (kSolveStore && cudaMalloc(&vbuf, (size_t)6 * g.n3 * g.plane * sizeof(double)) != cudaSuccess) {
+      vbuf = nullptr;
+      (void)cudaGetLastError();
+    }
     QG_CK(cudaStreamSynchronize(st));
     return QG_OK;
   }
@@ -465,7 +471,7 @@ class Engine : public EngineBase {
   C* tw = nullptr;
   int* tab_idx = nullptr;
   double4 *fac_psi = nullptr, *fac_A = nullptr;
-  double2* bscr = nullptr;
+  double* vbuf = nullptr;    // forward values of the column solves (k_solve_st)
   double *du = nullptr, *cu = nullptr, *cl = nullptr, *r2 = nullptr;
   double *diag_part = nullptr, *diag_out = nullptr, *diag_host = nullptr;
   double *om_t1 = nullptr, *om_du = nullptr, *om_dl = nullptr, *om_a = nullptr, *om_scr = nullptr;
@@ -488,7 +494,7 @@ class Engine : public EngineBase {
     if (st) cudaStreamSynchronize(st);
     for (auto& x : gexec) if (x) { cudaGraphExecDestroy(x); x = nullptr; }
     for (auto& p : F) if (p) { cudaFree(p); p = nullptr; }
-    void* ps[] = {e1, e2, e1w, e2w, tw, tab_idx, fac_psi, fac_A, bscr, du, cu, cl, r2, diag_part, diag_out, S, stage,
+    void* ps[] = {e1, e2, e1w, e2w, tw, tab_idx, fac_psi, fac_A, vbuf, du, cu, cl, r2, diag_part, diag_out, S, stage,
                   W, dstage, psi64, om_t1, om_du, om_dl, om_a, om_scr, sig[0], sig[1]};
     for (void* p : ps) if (p) cudaFree(p);
     for (auto& p : D) if (p) cudaFree(p);
@@ -664,6 +670,12 @@ class Engine : public EngineBase {
 
   int solve_generic(const C* qs, const C* br, const C* bi, C* psi, C* ar, C* ai, int do_psi, int do_A) {
     if (!do_psi && !do_A) return QG_OK;
+    if (kSolveStore && vbuf) {
+      k_solve_st<T><<<(unsigned)((g.plane + kSolveTC - 1) / kSolveTC), kSolveThreads, (size_t)g.n3 * 8, st>>>(
+          g, cfg.dz, cfg.Bu, tab_idx, fac_psi, fac_A, du, qs, br, bi, psi, ar, ai, do_psi, do_A, vbuf);
+      QG_LAUNCHED();
+      return QG_OK;
+    }
     k_solve<T><<<(unsigned)((g.plane + kSolveTC - 1) / kSolveTC), kSolveThreads, solve_smem(g.n3), st>>>(g, cfg.dz, cfg.Bu, tab_idx, fac_psi, fac_A,
                                                                            du, qs, br, bi, psi, ar, ai, do_psi, do_A);
     QG_LAUNCHED();

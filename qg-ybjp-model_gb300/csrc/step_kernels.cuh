@@ -636,7 +636,8 @@ template <> __device__ __forceinline__ float from64<float>(double v) { return f6
 // columns.  The forward sweep keeps only a checkpoint every kSeg levels (in
 // shared memory); the back substitution recomputes each kSeg-level segment
 // from its checkpoint in registers and then substitutes through it.  One
-// extra FMA per level buys a kernel with no scratch traffic and many warps.
+// extra FMA per level buys a kernel with no scratch memory: the engine uses
+// it when the scratch of k_solve_st (below) cannot be allocated.
 constexpr int kSeg = 8;
 constexpr int kMaxN3 = 1024;      // checkpoints + upper diagonal fit in shared memory up to here
 constexpr int kSolveTC = 32;
@@ -718,6 +719,87 @@ k_solve(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
     for (int k = 0; k < S; ++k) {
       if (j * S + k < n3) xc = fwd(xc, fprev[k], r[k]);
       v[k] = xc;
+    }
+#pragma unroll
+    for (int k = S - 1; k >= 0; --k) {
+      const int i = j * S + k;
+      if (i < n3) {
+        if (i == n3 - 1) xn = EXACT ? __ddiv_rn(v[k], fl[k].y) : fl[k].y * v[k];
+        else if (EXACT) xn = __ddiv_rn(__dsub_rn(v[k], __dmul_rn(du_s[i], xn)), fl[k].y);
+        else xn = fma(-fl[k].z, xn, fl[k].y * v[k]);
+        out[2 * (i * P + m)] = from64<T>(xn);
+      }
+    }
+  }
+}
+
+// The same recurrences with every forward value kept in global scratch
+// (vbuf: 6 chains x n3 x plane doubles) instead of checkpoints plus
+// recomputation: one FMA per level less on the FP64 pipe, the values
+// round-trip through memory (coalesced: a warp covers 32 consecutive
+// columns of one chain).  Same arithmetic, bitwise the same results.
+constexpr bool kSolveStore = true;
+template <typename T>
+__global__ void __launch_bounds__(kSolveThreads, 4)
+k_solve_st(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
+           const double4* __restrict__ fac_psi, const double4* __restrict__ fac_A, const double* __restrict__ du,
+           const cplx<T>* __restrict__ qs, const cplx<T>* __restrict__ BR, const cplx<T>* __restrict__ BI,
+           cplx<T>* __restrict__ psi, cplx<T>* __restrict__ AR, cplx<T>* __restrict__ AI,
+           int do_psi, int do_A, double* __restrict__ vbuf) {
+  constexpr bool EXACT = sizeof(T) == 8;
+  constexpr int TC = kSolveTC, S = kSeg;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n3 = g.n3;
+  double* du_s = reinterpret_cast<double*>(smem_raw);
+  for (int i = threadIdx.x; i < n3; i += kSolveThreads) du_s[i] = du[i];
+  __syncthreads();
+  const int chain = threadIdx.x / TC, c = threadIdx.x % TC;
+  const int rhs_id = chain >> 1, part = chain & 1;
+  if (rhs_id == 0 ? !do_psi : !do_A) return;
+  const long long m = (long long)blockIdx.x * TC + c;
+  if (m >= g.plane) return;
+  const int kx = (int)(m % g.KXP);
+  if (kx > g.K) return;
+  const long long P = g.plane;
+  const T* rhs = reinterpret_cast<const T*>(rhs_id == 0 ? qs : (rhs_id == 1 ? BR : BI)) + part;
+  T* out = reinterpret_cast<T*>(rhs_id == 0 ? psi : (rhs_id == 1 ? AR : AI)) + part;
+  const int idx = tab_idx[m];
+  if (idx < 0) {
+    for (int i = 0; i < n3; ++i) out[2 * (i * P + m)] = (T)0;
+    return;
+  }
+  const double4* F = (rhs_id == 0 ? fac_psi : fac_A) + (long long)idx * n3;
+  const double s = rhs_id == 0 ? __dmul_rn(dz, dz) : __dmul_rn(__dmul_rn(dz, dz), Bu);
+  double* vb = vbuf + (long long)chain * n3 * P + m;
+  auto fwd = [&](double x, double f, T r) -> double {
+    return EXACT ? __dsub_rn(__dmul_rn(s, to64<T>(r)), __dmul_rn(f, x)) : fma(-f, x, to64<T>(r));
+  };
+  const int nseg = (n3 + S - 1) / S;
+  double x = 0.0;
+  for (int j = 0; j < nseg; ++j) {
+    T r[S];
+    double f[S];
+#pragma unroll
+    for (int k = 0; k < S; ++k) {
+      const int i = j * S + k;
+      r[k] = i < n3 ? rhs[2 * (i * P + m)] : (T)0;
+      f[k] = (i > 0 && i < n3) ? F[i - 1].x : 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < S; ++k) {
+      const int i = j * S + k;
+      if (i < n3) { x = fwd(x, f[k], r[k]); vb[(long long)i * P] = x; }
+    }
+  }
+  double xn = 0.0;
+  for (int j = nseg - 1; j >= 0; --j) {
+    double v[S];
+    double4 fl[S];
+#pragma unroll
+    for (int k = 0; k < S; ++k) {
+      const int i = j * S + k;
+      v[k] = i < n3 ? vb[(long long)i * P] : 0.0;
+      fl[k] = i < n3 ? F[i] : make_double4(0, 1, 0, 0);
     }
 #pragma unroll
     for (int k = S - 1; k >= 0; --k) {
