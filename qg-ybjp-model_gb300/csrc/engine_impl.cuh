@@ -160,17 +160,22 @@ class Engine : public EngineBase {
     if (f < 0 || field == QG_CR || field == QG_CI || field == QG_QSTAR) { err = "field is read-only or unknown"; return QG_ERR_ARG; }
     if (!kvar || level0 < 0 || nlev <= 0 || level0 + nlev > g.n3) { err = "bad level range or null pointer"; return QG_ERR_ARG; }
     const size_t bytes = (size_t)nlev * g.n * (g.n / 2 + 1) * sizeof(double2);
-    int rc = ensure(&stage, &stage_bytes, bytes);
-    if (rc) return rc;
-    QG_CK(cudaMemcpyAsync(stage, kvar, bytes, cudaMemcpyDefault, st));
-    k_dense_to_compact<T><<<grid_for((long long)nlev * g.plane), 256, 0, st>>>(g, level0, nlev, (const double2*)stage, F[f]);
+    // pinned host or device arrays are read in place (only the retained
+    // modes cross the link); others go through a device staging copy
+    const double2* src = static_cast<const double2*>(device_view(kvar));
+    if (!src) {
+      int rc = ensure(&stage, &stage_bytes, bytes);
+      if (rc) return rc;
+      QG_CK(cudaMemcpyAsync(stage, kvar, bytes, cudaMemcpyDefault, st));
+      src = (const double2*)stage;
+    }
+    k_dense_to_compact<T><<<grid_for((long long)nlev * g.plane), 256, 0, st>>>(g, level0, nlev, src, F[f]);
     QG_LAUNCHED();
     if (f == F_PSI && sizeof(T) == 4) {
       // mixed path: keep psi in FP64 until qg_init_state has built q from it
       // (init_q's vertical second difference would amplify FP32 rounding)
       if (!psi64) QG_CK(cudaMalloc(&psi64, (size_t)g.n3 * g.plane * sizeof(double2)));
-      k_dense_to_compact<double><<<grid_for((long long)nlev * g.plane), 256, 0, st>>>(g, level0, nlev,
-                                                                                      (const double2*)stage, psi64);
+      k_dense_to_compact<double><<<grid_for((long long)nlev * g.plane), 256, 0, st>>>(g, level0, nlev, src, psi64);
       QG_LAUNCHED();
     }
     QG_CK(cudaStreamSynchronize(st));
@@ -184,14 +189,28 @@ class Engine : public EngineBase {
     if (field == QG_QSTAR && !need_qw) f = F_Q;
     const int mode = (field == QG_CR || field == QG_CI) ? 1 : 0;
     const size_t bytes = (size_t)nlev * g.n * (g.n / 2 + 1) * sizeof(double2);
-    int rc = ensure(&stage, &stage_bytes, bytes);
-    if (rc) return rc;
-    k_compact_to_dense<T><<<grid_for((long long)nlev * g.n * (g.n / 2 + 1)), 256, 0, st>>>(g, level0, nlev, F[f],
-                                                                                          (double2*)stage, mode, cfg.dz);
+    double2* dst = static_cast<double2*>(const_cast<void*>(device_view(kvar)));
+    if (!dst) {
+      int rc = ensure(&stage, &stage_bytes, bytes);
+      if (rc) return rc;
+    }
+    k_compact_to_dense<T><<<grid_for((long long)nlev * g.n * (g.n / 2 + 1)), 256, 0, st>>>(
+        g, level0, nlev, F[f], dst ? dst : (double2*)stage, mode, cfg.dz);
     QG_LAUNCHED();
-    QG_CK(cudaMemcpyAsync(kvar, stage, bytes, cudaMemcpyDefault, st));
+    if (!dst) QG_CK(cudaMemcpyAsync(kvar, stage, bytes, cudaMemcpyDefault, st));
     QG_CK(cudaStreamSynchronize(st));
     return QG_OK;
+  }
+
+  // Device address through which kernels may access p: device memory as is,
+  // page-locked host memory through its mapping; nullptr for anything else
+  // (pageable or managed memory is staged through a copy instead).
+  static const void* device_view(const void* p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) { (void)cudaGetLastError(); return nullptr; }
+    if (at.type == cudaMemoryTypeDevice) return p;
+    if (at.type == cudaMemoryTypeHost && at.devicePointer) return at.devicePointer;
+    return nullptr;
   }
 
   int init_state(int apply_sumB, int q_from_psi) override {
