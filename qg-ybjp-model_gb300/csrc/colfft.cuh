@@ -162,4 +162,32 @@ __device__ __forceinline__ void col_fft(cplx<T>* __restrict__ sm, const cplx<T>*
   }
 }
 
+// First Stockham pass (NS = 1) of NF*RT row transforms stored [f][rr][LD]
+// with element i at pad_idx(i), inputs from registers: pro(rr, j, v) fills
+// v[f][r] with the input at index j + r*N/R0.  Threads take tasks (rr, j)
+// with j fastest (coalesced row reads).  The remaining passes are
+// ip_passes<..., radix_of(N)> after a barrier.
+template <typename T, int N, bool FWD, int NF, int RT, int NT, int LD, class Pro>
+__device__ __forceinline__ void row_pass0(cplx<T>* __restrict__ sm, Pro pro) {
+  constexpr int R = radix_of(N);
+  constexpr int NB = N / R;
+  constexpr int TASKS = RT * NB;
+  constexpr int PER = (TASKS + NT - 1) / NT;
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int t = threadIdx.x + p * NT;
+    if ((TASKS % NT) == 0 || t < TASKS) {
+      const int j = t % NB, rr = t / NB;
+      cplx<T> v[NF][R];
+      pro(rr, j, v);
+#pragma unroll
+      for (int f = 0; f < NF; ++f) {
+        dftR<T, R, FWD>(v[f]);
+#pragma unroll
+        for (int r = 0; r < R; ++r) sm[(f * RT + rr) * LD + pad_idx(j * R + r)] = v[f][r];
+      }
+    }
+  }
+}
+
 }  // namespace qg

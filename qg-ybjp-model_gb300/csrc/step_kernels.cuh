@@ -44,6 +44,7 @@ __device__ __forceinline__ void realit_col(cplx<T>* col, int n) {
 constexpr int kRowMinB = 4;        // k_row_main, k_row_qw
 constexpr int kColInvMinB = 2;     // k_col_inv
 constexpr int kColQwMinB = 4;      // k_col_qw
+constexpr bool kRowPass0 = true;   // row kernels: first inverse pass fed from registers
 __host__ __device__ constexpr int smem_ctas(int bytes) {
   return 233472 / (bytes + 1024) >= 4 ? 4 : (233472 / (bytes + 1024) >= 1 ? 233472 / (bytes + 1024) : 1);
 }
@@ -209,16 +210,32 @@ k_row_main(Geom g, StepParams sp, cplx<T>* __restrict__ S, const cplx<T>* __rest
   const int y0 = blockIdx.x * RT;
   const int K = g.K;
   load_tw<T, N>(tw, twg, NT);
+  if constexpr (kRowPass0) {
+    constexpr int R0 = radix_of(N), NB0 = N / R0;
+    row_pass0<T, N, false, 3, RT, NT, LD>(bA, [&](int rr, int j, cplx<T> (&v)[3][R0]) {
+      const int y = y0 + rr;
+#pragma unroll
+      for (int p = 0; p < 3; ++p) {
+        const cplx<T>* X = S + scr_off(zb, 2 * p, y, N, g.KXP);
+        const cplx<T>* Y = S + scr_off(zb, 2 * p + 1, y, N, g.KXP);
+#pragma unroll
+        for (int r = 0; r < R0; ++r) v[p][r] = pack_spec<T>(X, Y, j + r * NB0, N, K);
+      }
+    });
+    __syncthreads();
+    ip_passes<T, N, false, 3 * RT, NT, LD, radix_of(N)>(bA, tw);
+  } else {
 #pragma unroll 4
-  for (int e = tid; e < 3 * RT * N; e += NT) {
-    const int k = e % N, p = (e / N) % 3, rr = e / (3 * N);
-    const int y = y0 + rr;
-    const cplx<T>* X = S + scr_off(zb, 2 * p, y, N, g.KXP);
-    const cplx<T>* Y = S + scr_off(zb, 2 * p + 1, y, N, g.KXP);
-    bA[(p * RT + rr) * LD + pad_idx(k)] = pack_spec<T>(X, Y, k, N, K);
+    for (int e = tid; e < 3 * RT * N; e += NT) {
+      const int k = e % N, p = (e / N) % 3, rr = e / (3 * N);
+      const int y = y0 + rr;
+      const cplx<T>* X = S + scr_off(zb, 2 * p, y, N, g.KXP);
+      const cplx<T>* Y = S + scr_off(zb, 2 * p + 1, y, N, g.KXP);
+      bA[(p * RT + rr) * LD + pad_idx(k)] = pack_spec<T>(X, Y, k, N, K);
+    }
+    __syncthreads();
+    fft_ip<T, N, false, 3 * RT, NT, LD>(bA, tw);
   }
-  __syncthreads();
-  fft_ip<T, N, false, 3 * RT, NT, LD>(bA, tw);
   // products: (u q, v q), (u br, v br), (u bi, v bi), (zeta br, zeta bi)
 #pragma unroll 4
   for (int e = tid; e < RT * N; e += NT) {
@@ -465,30 +482,38 @@ k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
   const int K = g.K;
   load_tw<T, N>(tw, twg, NT);
   // packed: (BR, BI), (BRx, BIx), (BRy, BIy)
-#pragma unroll 4
-  for (int e = tid; e < 3 * RT * N; e += NT) {
-    const int k = e % N, p = (e / N) % 3, rr = e / (3 * N);
+  auto packed = [&](int p, int rr, int k) -> cplx<T> {
     const int y = y0 + rr;
     const cplx<T>* sBR = S + scr_off(zb, 0, y, N, g.KXP);
     const cplx<T>* sBRy = S + scr_off(zb, 1, y, N, g.KXP);
     const cplx<T>* sBI = S + scr_off(zb, 2, y, N, g.KXP);
     const cplx<T>* sBIy = S + scr_off(zb, 3, y, N, g.KXP);
-    cplx<T> v;
-    if (p == 0) {
-      v = pack_spec<T>(sBR, sBI, k, N, K);
-    } else if (p == 2) {
-      v = pack_spec<T>(sBRy, sBIy, k, N, K);
-    } else if (k == 0 || (k > K && k < N - K)) {
-      v = mk<T>(0, 0);      // x-derivatives vanish at kx = 0
-    } else {
-      const int kk = k <= K ? k : N - k;
-      const cplx<T> a = cscale(cmul_i(sBR[kk]), (T)kk), b = cscale(cmul_i(sBI[kk]), (T)kk);
-      v = k <= K ? mk<T>(a.x - b.y, a.y + b.x) : mk<T>(a.x + b.y, b.x - a.y);
+    if (p == 0) return pack_spec<T>(sBR, sBI, k, N, K);
+    if (p == 2) return pack_spec<T>(sBRy, sBIy, k, N, K);
+    if (k == 0 || (k > K && k < N - K)) return mk<T>(0, 0);      // x-derivatives vanish at kx = 0
+    const int kk = k <= K ? k : N - k;
+    const cplx<T> a = cscale(cmul_i(sBR[kk]), (T)kk), b = cscale(cmul_i(sBI[kk]), (T)kk);
+    return k <= K ? mk<T>(a.x - b.y, a.y + b.x) : mk<T>(a.x + b.y, b.x - a.y);
+  };
+  if constexpr (kRowPass0) {
+    constexpr int R0 = radix_of(N), NB0 = N / R0;
+    row_pass0<T, N, false, 3, RT, NT, LD>(bA, [&](int rr, int j, cplx<T> (&v)[3][R0]) {
+#pragma unroll
+      for (int p = 0; p < 3; ++p)
+#pragma unroll
+        for (int r = 0; r < R0; ++r) v[p][r] = packed(p, rr, j + r * NB0);
+    });
+    __syncthreads();
+    ip_passes<T, N, false, 3 * RT, NT, LD, radix_of(N)>(bA, tw);
+  } else {
+#pragma unroll 4
+    for (int e = tid; e < 3 * RT * N; e += NT) {
+      const int k = e % N, p = (e / N) % 3, rr = e / (3 * N);
+      bA[(p * RT + rr) * LD + pad_idx(k)] = packed(p, rr, k);
     }
-    bA[(p * RT + rr) * LD + pad_idx(k)] = v;
+    __syncthreads();
+    fft_ip<T, N, false, 3 * RT, NT, LD>(bA, tw);
   }
-  __syncthreads();
-  fft_ip<T, N, false, 3 * RT, NT, LD>(bA, tw);
 #pragma unroll 4
   for (int e = tid; e < RT * N; e += NT) {
     const int x = e % N, rr = e / N;
