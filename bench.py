@@ -39,7 +39,7 @@ FALLBACK_HBM_GBS = 6800.0
 # profiles/dram_per_launch_c2_512x512x32_mixed.md (512^2 levels, 11 levels per
 # launch: 49.5 MB).  The traffic of a launch grows with the levels it covers,
 # so the roofline entry scales it by the levels per launch of the run.
-MEASURED_TRAFFIC_PER_LEVEL = {("col_update", 512, "mixed"): 132.1e6 / 13}
+MEASURED_TRAFFIC_PER_LEVEL = {("col_update", 512, "mixed"): 121.7e6 / 13}
 
 
 # ---------------------------------------------------------------------------
