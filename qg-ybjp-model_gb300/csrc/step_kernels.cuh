@@ -42,11 +42,15 @@ __device__ __forceinline__ void realit_col(cplx<T>* col, int n) {
 // CTAs per SM the register budgets of the FP32 kernels target (FP64
 // kernels: at most 2); shared memory caps them further per shape
 constexpr int kRowMinB = 4;        // k_row_main, k_row_qw
+constexpr int kRowThreads = 256;   // threads of k_row_main, k_row_qw
+constexpr int kRowRT = 0;          // rows per CTA of k_row_main, k_row_qw (0: Tiles RT)
+constexpr int kRowQwThreads = 128; // k_row_qw: half the threads of k_row_main, twice the CTAs
+constexpr int kRowQwMinB = 5;
 constexpr int kColInvMinB = 2;     // k_col_inv
 constexpr int kColQwMinB = 4;      // k_col_qw
 constexpr bool kRowPass0 = true;   // row kernels: first inverse pass fed from registers
 __host__ __device__ constexpr int smem_ctas(int bytes) {
-  return 233472 / (bytes + 1024) >= 4 ? 4 : (233472 / (bytes + 1024) >= 1 ? 233472 / (bytes + 1024) : 1);
+  return 233472 / (bytes + 1024) >= 8 ? 8 : (233472 / (bytes + 1024) >= 1 ? 233472 / (bytes + 1024) : 1);
 }
 __host__ __device__ constexpr int imin(int a, int b) { return a < b ? a : b; }
 
@@ -71,7 +75,9 @@ template <typename T, int N> struct Tiles {
   static constexpr int mb0 = 233472 / (SM6 + 1024);
   static constexpr int MINB = mb0 >= 4 ? 4 : (mb0 >= 1 ? mb0 : 1);
   static constexpr int FSC = PadLD<N>::value * CT;   // interleaved column tile (colfft.cuh)
-  static constexpr int RMINB = imin(CB == 8 ? kRowMinB : 2, smem_ctas((N + 4 * RT * LD) * CB));
+  static constexpr int RRT = kRowRT > 0 ? kRowRT : RT;   // rows per CTA of the forward row kernels
+  static constexpr int RMINB = imin(CB == 8 ? kRowMinB : 2, smem_ctas((N + 4 * RRT * LD) * CB));
+  static constexpr int QMINB = imin(CB == 8 ? kRowQwMinB : 2, smem_ctas((N + 3 * RRT * LD) * CB));
   static constexpr int CIMINB = imin(CB == 8 ? kColInvMinB : 2, smem_ctas((N + 3 * FSC) * CB));
   static constexpr int CQMINB = imin(CB == 8 ? kColQwMinB : 2, smem_ctas((N + 2 * FSC) * CB));
 };
@@ -198,9 +204,9 @@ __device__ __forceinline__ void unpack_pad(const cplx<T>* F, int k, int n, cplx<
 // Phase A, kernel 2: rows — physical products of convol_waqg / refraction_waqg
 // ===========================================================================
 template <typename T, int N>
-__global__ void __launch_bounds__(kThreadsB, Tiles<T, N>::RMINB)
+__global__ void __launch_bounds__(kRowThreads, Tiles<T, N>::RMINB)
 k_row_main(Geom g, StepParams sp, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
-  constexpr int RT = Tiles<T, N>::RT, LD = Tiles<T, N>::LD, NT = kThreadsB;
+  constexpr int RT = Tiles<T, N>::RRT, LD = Tiles<T, N>::LD, NT = kRowThreads;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   // [4][RT][LD]: (u,v), (zeta,q), (br,bi); then, in place, the 4 products
@@ -470,9 +476,9 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
 // Phase A, kernel 4: rows — products of compute_qw
 // ===========================================================================
 template <typename T, int N>
-__global__ void __launch_bounds__(kThreadsB, Tiles<T, N>::RMINB)
+__global__ void __launch_bounds__(kRowQwThreads, Tiles<T, N>::QMINB)
 k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
-  constexpr int RT = Tiles<T, N>::RT, LD = Tiles<T, N>::LD, NT = kThreadsB;
+  constexpr int RT = Tiles<T, N>::RRT, LD = Tiles<T, N>::LD, NT = kRowQwThreads;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* bA = tw + N;               // [3][RT][LD]; then, in place, (P1, P2) in the first RT
