@@ -187,7 +187,8 @@ def run_ours(args, world, rank, local):
     precision = args.precision or rc.precision
     ic = make_initial_condition(rc)
     params = model_parameters(rc, ic.delt)
-    sim = qgybj.Simulation(params, precision, device=local, levels_per_batch=rc.levels_per_batch)
+    sim = qgybj.Simulation(params, precision, device=local, levels_per_batch=rc.levels_per_batch,
+                           solve_columns=rc.solve_columns)
     sim.set_state("psi", ic.psi)
     sim.set_state("BR", ic.BR)
     sim.set_state("BI", ic.BI)
@@ -275,7 +276,8 @@ def run_ours(args, world, rank, local):
     # FP64 GPU step on the same workload (the metric compares the two)
     fp64 = None
     if not args.no_fp64 and precision == "mixed":
-        sim64 = qgybj.Simulation(params, "fp64", device=local, levels_per_batch=CONFIGS["c1"].levels_per_batch)
+        sim64 = qgybj.Simulation(params, "fp64", device=local, levels_per_batch=CONFIGS["c1"].levels_per_batch,
+                                 solve_columns=CONFIGS["c1"].solve_columns)
         sim64.set_state("psi", ic.psi); sim64.set_state("BR", ic.BR); sim64.set_state("BI", ic.BI)
         sim64.init_state(True, True)
         sim64.steps_async(2, True)
@@ -360,13 +362,14 @@ def run_ensemble(args, world, rank, local):
         if (rc.n, rc.n3) not in tuned:
             tuned[(rc.n, rc.n3)] = qgybj.autotune(p, "mixed", local, nsteps=3)
     lpb = [tuned[(rc.n, rc.n3)]["levels_per_batch"] for rc in members]
+    stc = [tuned[(rc.n, rc.n3)]["solve_columns"] for rc in members]
     cells = sum(rc.n * rc.n * rc.n3 for rc in members)
 
     def init(sim, ic):
         sim.set_state("psi", ic.psi); sim.set_state("BR", ic.BR); sim.set_state("BI", ic.BI)
         sim.init_state(True, True)
 
-    ens = qgybj.Ensemble(params, "mixed", local, levels_per_batch=lpb)
+    ens = qgybj.Ensemble(params, "mixed", local, levels_per_batch=lpb, solve_columns=stc)
     for sim, ic in zip(ens.members, ics):
         init(sim, ic)
     # concurrent member chains of the step graph: timed choice among a few
@@ -409,8 +412,8 @@ def run_ensemble(args, world, rank, local):
     ens.close()
     # the same members one after another
     seq_ms = 0.0
-    for p, ic, l in zip(params, ics, lpb):
-        sim = qgybj.Simulation(p, "mixed", local, levels_per_batch=l)
+    for p, ic, l, tc in zip(params, ics, lpb, stc):
+        sim = qgybj.Simulation(p, "mixed", local, levels_per_batch=l, solve_columns=tc)
         init(sim, ic)
         sim.steps_async(args.warmup, True)
         sim.synchronize()
@@ -433,6 +436,7 @@ def run_ensemble(args, world, rank, local):
                    "sizes": {f"{n}x{n}x{n3}": sum(1 for rc in members if (rc.n, rc.n3) == (n, n3))
                              for (n, n3) in tuned},
                    "levels_per_batch": {f"{n}x{n}x{n3}": t["levels_per_batch"] for (n, n3), t in tuned.items()},
+                   "solve_columns": {f"{n}x{n}x{n3}": t["solve_columns"] for (n, n3), t in tuned.items()},
                    "precision": "mixed", "parallelism": f"replicas{world}"},
         "lanes": best_lanes, "lanes_ms_per_step": lane_ms,
         "sequential_value": cells * args.steps / (seq_ms / 1e3),

@@ -79,6 +79,7 @@ typedef struct qg_config {
   const double* r_2ut;     /* [n3] N^2 at za(iz), or NULL (= Bu/a_ell_ut); diagnostics */
   int levels_per_batch;    /* z levels per phase-A batch; 0 = choose automatically     */
   int use_graphs;          /* 1 = replay the step as a CUDA graph (default), 0 = launch */
+  int solve_columns;       /* columns per CTA of the column solves: 16, 32 or 64; 0 = 32 */
 } qg_config;
 
 typedef struct qg_handle qg_handle;
@@ -266,7 +267,15 @@ typedef struct qg_tuning {
   int ncandidates;           /* candidates timed (<= 16)                   */
   int candidates[16];        /* their batch depths ...                     */
   double candidate_ms[16];   /* ... and times per step                     */
+  int solve_columns;         /* fastest columns per CTA of the column solves */
+  int nsolve;                /* solve shapes timed (<= 4)                  */
+  int solve_candidates[4];   /* their columns per CTA ...                  */
+  double solve_candidate_ms[4]; /* ... and times per step                  */
 } qg_tuning;
+/* Times nsteps steps of a throw-away handle built from cfg for every
+ * candidate batch depth, then, at the fastest depth, for every block shape
+ * of the column solves (16, 32, 64 columns per CTA); returns the fastest
+ * pair (set them in qg_config.levels_per_batch / solve_columns). */
 int qg_autotune(const qg_config* cfg, int nsteps, qg_tuning* out);
 
 /* Allocation-free variant of qg_fft_c2r.  No counterpart in the reference.

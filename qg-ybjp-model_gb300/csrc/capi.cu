@@ -223,6 +223,7 @@ int qg_config_defaults(qg_config* c) {
   c->ilap1 = c->ilap1w = 2;
   c->ilap2 = c->ilap2w = 6;
   c->use_graphs = 1;
+  c->solve_columns = 0;
   return QG_OK;
 }
 
@@ -603,12 +604,35 @@ int qg_autotune(const qg_config* cfg, int nsteps, qg_tuning* out) {
     out->ncandidates++;
     if (per < best) { best = per; bestz = zeff; }
   }
+  // block shape of the column solves at the chosen batch depth
+  int best_tc = h->eng->solve_columns();
+  if (!rc) rc = h->eng->set_batch_levels(bestz);
+  for (int tc : {16, 32, 64}) {
+    if (rc) break;
+    rc = h->eng->set_solve_columns(tc);
+    if (!rc) rc = h->eng->steps_async(2, 1);
+    if (!rc) rc = h->eng->synchronize();
+    if (rc) break;
+    cudaEventRecord(a, st);
+    rc = h->eng->steps_async(nsteps, 0);
+    cudaEventRecord(b, st);
+    if (!rc) rc = h->eng->synchronize();
+    if (rc) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    const double per = ms / nsteps;
+    out->solve_candidates[out->nsolve] = tc;
+    out->solve_candidate_ms[out->nsolve] = per;
+    out->nsolve++;
+    if (per < best) { best = per; best_tc = tc; }
+  }
   std::string err = rc ? h->eng->err : "";
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   qg_destroy(h);
   if (rc) return fail(nullptr, rc, "qg_autotune: " + err);
   out->levels_per_batch = bestz;
+  out->solve_columns = best_tc;
   out->ms_per_step = best;
   return QG_OK;
 }

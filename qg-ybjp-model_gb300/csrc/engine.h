@@ -44,6 +44,9 @@ struct EngineBase {
   // levels per phase-A batch: current value and re-selection (drops graphs)
   virtual int batch_levels() const = 0;
   virtual int set_batch_levels(int zb) = 0;
+  // columns per CTA of the column solves (16, 32, 64): current value and re-selection
+  virtual int solve_columns() const = 0;
+  virtual int set_solve_columns(int tc) = 0;
   // adjoint (FP64 engines only)
   virtual int adjoint_run(const double* q0, const double* BR0, const double* BI0, int nsteps, int ckpt_every,
                           int objective, double* J, double* gq, double* gR, double* gI) {

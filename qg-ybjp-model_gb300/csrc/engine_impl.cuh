@@ -120,6 +120,11 @@ class Engine : public EngineBase {
     need_qw = (!cfg.fixed_flow && !cfg.no_feedback);
     int r0 = set_smem_attrs();
     if (r0) return r0;
+    if (cfg.solve_columns != 0 && cfg.solve_columns != 16 && cfg.solve_columns != 32 && cfg.solve_columns != 64) {
+      err = "solve_columns must be 0, 16, 32 or 64";
+      return QG_ERR_ARG;
+    }
+    solve_tc = cfg.solve_columns ? cfg.solve_columns : 32;
     // forward values of the column solves; without this scratch the solves
     // checkpoint and recompute instead (k_solve)
     if (kSolveStore && cudaMalloc(&vbuf, (size_t)6 * g.n3 * g.plane * sizeof(double)) != cudaSuccess) {
@@ -149,6 +154,16 @@ class Engine : public EngineBase {
       QG_CK(cudaMalloc(&S, (size_t)nz * per_level));
     }
     Zb = nz;
+    return QG_OK;
+  }
+
+  int solve_columns() const override { return solve_tc; }
+  int set_solve_columns(int tc) override {
+    if (tc == 0) tc = 32;
+    if (tc != 16 && tc != 32 && tc != 64) { err = "solve_columns must be 16, 32 or 64"; return QG_ERR_ARG; }
+    QG_CK(cudaStreamSynchronize(st));
+    for (auto& x : gexec) if (x) { cudaGraphExecDestroy(x); x = nullptr; }
+    solve_tc = tc;
     return QG_OK;
   }
 
@@ -491,6 +506,7 @@ class Engine : public EngineBase {
   int* tab_idx = nullptr;
   double4 *fac_psi = nullptr, *fac_A = nullptr;
   double* vbuf = nullptr;    // forward values of the column solves (k_solve_st)
+  int solve_tc = 32;         // columns per CTA of k_solve_st
   double *du = nullptr, *cu = nullptr, *cl = nullptr, *r2 = nullptr;
   double *diag_part = nullptr, *diag_out = nullptr, *diag_host = nullptr;
   double *om_t1 = nullptr, *om_du = nullptr, *om_dl = nullptr, *om_a = nullptr, *om_scr = nullptr;
@@ -691,8 +707,13 @@ class Engine : public EngineBase {
   int solve_generic(const C* qs, const C* br, const C* bi, C* psi, C* ar, C* ai, int do_psi, int do_A) {
     if (!do_psi && !do_A) return QG_OK;
     if (kSolveStore && vbuf) {
-      k_solve_st<T><<<(unsigned)((g.plane + kSolveTC - 1) / kSolveTC), kSolveThreads, (size_t)g.n3 * 8, st>>>(
-          g, cfg.dz, cfg.Bu, tab_idx, fac_psi, fac_A, du, qs, br, bi, psi, ar, ai, do_psi, do_A, vbuf);
+#define QG_SOLVE_ST(TCV)                                                                                   \
+  k_solve_st<T, TCV><<<(unsigned)((g.plane + TCV - 1) / TCV), 6 * TCV, (size_t)g.n3 * 8, st>>>(           \
+      g, cfg.dz, cfg.Bu, tab_idx, fac_psi, fac_A, du, qs, br, bi, psi, ar, ai, do_psi, do_A, vbuf)
+      if (solve_tc == 16) QG_SOLVE_ST(16);
+      else if (solve_tc == 64) QG_SOLVE_ST(64);
+      else QG_SOLVE_ST(32);
+#undef QG_SOLVE_ST
       QG_LAUNCHED();
       return QG_OK;
     }

@@ -769,20 +769,22 @@ k_solve(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
 // recomputation: one FMA per level less on the FP64 pipe, the values
 // round-trip through memory (coalesced: a warp covers 32 consecutive
 // columns of one chain).  Same arithmetic, bitwise the same results.
+// TC columns per CTA (16, 32 or 64: the block shape the autotuner picks),
+// 6*TC threads, the register budget of 4 CTAs of 192 threads.
 constexpr bool kSolveStore = true;
-template <typename T>
-__global__ void __launch_bounds__(kSolveThreads, 4)
+template <typename T, int TC>
+__global__ void __launch_bounds__(6 * TC, 128 / TC)
 k_solve_st(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
            const double4* __restrict__ fac_psi, const double4* __restrict__ fac_A, const double* __restrict__ du,
            const cplx<T>* __restrict__ qs, const cplx<T>* __restrict__ BR, const cplx<T>* __restrict__ BI,
            cplx<T>* __restrict__ psi, cplx<T>* __restrict__ AR, cplx<T>* __restrict__ AI,
            int do_psi, int do_A, double* __restrict__ vbuf) {
   constexpr bool EXACT = sizeof(T) == 8;
-  constexpr int TC = kSolveTC, S = kSeg;
+  constexpr int S = kSeg, NTH = 6 * TC;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n3 = g.n3;
   double* du_s = reinterpret_cast<double*>(smem_raw);
-  for (int i = threadIdx.x; i < n3; i += kSolveThreads) du_s[i] = du[i];
+  for (int i = threadIdx.x; i < n3; i += NTH) du_s[i] = du[i];
   __syncthreads();
   const int chain = threadIdx.x / TC, c = threadIdx.x % TC;
   const int rhs_id = chain >> 1, part = chain & 1;

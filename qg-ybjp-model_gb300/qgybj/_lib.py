@@ -44,13 +44,15 @@ class QgConfig(C.Structure):
         ("nuz", C.c_double),
         ("a_ell_ut", C.POINTER(C.c_double)), ("rho_ut", C.POINTER(C.c_double)),
         ("rho_st", C.POINTER(C.c_double)), ("r_2ut", C.POINTER(C.c_double)),
-        ("levels_per_batch", C.c_int), ("use_graphs", C.c_int),
+        ("levels_per_batch", C.c_int), ("use_graphs", C.c_int), ("solve_columns", C.c_int),
     ]
 
 
 class QgTuning(C.Structure):
     _fields_ = [("levels_per_batch", C.c_int), ("ms_per_step", C.c_double), ("ncandidates", C.c_int),
-                ("candidates", C.c_int * 16), ("candidate_ms", C.c_double * 16)]
+                ("candidates", C.c_int * 16), ("candidate_ms", C.c_double * 16),
+                ("solve_columns", C.c_int), ("nsolve", C.c_int), ("solve_candidates", C.c_int * 4),
+                ("solve_candidate_ms", C.c_double * 4)]
 
 
 class QgEnergy(C.Structure):

@@ -76,6 +76,7 @@ class RunConfig:
     ilap: int = 2
     delt: float | None = None        # derived from the CFL number when None
     levels_per_batch: int = 0
+    solve_columns: int = 0
     use_graphs: int = 1
     extra: dict = field(default_factory=dict)
 
@@ -107,11 +108,11 @@ class RunConfig:
 # 512^2x256 mixed precision, ensemble members, adjoint case)
 CONFIGS = {
     "c0": RunConfig("c0_64x64x64_fp64", 64, 64, "fp64", steps=200, seed=0, k0=3.0),
-    # levels_per_batch: the choice of qg_autotune on GB300 for these sizes
+    # levels_per_batch, solve_columns: the choices of qg_autotune on GB300 for these sizes
     "c1": RunConfig("c1_256x256x128_fp64", 256, 128, "fp64", steps=200, seed=1, k0=6.0,
-                    stratification="exponential", levels_per_batch=32),
+                    stratification="exponential", levels_per_batch=32, solve_columns=16),
     "c2": RunConfig("c2_512x512x256_mixed", 512, 256, "mixed", steps=100, seed=2, k0=8.0,
-                    stratification="exponential", levels_per_batch=13),
+                    stratification="exponential", levels_per_batch=13, solve_columns=16),
     "c4": RunConfig("c4_128x128x64_fp64", 128, 64, "fp64", steps=50, seed=4, k0=3.0),
 }
 

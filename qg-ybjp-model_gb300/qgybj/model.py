@@ -22,7 +22,7 @@ def _arr(a, n3=None):
 
 
 def make_config(params: dict, precision: str = "fp64", device: int = 0, levels_per_batch: int = 0,
-                use_graphs: int = 1, flags: dict | None = None):
+                use_graphs: int = 1, flags: dict | None = None, solve_columns: int = 0):
     """qg_config of a parameter dict; returns (config, arrays kept alive)."""
     cfg = QgConfig()
     check(lib().qg_config_defaults(C.byref(cfg)))
@@ -44,6 +44,7 @@ def make_config(params: dict, precision: str = "fp64", device: int = 0, levels_p
             setattr(cfg, k, a.ctypes.data_as(C.POINTER(C.c_double)))
     cfg.levels_per_batch = levels_per_batch
     cfg.use_graphs = use_graphs
+    cfg.solve_columns = solve_columns
     return cfg, keep
 
 
@@ -52,22 +53,24 @@ def autotune(params: dict, precision: str = "mixed", device: int = 0, nsteps: in
     cfg, keep = make_config(params, precision, device)
     t = QgTuning()
     check(lib().qg_autotune(C.byref(cfg), int(nsteps), C.byref(t)))
-    return {"levels_per_batch": t.levels_per_batch, "ms_per_step": t.ms_per_step,
-            "candidates": {t.candidates[i]: t.candidate_ms[i] for i in range(t.ncandidates)}}
+    return {"levels_per_batch": t.levels_per_batch, "solve_columns": t.solve_columns, "ms_per_step": t.ms_per_step,
+            "candidates": {t.candidates[i]: t.candidate_ms[i] for i in range(t.ncandidates)},
+            "solve_candidates": {t.solve_candidates[i]: t.solve_candidate_ms[i] for i in range(t.nsolve)}}
 
 
 class Simulation:
     def __init__(self, params: dict, precision: str = "fp64", device: int = 0, levels_per_batch: int = 0,
-                 use_graphs: int = 1, flags: dict | None = None, _handle=None):
+                 use_graphs: int = 1, flags: dict | None = None, _handle=None, solve_columns: int = 0):
         L = lib()
         self.n, self.n3 = int(params["n1"]), int(params["n3"])
         self.precision = precision
         if _handle is not None:          # a member handle owned by an Ensemble
             self.h, self._owned, self._keep = _handle, False, []
-            self.cfg, _ = make_config(params, precision, device, levels_per_batch, use_graphs, flags)
+            self.cfg, _ = make_config(params, precision, device, levels_per_batch, use_graphs, flags, solve_columns)
             return
         self._owned = True
-        self.cfg, self._keep = make_config(params, precision, device, levels_per_batch, use_graphs, flags)
+        self.cfg, self._keep = make_config(params, precision, device, levels_per_batch, use_graphs, flags,
+                                           solve_columns)
         h = C.c_void_p()
         check(L.qg_create(C.byref(self.cfg), C.byref(h)))
         self.h = h
@@ -277,6 +280,7 @@ def simulation_for(rc: RunConfig, device: int = 0, precision: str | None = None)
     ic = make_initial_condition(rc)
     params = model_parameters(rc, ic.delt)
     sim = Simulation(params, precision or rc.precision, device=device, levels_per_batch=rc.levels_per_batch,
+                     solve_columns=rc.solve_columns,
                      use_graphs=rc.use_graphs)
     sim.set_state("psi", ic.psi)
     sim.set_state("BR", ic.BR)
@@ -292,14 +296,14 @@ class Ensemble:
     step()."""
 
     def __init__(self, params_list: list[dict], precision: str = "mixed", device: int = 0,
-                 levels_per_batch: list[int] | None = None):
+                 levels_per_batch: list[int] | None = None, solve_columns: list[int] | None = None):
         L = lib()
         n = len(params_list)
         cfgs = (QgConfig * n)()
         self._keep = []
         for m, p in enumerate(params_list):
             lpb = levels_per_batch[m] if levels_per_batch else 0
-            c, keep = make_config(p, precision, device, lpb)
+            c, keep = make_config(p, precision, device, lpb, solve_columns=solve_columns[m] if solve_columns else 0)
             cfgs[m] = c
             self._keep += keep
         e = C.c_void_p()

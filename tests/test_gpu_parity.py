@@ -347,4 +347,21 @@ def test_autotune_picks_a_timed_candidate():
     ic = make_initial_condition(rc)
     t = autotune(model_parameters(rc, ic.delt), "mixed", nsteps=2)
     assert t["levels_per_batch"] in t["candidates"]
-    assert t["ms_per_step"] == min(t["candidates"].values()) > 0
+    assert set(t["solve_candidates"]) == {16, 32, 64} and t["solve_columns"] in t["solve_candidates"]
+    assert t["ms_per_step"] == min(list(t["candidates"].values()) + list(t["solve_candidates"].values())) > 0
+    # the tuned block shape is accepted by the library and gives the same results
+    rc2 = scaled(CONFIGS["c0"], 32, 8)
+    ic2 = make_initial_condition(rc2)
+    p2 = model_parameters(rc2, ic2.delt)
+    outs = []
+    for tc in (16, 64):
+        sim = Simulation(p2, "mixed", solve_columns=tc)
+        sim.set_state("psi", ic2.psi); sim.set_state("BR", ic2.BR); sim.set_state("BI", ic2.BI)
+        sim.init_state(True, True)
+        sim.steps_async(3, True)
+        sim.synchronize()
+        outs.append(sim.get_state("psi"))
+        sim.close()
+    assert np.array_equal(outs[0], outs[1])
+    with pytest.raises(QgError):
+        Simulation(p2, "mixed", solve_columns=48)

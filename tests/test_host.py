@@ -44,6 +44,7 @@ def test_struct_layout_matches_header(tmp_path):
                                                         check=True).stdout.splitlines())
     assert int(out.pop("sizeof")) == C.sizeof(_lib.QgConfig)
     assert int(out.pop("energy")) == C.sizeof(_lib.QgEnergy)
+    assert int(out.pop("tuning")) == C.sizeof(_lib.QgTuning)
     for f, off in out.items():
         assert getattr(_lib.QgConfig, f).offset == int(off), f
 
