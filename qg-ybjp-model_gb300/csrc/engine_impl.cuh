@@ -677,7 +677,7 @@ class Engine : public EngineBase {
         if (int rc0 = pend()) return rc0;
         if (need_qw) {
           if (int rc0 = pbeg(QG_K_ROW_QW)) return rc0;
-          k_row_qw<T, NN><<<gr, kRowQwThreads, sm_rr3<NN>(), st>>>(g, S, tw);
+          k_row_qw<T, NN><<<gr, Tiles<T, NN>::QTHREADS, sm_rr3<NN>(), st>>>(g, S, tw);
           QG_LAUNCHED();
           if (int rc0 = pend()) return rc0;
           if (int rc0 = pbeg(QG_K_COL_QW)) return rc0;

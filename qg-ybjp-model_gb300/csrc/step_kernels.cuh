@@ -78,6 +78,11 @@ template <typename T, int N> struct Tiles {
   static constexpr int RRT = kRowRT > 0 ? kRowRT : RT;   // rows per CTA of the forward row kernels
   static constexpr int RMINB = imin(CB == 8 ? kRowMinB : 2, smem_ctas((N + 4 * RRT * LD) * CB));
   static constexpr int QMINB = imin(CB == 8 ? kRowQwMinB : 2, smem_ctas((N + 3 * RRT * LD) * CB));
+  // FP32: the first inverse row pass fed from registers, k_row_qw on 128
+  // threads; FP64 keeps the shared-memory fill and 256 threads (the
+  // register-fed pass doubles its registers and halves its occupancy)
+  static constexpr bool RPASS0 = kRowPass0 && CB == 8;
+  static constexpr int QTHREADS = CB == 8 ? kRowQwThreads : kRowThreads;
   static constexpr int CIMINB = imin(CB == 8 ? kColInvMinB : 2, smem_ctas((N + 3 * FSC) * CB));
   static constexpr int CQMINB = imin(CB == 8 ? kColQwMinB : 2, smem_ctas((N + 2 * FSC) * CB));
 };
@@ -216,7 +221,7 @@ k_row_main(Geom g, StepParams sp, cplx<T>* __restrict__ S, const cplx<T>* __rest
   const int y0 = blockIdx.x * RT;
   const int K = g.K;
   load_tw<T, N>(tw, twg, NT);
-  if constexpr (kRowPass0) {
+  if constexpr (Tiles<T, N>::RPASS0) {
     constexpr int R0 = radix_of(N), NB0 = N / R0;
     row_pass0<T, N, false, 3, RT, NT, LD>(bA, [&](int rr, int j, cplx<T> (&v)[3][R0]) {
       const int y = y0 + rr;
@@ -476,9 +481,9 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
 // Phase A, kernel 4: rows — products of compute_qw
 // ===========================================================================
 template <typename T, int N>
-__global__ void __launch_bounds__(kRowQwThreads, Tiles<T, N>::QMINB)
+__global__ void __launch_bounds__(Tiles<T, N>::QTHREADS, Tiles<T, N>::QMINB)
 k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
-  constexpr int RT = Tiles<T, N>::RRT, LD = Tiles<T, N>::LD, NT = kRowQwThreads;
+  constexpr int RT = Tiles<T, N>::RRT, LD = Tiles<T, N>::LD, NT = Tiles<T, N>::QTHREADS;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* bA = tw + N;               // [3][RT][LD]; then, in place, (P1, P2) in the first RT
@@ -501,7 +506,7 @@ k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
     const cplx<T> a = cscale(cmul_i(sBR[kk]), (T)kk), b = cscale(cmul_i(sBI[kk]), (T)kk);
     return k <= K ? mk<T>(a.x - b.y, a.y + b.x) : mk<T>(a.x + b.y, b.x - a.y);
   };
-  if constexpr (kRowPass0) {
+  if constexpr (Tiles<T, N>::RPASS0) {
     constexpr int R0 = radix_of(N), NB0 = N / R0;
     row_pass0<T, N, false, 3, RT, NT, LD>(bA, [&](int rr, int j, cplx<T> (&v)[3][R0]) {
 #pragma unroll
