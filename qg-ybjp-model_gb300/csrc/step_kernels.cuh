@@ -10,6 +10,7 @@
 //   col_qw     : y-forward FFTs -> q^w, q* = q - q^w
 // Phase B (column-local): FP64 tridiagonal solves q*->psi, B->A.
 #pragma once
+#include <type_traits>
 #include "common.cuh"
 #include "fft_block.cuh"
 #include "colfft.cuh"
@@ -300,8 +301,11 @@ template <typename T, int N> struct UpdLay {
   static constexpr int CT = Tiles<T, N>::CT;
   static constexpr int KYM = 2 * ((N + 2) / 3) + 1;     // >= KY for this n
   static constexpr int FE = CT * KYM;                   // entries per staged field
+  // the four q^w inverse transforms reuse the transform and staging regions
+  static constexpr int PAD = 4 * ColLay<N, CT>::FS > 2 * ColLay<N, CT>::FS + 3 * FE
+                                 ? 4 * ColLay<N, CT>::FS - 2 * ColLay<N, CT>::FS - 3 * FE : 0;
   static constexpr size_t bytes() {
-    return (size_t)(N + 2 * ColLay<N, CT>::FS + 5 * FE) * sizeof(cplx<T>) + (size_t)2 * FE * sizeof(T);
+    return (size_t)(N + 2 * ColLay<N, CT>::FS + 5 * FE + PAD) * sizeof(cplx<T>) + (size_t)2 * FE * sizeof(T);
   }
 };
 
@@ -327,7 +331,7 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* sm = tw + N;                          // [2][FS]
   cplx<T>* stg = sm + 2 * ColLay<N, CT>::FS;     // [3][FE]: x, x_old, third (dq / AI / AR)
-  cplx<T>* bnew = stg + 3 * FE;                  // [2][FE]: BR, BI at n+1
+  cplx<T>* bnew = stg + 3 * FE + L::PAD;         // [2][FE]: BR, BI at n+1
   T* tab = reinterpret_cast<T*>(bnew + 2 * FE);  // [2][FE]: e1, e2 or e1w, e2w
   const int tid = threadIdx.x;
   const int zb = blockIdx.y, z = zbase + zb;
@@ -448,33 +452,46 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
   if (!qw_prep) return;
   __syncthreads();
   // y-inverse FFTs of B and i ky B at n+1 (compute_qw, derivatives.f90:929-957)
-  auto pro_B = [&](int which) {
-    return [&, which](int c, int j, cplx<T> (&v)[2][R0]) {
+  // BR, i ky BR, BI, i ky BI: one pass over the four transforms in FP32 (the
+  // transform and staging regions are free now), two passes of two in FP64
+  // (four FP64 transforms per task would spill)
+  auto pro_B = [&](int b0i, auto nf) {
+    constexpr int NFQ = decltype(nf)::value;
+    return [&, b0i](int c, int j, cplx<T> (&v)[NFQ][R0]) {
       const int kx = kx0 + c;
-      const cplx<T>* X = bnew + (which - 1) * FE;
 #pragma unroll
       for (int r = 0; r < R0; ++r) {
         int row; bool cj;
         col_src(g, kx, j + r * NB0, row, cj);
-        const cplx<T> b = row >= 0 ? X[row * CT + c] : mk<T>(0, 0);
         const T ky = row >= 0 ? (T)g.ky_of_row(row) : (T)0;
-        cplx<T> b0 = b, b1 = cscale(cmul_i(b), ky);
-        if (cj) { b0 = cconj(b0); b1 = cconj(b1); }
-        v[0][r] = b0; v[1][r] = b1;
+#pragma unroll
+        for (int b = 0; b < NFQ / 2; ++b) {
+          const cplx<T> x = row >= 0 ? bnew[(b0i + b) * FE + row * CT + c] : mk<T>(0, 0);
+          cplx<T> u0 = x, u1 = cscale(cmul_i(x), ky);
+          if (cj) { u0 = cconj(u0); u1 = cconj(u1); }
+          v[2 * b][r] = u0; v[2 * b + 1][r] = u1;
+        }
       }
     };
   };
-  auto epi_store = [&](int f0) {
-    return [&, f0](int c, int j, cplx<T> (&v)[2][RL]) {
+  auto epi_store = [&](int f0, auto nf) {
+    constexpr int NFQ = decltype(nf)::value;
+    return [&, f0](int c, int j, cplx<T> (&v)[NFQ][RL]) {
 #pragma unroll
-      for (int f = 0; f < 2; ++f)
+      for (int f = 0; f < NFQ; ++f)
 #pragma unroll
         for (int r = 0; r < RL; ++r) S[scr_off(zb, f0 + f, j + r * NSL, N, g.KXP) + kx0 + c] = v[f][r];
     };
   };
-  col_fft<T, N, false, 2, CT, NT>(sm, tw, pro_B(1), epi_store(0));
-  __syncthreads();
-  col_fft<T, N, false, 2, CT, NT>(sm, tw, pro_B(2), epi_store(2));
+  if constexpr (sizeof(T) == 4) {
+    using NF4 = std::integral_constant<int, 4>;
+    col_fft<T, N, false, 4, CT, NT>(sm, tw, pro_B(0, NF4{}), epi_store(0, NF4{}));
+  } else {
+    using NF2 = std::integral_constant<int, 2>;
+    col_fft<T, N, false, 2, CT, NT>(sm, tw, pro_B(0, NF2{}), epi_store(0, NF2{}));
+    __syncthreads();
+    col_fft<T, N, false, 2, CT, NT>(sm, tw, pro_B(1, NF2{}), epi_store(2, NF2{}));
+  }
 }
 
 // ===========================================================================
