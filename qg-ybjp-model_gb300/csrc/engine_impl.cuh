@@ -572,7 +572,7 @@ class Engine : public EngineBase {
   template <int NN> static constexpr size_t sm_col6() { return (size_t)(NN + 6 * Tiles<T, NN>::CT * Tiles<T, NN>::LD) * sizeof(C); }
   template <int NN> static constexpr size_t sm_row7() { return (size_t)(NN + 7 * Tiles<T, NN>::RT * Tiles<T, NN>::LD) * sizeof(C); }
   template <int NN> static constexpr size_t sm_rr3() { return (size_t)(NN + 3 * Tiles<T, NN>::RRT * Tiles<T, NN>::LD) * sizeof(C); }
-  template <int NN> static constexpr size_t sm_rr4() { return (size_t)(NN + 4 * Tiles<T, NN>::RRT * Tiles<T, NN>::LD) * sizeof(C); }
+  template <int NN> static constexpr size_t sm_rm4() { return (size_t)(NN + 4 * Tiles<T, NN>::RTM * Tiles<T, NN>::LD) * sizeof(C); }
   template <int NN> static constexpr size_t sm_row4() { return (size_t)(NN + 4 * Tiles<T, NN>::RT * Tiles<T, NN>::LD) * sizeof(C); }
   // shared memory of the dense (routine-level) kernels
   size_t sm_colinv() const { return (size_t)(g.n + 2 * Tile<T>::CT * (g.n + 1)) * sizeof(C); }
@@ -582,7 +582,7 @@ class Engine : public EngineBase {
     const int mx = cudaFuncAttributeMaxDynamicSharedMemorySize;
     QG_SWITCH_N(g.n, {
       QG_CK(cudaFuncSetAttribute(k_col_inv<T, NN>, (cudaFuncAttribute)mx, (int)sm_ci<NN>(3)));
-      QG_CK(cudaFuncSetAttribute(k_row_main<T, NN>, (cudaFuncAttribute)mx, (int)sm_rr4<NN>()));
+      QG_CK(cudaFuncSetAttribute(k_row_main<T, NN>, (cudaFuncAttribute)mx, (int)sm_rm4<NN>()));
       QG_CK(cudaFuncSetAttribute(k_col_update<T, NN>, (cudaFuncAttribute)mx, (int)UpdLay<T, NN>::bytes()));
       QG_CK(cudaFuncSetAttribute(k_row_qw<T, NN>, (cudaFuncAttribute)mx, (int)sm_rr3<NN>()));
       QG_CK(cudaFuncSetAttribute(k_col_qw<T, NN>, (cudaFuncAttribute)mx, (int)sm_ci<NN>(2)));
@@ -661,13 +661,14 @@ class Engine : public EngineBase {
     for (int z0 = 0; z0 < g.n3; z0 += Zb) {
       const int zc = std::min(Zb, g.n3 - z0);
       QG_SWITCH_N(g.n, {
-        const dim3 gc(g.KXP / Tiles<T, NN>::CT, zc), gr(g.n / Tiles<T, NN>::RRT, zc);
+        const dim3 gc(g.KXP / Tiles<T, NN>::CT, zc), gr(g.n / Tiles<T, NN>::RRT, zc),
+            grm(g.n / Tiles<T, NN>::RTM, zc);
         if (int rc0 = pbeg(QG_K_COL_INV)) return rc0;
         k_col_inv<T, NN><<<gc, kColThreads, sm_ci<NN>(3), st>>>(g, z0, F[F_PSI], F[F_Q], F[F_BR], F[F_BI], S, tw);
         QG_LAUNCHED();
         if (int rc0 = pend()) return rc0;
         if (int rc0 = pbeg(QG_K_ROW_MAIN)) return rc0;
-        k_row_main<T, NN><<<gr, kRowThreads, sm_rr4<NN>(), st>>>(g, s, S, tw);
+        k_row_main<T, NN><<<grm, kRowThreads, sm_rm4<NN>(), st>>>(g, s, S, tw);
         QG_LAUNCHED();
         if (int rc0 = pend()) return rc0;
         if (int rc0 = pbeg(QG_K_COL_UPDATE)) return rc0;

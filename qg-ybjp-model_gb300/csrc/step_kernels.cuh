@@ -50,6 +50,8 @@ constexpr int kRowQwMinB = 5;
 constexpr int kColInvMinB = 2;     // k_col_inv
 constexpr int kColQwMinB = 4;      // k_col_qw
 constexpr bool kRowPass0 = true;   // row kernels: first inverse pass fed from registers
+constexpr bool kRowFuse = true;    // k_row_main: inverse last pass, products, forward first pass in registers
+constexpr int kRowMainMinB = 2;    // k_row_main CTAs per SM when fused
 __host__ __device__ constexpr int smem_ctas(int bytes) {
   return 233472 / (bytes + 1024) >= 8 ? 8 : (233472 / (bytes + 1024) >= 1 ? 233472 / (bytes + 1024) : 1);
 }
@@ -84,6 +86,13 @@ template <typename T, int N> struct Tiles {
   // register-fed pass doubles its registers and halves its occupancy)
   static constexpr bool RPASS0 = kRowPass0 && CB == 8;
   static constexpr int QTHREADS = CB == 8 ? kRowQwThreads : kRowThreads;
+  // k_row_main with the inverse last pass, the products and the forward first
+  // pass in registers: needs the inverse's last radix to equal the forward's
+  // first (N = 512: 8 x 8 x 8) and one (row, butterfly) task per thread
+  static constexpr bool RFUSE = kRowFuse && RPASS0 && N >= 256 && LastNS<N>::value == N / radix_of(N) &&
+                                kRowThreads % (N / radix_of(N)) == 0;
+  static constexpr int RTM = RFUSE ? kRowThreads / (N / radix_of(N)) : RRT;   // rows per k_row_main CTA
+  static constexpr int MMINB = imin(CB == 8 ? (RFUSE ? kRowMainMinB : kRowMinB) : 2, smem_ctas((N + 4 * RTM * LD) * CB));
   static constexpr int CIMINB = imin(CB == 8 ? kColInvMinB : 2, smem_ctas((N + 3 * FSC) * CB));
   static constexpr int CQMINB = imin(CB == 8 ? kColQwMinB : 2, smem_ctas((N + 2 * FSC) * CB));
 };
@@ -210,9 +219,9 @@ __device__ __forceinline__ void unpack_pad(const cplx<T>* F, int k, int n, cplx<
 // Phase A, kernel 2: rows — physical products of convol_waqg / refraction_waqg
 // ===========================================================================
 template <typename T, int N>
-__global__ void __launch_bounds__(kRowThreads, Tiles<T, N>::RMINB)
+__global__ void __launch_bounds__(kRowThreads, Tiles<T, N>::MMINB)
 k_row_main(Geom g, StepParams sp, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
-  constexpr int RT = Tiles<T, N>::RRT, LD = Tiles<T, N>::LD, NT = kRowThreads;
+  constexpr int RT = Tiles<T, N>::RTM, LD = Tiles<T, N>::LD, NT = kRowThreads;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   // [4][RT][LD]: (u,v), (zeta,q), (br,bi); then, in place, the 4 products
@@ -222,8 +231,8 @@ k_row_main(Geom g, StepParams sp, cplx<T>* __restrict__ S, const cplx<T>* __rest
   const int y0 = blockIdx.x * RT;
   const int K = g.K;
   load_tw<T, N>(tw, twg, NT);
+  constexpr int R0 = radix_of(N), NB0 = N / R0;
   if constexpr (Tiles<T, N>::RPASS0) {
-    constexpr int R0 = radix_of(N), NB0 = N / R0;
     row_pass0<T, N, false, 3, RT, NT, LD>(bA, [&](int rr, int j, cplx<T> (&v)[3][R0]) {
       const int y = y0 + rr;
 #pragma unroll
@@ -235,7 +244,49 @@ k_row_main(Geom g, StepParams sp, cplx<T>* __restrict__ S, const cplx<T>* __rest
       }
     });
     __syncthreads();
-    ip_passes<T, N, false, 3 * RT, NT, LD, radix_of(N)>(bA, tw);
+    if constexpr (Tiles<T, N>::RFUSE) {
+      constexpr int NS = LastNS<N>::value, R = N / NS;     // == R0, NS == NB0
+      ip_passes_but_last<T, N, false, 3 * RT, NT, LD, R0>(bA, tw);
+      // last inverse pass into registers: task (row, j) holds the physical
+      // values at x = j + r*NS of the three packed pairs
+      const int j = tid % NS, rr = tid / NS;
+      cplx<T> v[3][R];
+      constexpr int off = tw_off<N>(NS);
+#pragma unroll
+      for (int f = 0; f < 3; ++f) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[f][r] = bA[(f * RT + rr) * LD + pad_idx(j + r * NS)];
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+          cplx<T> w = tw[off + (r - 1) * NS + j];
+          w.y = -w.y;
+          v[f][r] = cmul(v[f][r], w);
+        }
+        dftR<T, R, false>(v[f]);
+      }
+      __syncthreads();
+      // products (u q, v q), (u br, v br), (u bi, v bi), (zeta br, zeta bi)
+      // at the same x are the first forward pass's inputs
+#pragma unroll
+      for (int f = 0; f < 4; ++f) {
+        cplx<T> w[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const cplx<T> uv = v[0][r], zq = v[1][r], bb = v[2][r];
+          w[r] = f == 0 ? mk<T>(uv.x * zq.y, uv.y * zq.y)
+               : f == 1 ? mk<T>(uv.x * bb.x, uv.y * bb.x)
+               : f == 2 ? mk<T>(uv.x * bb.y, uv.y * bb.y)
+                        : mk<T>(zq.x * bb.x, zq.x * bb.y);
+        }
+        dftR<T, R, true>(w);
+#pragma unroll
+        for (int r = 0; r < R; ++r) bA[(f * RT + rr) * LD + pad_idx(j * R + r)] = w[r];
+      }
+      __syncthreads();
+      ip_passes<T, N, true, 4 * RT, NT, LD, R0>(bA, tw);
+    } else {
+      ip_passes<T, N, false, 3 * RT, NT, LD, R0>(bA, tw);
+    }
   } else {
 #pragma unroll 4
     for (int e = tid; e < 3 * RT * N; e += NT) {
@@ -248,21 +299,23 @@ k_row_main(Geom g, StepParams sp, cplx<T>* __restrict__ S, const cplx<T>* __rest
     __syncthreads();
     fft_ip<T, N, false, 3 * RT, NT, LD>(bA, tw);
   }
-  // products: (u q, v q), (u br, v br), (u bi, v bi), (zeta br, zeta bi)
+  if constexpr (!Tiles<T, N>::RFUSE) {
+    // products: (u q, v q), (u br, v br), (u bi, v bi), (zeta br, zeta bi)
 #pragma unroll 4
-  for (int e = tid; e < RT * N; e += NT) {
-    const int x = e % N, rr = e / N;
-    const int px = pad_idx(x);
-    const cplx<T> uv = bA[(0 * RT + rr) * LD + px];
-    const cplx<T> zq = bA[(1 * RT + rr) * LD + px];
-    const cplx<T> bb = bA[(2 * RT + rr) * LD + px];
-    bA[(0 * RT + rr) * LD + px] = mk<T>(uv.x * zq.y, uv.y * zq.y);
-    bA[(1 * RT + rr) * LD + px] = mk<T>(uv.x * bb.x, uv.y * bb.x);
-    bA[(2 * RT + rr) * LD + px] = mk<T>(uv.x * bb.y, uv.y * bb.y);
-    bA[(3 * RT + rr) * LD + px] = mk<T>(zq.x * bb.x, zq.x * bb.y);
+    for (int e = tid; e < RT * N; e += NT) {
+      const int x = e % N, rr = e / N;
+      const int px = pad_idx(x);
+      const cplx<T> uv = bA[(0 * RT + rr) * LD + px];
+      const cplx<T> zq = bA[(1 * RT + rr) * LD + px];
+      const cplx<T> bb = bA[(2 * RT + rr) * LD + px];
+      bA[(0 * RT + rr) * LD + px] = mk<T>(uv.x * zq.y, uv.y * zq.y);
+      bA[(1 * RT + rr) * LD + px] = mk<T>(uv.x * bb.x, uv.y * bb.x);
+      bA[(2 * RT + rr) * LD + px] = mk<T>(uv.x * bb.y, uv.y * bb.y);
+      bA[(3 * RT + rr) * LD + px] = mk<T>(zq.x * bb.x, zq.x * bb.y);
+    }
+    __syncthreads();
+    fft_ip<T, N, true, 4 * RT, NT, LD>(bA, tw);
   }
-  __syncthreads();
-  fft_ip<T, N, true, 4 * RT, NT, LD>(bA, tw);
   const T adv = sp.adv ? (T)1 : (T)0;
   const T half = sp.refr ? (T)0.5 : (T)0;
   for (int e = tid; e < RT * (K + 1); e += NT) {
