@@ -93,6 +93,9 @@ template <typename T, int N> struct Tiles {
                                 kRowThreads % (N / radix_of(N)) == 0;
   static constexpr int RTM = RFUSE ? kRowThreads / (N / radix_of(N)) : RRT;   // rows per k_row_main CTA
   static constexpr int MMINB = imin(CB == 8 ? (RFUSE ? kRowMainMinB : kRowMinB) : 2, smem_ctas((N + 4 * RTM * LD) * CB));
+  // the same for k_row_qw (rows RRT, QTHREADS threads)
+  static constexpr bool QFUSE = kRowFuse && RPASS0 && N >= 256 && LastNS<N>::value == N / radix_of(N) &&
+                                RRT * (N / radix_of(N)) == QTHREADS;
   static constexpr int CIMINB = imin(CB == 8 ? kColInvMinB : 2, smem_ctas((N + 3 * FSC) * CB));
   static constexpr int CQMINB = imin(CB == 8 ? kColQwMinB : 2, smem_ctas((N + 2 * FSC) * CB));
 };
@@ -585,7 +588,41 @@ k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
         for (int r = 0; r < R0; ++r) v[p][r] = packed(p, rr, j + r * NB0);
     });
     __syncthreads();
-    ip_passes<T, N, false, 3 * RT, NT, LD, radix_of(N)>(bA, tw);
+    if constexpr (Tiles<T, N>::QFUSE) {
+      // inverse last pass, the q^w products and the forward first pass in
+      // registers (the same (row, butterfly) task holds both ends)
+      constexpr int R0 = radix_of(N), NS = LastNS<N>::value, R = N / NS;
+      ip_passes_but_last<T, N, false, 3 * RT, NT, LD, R0>(bA, tw);
+      const int j = tid % NS, rr = tid / NS;
+      cplx<T> v[3][R];
+      constexpr int off = tw_off<N>(NS);
+#pragma unroll
+      for (int f = 0; f < 3; ++f) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[f][r] = bA[(f * RT + rr) * LD + pad_idx(j + r * NS)];
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+          cplx<T> w = tw[off + (r - 1) * NS + j];
+          w.y = -w.y;
+          v[f][r] = cmul(v[f][r], w);
+        }
+        dftR<T, R, false>(v[f]);
+      }
+      __syncthreads();
+      cplx<T> w[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const cplx<T> b = v[0][r], bx = v[1][r], by = v[2][r];
+        w[r] = mk<T>(by.x * bx.y - bx.x * by.y, b.x * b.x + b.y * b.y);
+      }
+      dftR<T, R, true>(w);
+#pragma unroll
+      for (int r = 0; r < R; ++r) bA[rr * LD + pad_idx(j * R + r)] = w[r];
+      __syncthreads();
+      ip_passes<T, N, true, RT, NT, LD, R0>(bA, tw);
+    } else {
+      ip_passes<T, N, false, 3 * RT, NT, LD, radix_of(N)>(bA, tw);
+    }
   } else {
 #pragma unroll 4
     for (int e = tid; e < 3 * RT * N; e += NT) {
@@ -595,19 +632,21 @@ k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
     __syncthreads();
     fft_ip<T, N, false, 3 * RT, NT, LD>(bA, tw);
   }
+  if constexpr (!Tiles<T, N>::QFUSE) {
 #pragma unroll 4
-  for (int e = tid; e < RT * N; e += NT) {
-    const int x = e % N, rr = e / N;
-    const int px = pad_idx(x);
-    const cplx<T> b = bA[(0 * RT + rr) * LD + px];    // (br, bi)
-    const cplx<T> bx = bA[(1 * RT + rr) * LD + px];   // (brx, bix)
-    const cplx<T> by = bA[(2 * RT + rr) * LD + px];   // (bry, biy)
-    const T p1 = by.x * bx.y - bx.x * by.y;           // BRy BIx - BRx BIy (derivatives.f90:973)
-    const T p2 = b.x * b.x + b.y * b.y;               // BR^2 + BI^2     (derivatives.f90:996)
-    bA[rr * LD + px] = mk<T>(p1, p2);
+    for (int e = tid; e < RT * N; e += NT) {
+      const int x = e % N, rr = e / N;
+      const int px = pad_idx(x);
+      const cplx<T> b = bA[(0 * RT + rr) * LD + px];    // (br, bi)
+      const cplx<T> bx = bA[(1 * RT + rr) * LD + px];   // (brx, bix)
+      const cplx<T> by = bA[(2 * RT + rr) * LD + px];   // (bry, biy)
+      const T p1 = by.x * bx.y - bx.x * by.y;           // BRy BIx - BRx BIy (derivatives.f90:973)
+      const T p2 = b.x * b.x + b.y * b.y;               // BR^2 + BI^2     (derivatives.f90:996)
+      bA[rr * LD + px] = mk<T>(p1, p2);
+    }
+    __syncthreads();
+    fft_ip<T, N, true, RT, NT, LD>(bA, tw);
   }
-  __syncthreads();
-  fft_ip<T, N, true, RT, NT, LD>(bA, tw);
   for (int e = tid; e < RT * (K + 1); e += NT) {
     const int k = e % (K + 1), rr = e / (K + 1);
     const int y = y0 + rr;
