@@ -52,6 +52,8 @@ constexpr int kColQwMinB = 4;      // k_col_qw
 constexpr bool kRowPass0 = true;   // row kernels: first inverse pass fed from registers
 constexpr bool kRowFuse = true;    // k_row_main: inverse last pass, products, forward first pass in registers
 constexpr int kRowMainMinB = 2;    // k_row_main CTAs per SM when fused
+constexpr bool kUpdLean = true;    // k_col_update (FP32): smaller shared footprint ...
+constexpr int kUpdMinB = 2;        // ... for this many CTAs per SM
 __host__ __device__ constexpr int smem_ctas(int bytes) {
   return 233472 / (bytes + 1024) >= 8 ? 8 : (233472 / (bytes + 1024) >= 1 ? 233472 / (bytes + 1024) : 1);
 }
@@ -360,8 +362,14 @@ template <typename T, int N> struct UpdLay {
   // the four q^w inverse transforms reuse the transform and staging regions
   static constexpr int PAD = 4 * ColLay<N, CT>::FS > 2 * ColLay<N, CT>::FS + 3 * FE
                                  ? 4 * ColLay<N, CT>::FS - 2 * ColLay<N, CT>::FS - 3 * FE : 0;
+  // lean (FP32): IF tables read from global memory, B^{n+1} re-read from
+  // global memory for the q^w transforms (two passes of two), so that three
+  // CTAs fit per SM
+  static constexpr bool LEAN = kUpdLean && sizeof(T) == 4;
+  static constexpr int MINB = LEAN ? kUpdMinB : Tiles<T, N>::MINB;
   static constexpr size_t bytes() {
-    return (size_t)(N + 2 * ColLay<N, CT>::FS + 5 * FE + PAD) * sizeof(cplx<T>) + (size_t)2 * FE * sizeof(T);
+    return LEAN ? (size_t)(N + 2 * ColLay<N, CT>::FS + 3 * FE) * sizeof(cplx<T>)
+                : (size_t)(N + 2 * ColLay<N, CT>::FS + 5 * FE + PAD) * sizeof(cplx<T>) + (size_t)2 * FE * sizeof(T);
   }
 };
 
@@ -376,7 +384,7 @@ __device__ __forceinline__ void cp_async_s(T* dst, const T* src, bool valid) {
 }
 
 template <typename T, int N>
-__global__ void __launch_bounds__(kColThreads, Tiles<T, N>::MINB)
+__global__ void __launch_bounds__(kColThreads, UpdLay<T, N>::MINB)
 k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict__ e1t, const T* __restrict__ e2t,
              const T* __restrict__ e1wt, const T* __restrict__ e2wt, cplx<T>* __restrict__ S,
              const cplx<T>* __restrict__ twg, int qw_prep) {
@@ -387,8 +395,8 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* sm = tw + N;                          // [2][FS]
   cplx<T>* stg = sm + 2 * ColLay<N, CT>::FS;     // [3][FE]: x, x_old, third (dq / AI / AR)
-  cplx<T>* bnew = stg + 3 * FE + L::PAD;         // [2][FE]: BR, BI at n+1
-  T* tab = reinterpret_cast<T*>(bnew + 2 * FE);  // [2][FE]: e1, e2 or e1w, e2w
+  cplx<T>* bnew = stg + 3 * FE + L::PAD;         // [2][FE]: BR, BI at n+1 (not LEAN)
+  T* tab = reinterpret_cast<T*>(bnew + 2 * FE);  // [2][FE]: e1, e2 or e1w, e2w (not LEAN)
   const int tid = threadIdx.x;
   const int zb = blockIdx.y, z = zbase + zb;
   const int kx0 = blockIdx.x * CT;
@@ -415,7 +423,7 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
       cp_async_c<T>(stg + e, in ? X + m : X, in);
       if (!eul) cp_async_c<T>(stg + FE + e, in ? Xo + m : Xo, in);
       if (need3) cp_async_c<T>(stg + 2 * FE + e, in ? X3 + m : X3, in);
-      if (which < 2) {
+      if (!L::LEAN && which < 2) {
         const long long mt = (long long)row * g.KXP + kx;
         const T* t1 = which == 0 ? e1t : e1wt;
         const T* t2 = which == 0 ? e2t : e2wt;
@@ -461,14 +469,16 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
         if (g.mask(kx, ky)) {
           if (which == 0) {
             const cplx<T> dqv = sp.use_dq ? stg[2 * FE + e] : mk<T>(0, 0);
-            const T e1 = tab[e], e2 = tab[FE + e];
+            const long long mt = (long long)row * g.KXP + kx;
+            const T e1 = L::LEAN ? e1t[mt] : tab[e], e2 = L::LEAN ? e2t[mt] : tab[FE + e];
             if (eul) {
               xn = cscale(cadd(csub(xo, cscale(tnd, dt)), cscale(dqv, dt)), e1);
             } else {
               xn = cadd(csub(cscale(xo, e2), cscale(cscale(tnd, dt2), e1)), cscale(cscale(dqv, dt2), e2));
             }
           } else {
-            const T e1w = tab[e], e2w = tab[FE + e];
+            const long long mt = (long long)row * g.KXP + kx;
+            const T e1w = L::LEAN ? e1wt[mt] : tab[e], e2w = L::LEAN ? e2wt[mt] : tab[FE + e];
             const T ck = cdisp * (T)(kx * kx + ky * ky);
             // nBR - 0.5 rBI + c kh2 AI ; nBI + 0.5 rBR - c kh2 AR
             const cplx<T> a3 = stg[2 * FE + e];
@@ -484,7 +494,7 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
         }
         X[m] = xn;
         Xo[m] = xf;
-        if (which > 0) bnew[(which - 1) * FE + e] = xn;
+        if (!L::LEAN && which > 0) bnew[(which - 1) * FE + e] = xn;
         if (!sp.ybj && which > 0) {
           // compute_sigma (derivatives.f90:1037-1068) with the tendencies
           // T_R = nBR - rBI/2, T_I = nBI + rBR/2: (rBR + 2 nBI) = 2 T_I,
@@ -522,7 +532,10 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
         const T ky = row >= 0 ? (T)g.ky_of_row(row) : (T)0;
 #pragma unroll
         for (int b = 0; b < NFQ / 2; ++b) {
-          const cplx<T> x = row >= 0 ? bnew[(b0i + b) * FE + row * CT + c] : mk<T>(0, 0);
+          // B^{n+1}: this CTA's own writes, visible after the barrier
+          const cplx<T>* Xg = (b0i + b) == 0 ? st.BR : st.BI;
+          const cplx<T> x = row < 0 ? mk<T>(0, 0)
+                          : L::LEAN ? Xg[zoff + (long long)row * g.KXP + kx] : bnew[(b0i + b) * FE + row * CT + c];
           cplx<T> u0 = x, u1 = cscale(cmul_i(x), ky);
           if (cj) { u0 = cconj(u0); u1 = cconj(u1); }
           v[2 * b][r] = u0; v[2 * b + 1][r] = u1;
@@ -539,7 +552,7 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
         for (int r = 0; r < RL; ++r) S[scr_off(zb, f0 + f, j + r * NSL, N, g.KXP) + kx0 + c] = v[f][r];
     };
   };
-  if constexpr (sizeof(T) == 4) {
+  if constexpr (sizeof(T) == 4 && !L::LEAN) {
     using NF4 = std::integral_constant<int, 4>;
     col_fft<T, N, false, 4, CT, NT>(sm, tw, pro_B(0, NF4{}), epi_store(0, NF4{}));
   } else {
