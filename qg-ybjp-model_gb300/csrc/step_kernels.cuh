@@ -53,6 +53,7 @@ constexpr bool kRowPass0 = true;   // row kernels: first inverse pass fed from r
 constexpr bool kRowFuse = true;    // k_row_main: inverse last pass, products, forward first pass in registers
 constexpr int kRowMainMinB = 2;    // k_row_main CTAs per SM when fused
 constexpr bool kUpdLean = true;    // k_col_update (FP32): smaller shared footprint ...
+constexpr bool kUpdStage16 = true; // k_col_update (FP32): state staged by 16-byte copies
 constexpr int kUpdMinB = 2;        // ... for this many CTAs per SM
 __host__ __device__ constexpr int smem_ctas(int bytes) {
   return 233472 / (bytes + 1024) >= 8 ? 8 : (233472 / (bytes + 1024) >= 1 ? 233472 / (bytes + 1024) : 1);
@@ -373,6 +374,12 @@ template <typename T, int N> struct UpdLay {
   }
 };
 
+// 16-byte asynchronous copy of nbytes (0, 8 or 16) and zeros for the rest
+__device__ __forceinline__ void cp_async_16(void* dst, const void* src, int nbytes) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(nbytes));
+}
+
 template <typename T>
 __device__ __forceinline__ void cp_async_s(T* dst, const T* src, bool valid) {
   const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
@@ -415,20 +422,41 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
     const cplx<T>* Xo = which == 0 ? st.qo : (which == 1 ? st.BRo : st.BIo);
     const cplx<T>* X3 = which == 0 ? st.dq : (which == 1 ? st.AI : st.AR);
     const bool need3 = which != 0 || sp.use_dq;
-    for (int e = tid; e < CT * KY; e += NT) {
-      const int c = e % CT, row = e / CT;
-      const int kx = kx0 + c;
-      const bool in = kx <= g.K;
-      const long long m = zoff + (long long)row * g.KXP + kx;
-      cp_async_c<T>(stg + e, in ? X + m : X, in);
-      if (!eul) cp_async_c<T>(stg + FE + e, in ? Xo + m : Xo, in);
-      if (need3) cp_async_c<T>(stg + 2 * FE + e, in ? X3 + m : X3, in);
-      if (!L::LEAN && which < 2) {
-        const long long mt = (long long)row * g.KXP + kx;
-        const T* t1 = which == 0 ? e1t : e1wt;
-        const T* t2 = which == 0 ? e2t : e2wt;
-        cp_async_s<T>(tab + e, in ? t1 + mt : t1, in);
-        cp_async_s<T>(tab + FE + e, in ? t2 + mt : t2, in);
+    if constexpr (kUpdStage16 && sizeof(T) == 4 && CT % 2 == 0) {
+      // FP32: 16-byte copies of column pairs (zero-filled past kx = K)
+      for (int e2 = tid; e2 < (CT / 2) * KY; e2 += NT) {
+        const int c = (e2 % (CT / 2)) * 2, row = e2 / (CT / 2);
+        const int kx = kx0 + c;
+        const int nb = kx + 1 <= g.K ? 16 : (kx <= g.K ? 8 : 0);
+        const long long m = zoff + (long long)row * g.KXP + kx;
+        const int e = row * CT + c;
+        cp_async_16(stg + e, nb ? X + m : X, nb);
+        if (!eul) cp_async_16(stg + FE + e, nb ? Xo + m : Xo, nb);
+        if (need3) cp_async_16(stg + 2 * FE + e, nb ? X3 + m : X3, nb);
+      }
+    } else {
+      for (int e = tid; e < CT * KY; e += NT) {
+        const int c = e % CT, row = e / CT;
+        const int kx = kx0 + c;
+        const bool in = kx <= g.K;
+        const long long m = zoff + (long long)row * g.KXP + kx;
+        cp_async_c<T>(stg + e, in ? X + m : X, in);
+        if (!eul) cp_async_c<T>(stg + FE + e, in ? Xo + m : Xo, in);
+        if (need3) cp_async_c<T>(stg + 2 * FE + e, in ? X3 + m : X3, in);
+      }
+    }
+    if constexpr (!L::LEAN) {
+      if (which < 2) {
+        for (int e = tid; e < CT * KY; e += NT) {
+          const int c = e % CT, row = e / CT;
+          const int kx = kx0 + c;
+          const bool in = kx <= g.K;
+          const long long mt = (long long)row * g.KXP + kx;
+          const T* t1 = which == 0 ? e1t : e1wt;
+          const T* t2 = which == 0 ? e2t : e2wt;
+          cp_async_s<T>(tab + e, in ? t1 + mt : t1, in);
+          cp_async_s<T>(tab + FE + e, in ? t2 + mt : t2, in);
+        }
       }
     }
   };
