@@ -35,11 +35,18 @@ for _p in (str(ROOT), str(PKG)):
 
 FALLBACK_HBM_GBS = 6800.0
 # DRAM bytes per level of a launch (dram__bytes_read.sum + dram__bytes_write.sum,
-# L2 not flushed) of the dominant kernel, from the ncu capture summarised in
-# profiles/dram_per_launch_c2_512x512x32_mixed.md (512^2 levels, 11 levels per
-# launch: 49.5 MB).  The traffic of a launch grows with the levels it covers,
-# so the roofline entry scales it by the levels per launch of the run.
-MEASURED_TRAFFIC_PER_LEVEL = {("col_update", 512, "mixed"): 121.7e6 / 13}
+# L2 not flushed) of each phase-A kernel, from the ncu capture summarised in
+# profiles/dram_per_launch_512x512x26_mixed.md (512^2 levels, 13 levels per
+# launch, mean of two launches).  The traffic of a launch grows with the
+# levels it covers, so the roofline entry scales it by the levels per launch
+# of the run.
+MEASURED_TRAFFIC_PER_LEVEL = {
+    ("col_inv", 512, "mixed"): 66.61e6 / 13,
+    ("row_main", 512, "mixed"): 8.451e6 / 13,
+    ("col_update", 512, "mixed"): 117.89e6 / 13,
+    ("row_qw", 512, "mixed"): 8.739e6 / 13,
+    ("col_qw", 512, "mixed"): 9.774e6 / 13,
+}
 
 
 # ---------------------------------------------------------------------------
