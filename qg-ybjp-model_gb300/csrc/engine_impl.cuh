@@ -101,6 +101,10 @@ class Engine : public EngineBase {
     QG_CK(cudaMalloc(&diag_part, (size_t)g.n3 * kDiagChunks * kNDiag * sizeof(double)));
     QG_CK(cudaMalloc(&diag_out, kNDiag * sizeof(double)));
     QG_CK(cudaMallocHost(&diag_host, kNDiag * sizeof(double)));
+    QG_CK(cudaHostAlloc(&wflag_h, sizeof(int), cudaHostAllocMapped));
+    *wflag_h = 0;
+    QG_CK(cudaHostGetDevicePointer(&wflag, wflag_h, 0));
+    QG_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, cfg.device));
     // phase-A batching: keep the scratch planes of one batch L2-sized
     const size_t per_level = (size_t)kNScr * g.n * g.KXP * sizeof(C);
     int zb = cfg.levels_per_batch;
@@ -167,7 +171,21 @@ class Engine : public EngineBase {
     return QG_OK;
   }
 
-  int synchronize() override { QG_CK(cudaStreamSynchronize(st)); return QG_OK; }
+  int synchronize() override {
+    QG_CK(cudaStreamSynchronize(st));
+    return check_waits();
+  }
+
+  // QG_ERR_TIMEOUT when a kernel's bounded wait expired since the last check
+  // (call after the stream has drained)
+  int check_waits() {
+    if (wflag_h && *(volatile int*)wflag_h) {
+      *(volatile int*)wflag_h = 0;
+      err = "a bounded device-side wait expired (bulk copy of the row kernels)";
+      return QG_ERR_TIMEOUT;
+    }
+    return QG_OK;
+  }
 
   // ---- state --------------------------------------------------------------
   int set_state(int field, const double* kvar, int level0, int nlev) override {
@@ -262,7 +280,7 @@ class Engine : public EngineBase {
     int rc = run_step(euler ? 1 : 0);
     if (rc) return rc;
     QG_CK(cudaStreamSynchronize(st));
-    return QG_OK;
+    return check_waits();
   }
 
   int steps_async(int nsteps, int euler) override {
@@ -509,6 +527,10 @@ class Engine : public EngineBase {
   int solve_tc = 32;         // columns per CTA of k_solve_st
   double *du = nullptr, *cu = nullptr, *cl = nullptr, *r2 = nullptr;
   double *diag_part = nullptr, *diag_out = nullptr, *diag_host = nullptr;
+  // set by a kernel whose bounded wait expired (mapped page-locked word)
+  int* wflag_h = nullptr;
+  int* wflag = nullptr;
+  int nsm = 1, occ_rm = 1, occ_rq = 1;   // SMs; resident CTAs per SM of the persistent row kernels
   double *om_t1 = nullptr, *om_du = nullptr, *om_dl = nullptr, *om_a = nullptr, *om_scr = nullptr;
   C* sig[2] = {};     // regular YBJ: per-level sigma terms
   C* S = nullptr;
@@ -536,6 +558,9 @@ class Engine : public EngineBase {
     for (auto& p : P) if (p) cudaFree(p);
     for (auto& p : tmpF) if (p) cudaFree(p);
     if (diag_host) cudaFreeHost(diag_host);
+    if (wflag_h) cudaFreeHost(wflag_h);
+    wflag_h = nullptr;
+    wflag = nullptr;
     if (st) cudaStreamDestroy(st);
     st = nullptr;
   }
@@ -573,6 +598,16 @@ class Engine : public EngineBase {
   template <int NN> static constexpr size_t sm_row7() { return (size_t)(NN + 7 * Tiles<T, NN>::RT * Tiles<T, NN>::LD) * sizeof(C); }
   template <int NN> static constexpr size_t sm_rr3() { return (size_t)(NN + 3 * Tiles<T, NN>::RRT * Tiles<T, NN>::LD) * sizeof(C); }
   template <int NN> static constexpr size_t sm_rm4() { return (size_t)(NN + 4 * Tiles<T, NN>::RTM * Tiles<T, NN>::LD) * sizeof(C); }
+  // the persistent row kernels add a staging copy of an item's scratch rows
+  // (nf planes x rows x kxp) and its mbarrier; the attribute is set for the
+  // widest rows any mask of this n can have (kxp for K = n/2)
+  template <int NN> static constexpr int kxp_max() { return ((NN / 2 + 1 + 7) / 8) * 8; }
+  template <int NN> static constexpr size_t sm_rm(int kxp) {
+    return sm_rm4<NN>() + (Tiles<T, NN>::RPRE ? (size_t)6 * Tiles<T, NN>::RTM * kxp * sizeof(C) + 16 : 0);
+  }
+  template <int NN> static constexpr size_t sm_rq(int kxp) {
+    return sm_rr3<NN>() + (Tiles<T, NN>::QPRE ? (size_t)4 * Tiles<T, NN>::RRT * kxp * sizeof(C) + 16 : 0);
+  }
   template <int NN> static constexpr size_t sm_row4() { return (size_t)(NN + 4 * Tiles<T, NN>::RT * Tiles<T, NN>::LD) * sizeof(C); }
   // shared memory of the dense (routine-level) kernels
   size_t sm_colinv() const { return (size_t)(g.n + 2 * Tile<T>::CT * (g.n + 1)) * sizeof(C); }
@@ -582,9 +617,14 @@ class Engine : public EngineBase {
     const int mx = cudaFuncAttributeMaxDynamicSharedMemorySize;
     QG_SWITCH_N(g.n, {
       QG_CK(cudaFuncSetAttribute(k_col_inv<T, NN>, (cudaFuncAttribute)mx, (int)sm_ci<NN>(3)));
-      QG_CK(cudaFuncSetAttribute(k_row_main<T, NN>, (cudaFuncAttribute)mx, (int)sm_rm4<NN>()));
+      QG_CK(cudaFuncSetAttribute(k_row_main<T, NN>, (cudaFuncAttribute)mx, (int)sm_rm<NN>(kxp_max<NN>())));
       QG_CK(cudaFuncSetAttribute(k_col_update<T, NN>, (cudaFuncAttribute)mx, (int)UpdLay<T, NN>::bytes()));
-      QG_CK(cudaFuncSetAttribute(k_row_qw<T, NN>, (cudaFuncAttribute)mx, (int)sm_rr3<NN>()));
+      QG_CK(cudaFuncSetAttribute(k_row_qw<T, NN>, (cudaFuncAttribute)mx, (int)sm_rq<NN>(kxp_max<NN>())));
+      QG_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_rm, k_row_main<T, NN>, kRowThreads, sm_rm<NN>(g.KXP)));
+      QG_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_rq, k_row_qw<T, NN>, Tiles<T, NN>::QTHREADS,
+                                                          sm_rq<NN>(g.KXP)));
+      occ_rm = std::max(occ_rm, 1);
+      occ_rq = std::max(occ_rq, 1);
       QG_CK(cudaFuncSetAttribute(k_col_qw<T, NN>, (cudaFuncAttribute)mx, (int)sm_ci<NN>(2)));
       // per-function attribute shared by every handle: set it for the deepest supported column
       QG_CK(cudaFuncSetAttribute(k_solve<T>, (cudaFuncAttribute)mx, (int)solve_smem(kMaxN3)));
@@ -668,7 +708,13 @@ class Engine : public EngineBase {
         QG_LAUNCHED();
         if (int rc0 = pend()) return rc0;
         if (int rc0 = pbeg(QG_K_ROW_MAIN)) return rc0;
-        k_row_main<T, NN><<<grm, kRowThreads, sm_rm4<NN>(), st>>>(g, s, S, tw);
+        if constexpr (Tiles<T, NN>::RPRE) {
+          const int items = zc * (NN / Tiles<T, NN>::RTM);
+          k_row_main<T, NN><<<std::min(items, nsm * occ_rm), kRowThreads, sm_rm<NN>(g.KXP), st>>>(g, s, S, tw, items,
+                                                                                                 wflag);
+        } else {
+          k_row_main<T, NN><<<grm, kRowThreads, sm_rm<NN>(g.KXP), st>>>(g, s, S, tw, 0, wflag);
+        }
         QG_LAUNCHED();
         if (int rc0 = pend()) return rc0;
         if (int rc0 = pbeg(QG_K_COL_UPDATE)) return rc0;
@@ -678,7 +724,13 @@ class Engine : public EngineBase {
         if (int rc0 = pend()) return rc0;
         if (need_qw) {
           if (int rc0 = pbeg(QG_K_ROW_QW)) return rc0;
-          k_row_qw<T, NN><<<gr, Tiles<T, NN>::QTHREADS, sm_rr3<NN>(), st>>>(g, S, tw);
+          if constexpr (Tiles<T, NN>::QPRE) {
+            const int items = zc * (NN / Tiles<T, NN>::RRT);
+            k_row_qw<T, NN><<<std::min(items, nsm * occ_rq), Tiles<T, NN>::QTHREADS, sm_rq<NN>(g.KXP), st>>>(
+                g, S, tw, items, wflag);
+          } else {
+            k_row_qw<T, NN><<<gr, Tiles<T, NN>::QTHREADS, sm_rq<NN>(g.KXP), st>>>(g, S, tw, 0, wflag);
+          }
           QG_LAUNCHED();
           if (int rc0 = pend()) return rc0;
           if (int rc0 = pbeg(QG_K_COL_QW)) return rc0;

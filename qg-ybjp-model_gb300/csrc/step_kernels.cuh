@@ -14,6 +14,7 @@
 #include "common.cuh"
 #include "fft_block.cuh"
 #include "colfft.cuh"
+#include "bulk_copy.cuh"
 
 namespace qg {
 
@@ -52,6 +53,7 @@ constexpr int kColQwMinB = 4;      // k_col_qw
 constexpr bool kRowPass0 = true;   // row kernels: first inverse pass fed from registers
 constexpr bool kRowFuse = true;    // k_row_main: inverse last pass, products, forward first pass in registers
 constexpr int kRowMainMinB = 2;    // k_row_main CTAs per SM when fused
+constexpr bool kRowPrefetch = true; // fused row kernels: persistent, next item's rows bulk-copied ahead
 constexpr bool kUpdLean = true;    // k_col_update (FP32): smaller shared footprint ...
 constexpr bool kUpdStage16 = true; // k_col_update (FP32): state staged by 16-byte copies
 constexpr int kUpdMinB = 2;        // ... for this many CTAs per SM
@@ -99,6 +101,10 @@ template <typename T, int N> struct Tiles {
   // the same for k_row_qw (rows RRT, QTHREADS threads)
   static constexpr bool QFUSE = kRowFuse && RPASS0 && N >= 256 && LastNS<N>::value == N / radix_of(N) &&
                                 RRT * (N / radix_of(N)) == QTHREADS;
+  // persistent row kernels that bulk-copy the next item's scratch rows into
+  // shared memory during the current item (the fused FP32 row kernels)
+  static constexpr bool RPRE = kRowPrefetch && RFUSE;
+  static constexpr bool QPRE = kRowPrefetch && QFUSE;
   static constexpr int CIMINB = imin(CB == 8 ? kColInvMinB : 2, smem_ctas((N + 3 * FSC) * CB));
   static constexpr int CQMINB = imin(CB == 8 ? kColQwMinB : 2, smem_ctas((N + 2 * FSC) * CB));
 };
@@ -224,32 +230,30 @@ __device__ __forceinline__ void unpack_pad(const cplx<T>* F, int k, int n, cplx<
 // ===========================================================================
 // Phase A, kernel 2: rows — physical products of convol_waqg / refraction_waqg
 // ===========================================================================
-template <typename T, int N>
-__global__ void __launch_bounds__(kRowThreads, Tiles<T, N>::MMINB)
-k_row_main(Geom g, StepParams sp, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
+// One CTA item: rows y0..y0+RT-1 of level zb of the batch.  src(f, rr)
+// points at row rr of scratch plane f (global memory, or the item's copy
+// in shared memory); after_pass0() runs once the first pass has read them
+// all (after a CTA barrier).  bA: [4][RT][LD].
+template <typename T, int N, class Src, class After>
+__device__ __forceinline__ void row_main_item(const Geom& g, const StepParams& sp, cplx<T>* __restrict__ S,
+                                              const cplx<T>* __restrict__ tw, cplx<T>* __restrict__ bA, int zb,
+                                              int y0, Src src, After after_pass0) {
   constexpr int RT = Tiles<T, N>::RTM, LD = Tiles<T, N>::LD, NT = kRowThreads;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
-  // [4][RT][LD]: (u,v), (zeta,q), (br,bi); then, in place, the 4 products
-  cplx<T>* bA = tw + N;
   const int tid = threadIdx.x;
-  const int zb = blockIdx.y;
-  const int y0 = blockIdx.x * RT;
   const int K = g.K;
-  load_tw<T, N>(tw, twg, NT);
   constexpr int R0 = radix_of(N), NB0 = N / R0;
   if constexpr (Tiles<T, N>::RPASS0) {
     row_pass0<T, N, false, 3, RT, NT, LD>(bA, [&](int rr, int j, cplx<T> (&v)[3][R0]) {
-      const int y = y0 + rr;
 #pragma unroll
       for (int p = 0; p < 3; ++p) {
-        const cplx<T>* X = S + scr_off(zb, 2 * p, y, N, g.KXP);
-        const cplx<T>* Y = S + scr_off(zb, 2 * p + 1, y, N, g.KXP);
+        const cplx<T>* X = src(2 * p, rr);
+        const cplx<T>* Y = src(2 * p + 1, rr);
 #pragma unroll
         for (int r = 0; r < R0; ++r) v[p][r] = pack_spec<T>(X, Y, j + r * NB0, N, K);
       }
     });
     __syncthreads();
+    after_pass0();
     if constexpr (Tiles<T, N>::RFUSE) {
       constexpr int NS = LastNS<N>::value, R = N / NS;     // == R0, NS == NB0
       ip_passes_but_last<T, N, false, 3 * RT, NT, LD, R0>(bA, tw);
@@ -297,12 +301,10 @@ k_row_main(Geom g, StepParams sp, cplx<T>* __restrict__ S, const cplx<T>* __rest
 #pragma unroll 4
     for (int e = tid; e < 3 * RT * N; e += NT) {
       const int k = e % N, p = (e / N) % 3, rr = e / (3 * N);
-      const int y = y0 + rr;
-      const cplx<T>* X = S + scr_off(zb, 2 * p, y, N, g.KXP);
-      const cplx<T>* Y = S + scr_off(zb, 2 * p + 1, y, N, g.KXP);
-      bA[(p * RT + rr) * LD + pad_idx(k)] = pack_spec<T>(X, Y, k, N, K);
+      bA[(p * RT + rr) * LD + pad_idx(k)] = pack_spec<T>(src(2 * p, rr), src(2 * p + 1, rr), k, N, K);
     }
     __syncthreads();
+    after_pass0();
     fft_ip<T, N, false, 3 * RT, NT, LD>(bA, tw);
   }
   if constexpr (!Tiles<T, N>::RFUSE) {
@@ -340,6 +342,62 @@ k_row_main(Geom g, StepParams sp, cplx<T>* __restrict__ S, const cplx<T>* __rest
     S[scr_off(zb, 3, y, N, g.KXP) + k] = cscale(vbr, adv);
     S[scr_off(zb, 4, y, N, g.KXP) + k] = cadd(cscale(cmul_i(ubi), kx * adv), cscale(zbr, half));
     S[scr_off(zb, 5, y, N, g.KXP) + k] = cscale(vbi, adv);
+  }
+}
+
+// Rows of the batch: grid (N/RT, levels) with one item per CTA, or, with
+// the prefetch (Tiles::RPRE), a persistent grid whose CTAs walk the items
+// it = blockIdx.x, += gridDim.x (item it: level it / (N/RT), rows
+// (it % (N/RT))*RT...), each CTA bulk-copying the six scratch rows of its
+// next item into shared memory while it transforms the current one.
+// A copy that does not land within the bounded wait sets *wflag and ends the
+// CTA.
+template <typename T, int N>
+__global__ void __launch_bounds__(kRowThreads, Tiles<T, N>::MMINB)
+k_row_main(Geom g, StepParams sp, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg, int nitems,
+           int* __restrict__ wflag) {
+  constexpr int RT = Tiles<T, N>::RTM, LD = Tiles<T, N>::LD, NT = kRowThreads;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
+  // [4][RT][LD]: (u,v), (zeta,q), (br,bi); then, in place, the 4 products
+  cplx<T>* bA = tw + N;
+  load_tw<T, N>(tw, twg, NT);
+  if constexpr (Tiles<T, N>::RPRE) {
+    constexpr int NGY = N / RT;
+    cplx<T>* stg = bA + 4 * RT * LD;                 // [6][RT][KXP]: the item's scratch rows
+    const unsigned bar = smem_u32(stg + 6 * RT * g.KXP);
+    const unsigned fb = (unsigned)(RT * g.KXP * sizeof(cplx<T>));
+    auto issue = [&](int it) {
+      const int zb = it / NGY, y0 = (it % NGY) * RT;
+      mbar_expect_tx(bar, 6u * fb);
+#pragma unroll
+      for (int f = 0; f < 6; ++f) bulk_g2s(stg + f * RT * g.KXP, S + scr_off(zb, f, y0, N, g.KXP), fb, bar);
+    };
+    if (threadIdx.x == 0) {
+      mbar_init(bar, 1);
+      if ((int)blockIdx.x < nitems) issue(blockIdx.x);
+    }
+    __syncthreads();
+    unsigned ph = 0;
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x, ph ^= 1u) {
+      // also orders the previous item's last reads of bA before this one's writes
+      const bool ok = mbar_wait(bar, ph);
+      if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) { atomicOr(wflag, 1); (void)mbar_wait(bar, ph); }
+        return;
+      }
+      const int nxt = it + (int)gridDim.x;
+      row_main_item<T, N>(g, sp, S, tw, bA, it / NGY, (it % NGY) * RT,
+                          [&](int f, int rr) -> const cplx<T>* { return stg + (f * RT + rr) * g.KXP; },
+                          [&]() {
+                            if (threadIdx.x == 0 && nxt < nitems) { fence_proxy_async(); issue(nxt); }
+                          });
+    }
+  } else {
+    const int zb = blockIdx.y, y0 = blockIdx.x * RT;
+    row_main_item<T, N>(g, sp, S, tw, bA, zb, y0,
+                        [&](int f, int rr) -> const cplx<T>* { return S + scr_off(zb, f, y0 + rr, N, g.KXP); },
+                        []() {});
   }
 }
 
@@ -594,25 +652,20 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
 // ===========================================================================
 // Phase A, kernel 4: rows — products of compute_qw
 // ===========================================================================
-template <typename T, int N>
-__global__ void __launch_bounds__(Tiles<T, N>::QTHREADS, Tiles<T, N>::QMINB)
-k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
+// One CTA item of k_row_qw: rows y0..y0+RT-1 of level zb; src(f, rr) and
+// after_pass0 as in row_main_item.  bA: [3][RT][LD].
+template <typename T, int N, class Src, class After>
+__device__ __forceinline__ void row_qw_item(const Geom& g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ tw,
+                                            cplx<T>* __restrict__ bA, int zb, int y0, Src src, After after_pass0) {
   constexpr int RT = Tiles<T, N>::RRT, LD = Tiles<T, N>::LD, NT = Tiles<T, N>::QTHREADS;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* bA = tw + N;               // [3][RT][LD]; then, in place, (P1, P2) in the first RT
   const int tid = threadIdx.x;
-  const int zb = blockIdx.y;
-  const int y0 = blockIdx.x * RT;
   const int K = g.K;
-  load_tw<T, N>(tw, twg, NT);
   // packed: (BR, BI), (BRx, BIx), (BRy, BIy)
   auto packed = [&](int p, int rr, int k) -> cplx<T> {
-    const int y = y0 + rr;
-    const cplx<T>* sBR = S + scr_off(zb, 0, y, N, g.KXP);
-    const cplx<T>* sBRy = S + scr_off(zb, 1, y, N, g.KXP);
-    const cplx<T>* sBI = S + scr_off(zb, 2, y, N, g.KXP);
-    const cplx<T>* sBIy = S + scr_off(zb, 3, y, N, g.KXP);
+    const cplx<T>* sBR = src(0, rr);
+    const cplx<T>* sBRy = src(1, rr);
+    const cplx<T>* sBI = src(2, rr);
+    const cplx<T>* sBIy = src(3, rr);
     if (p == 0) return pack_spec<T>(sBR, sBI, k, N, K);
     if (p == 2) return pack_spec<T>(sBRy, sBIy, k, N, K);
     if (k == 0 || (k > K && k < N - K)) return mk<T>(0, 0);      // x-derivatives vanish at kx = 0
@@ -629,6 +682,7 @@ k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
         for (int r = 0; r < R0; ++r) v[p][r] = packed(p, rr, j + r * NB0);
     });
     __syncthreads();
+    after_pass0();
     if constexpr (Tiles<T, N>::QFUSE) {
       // inverse last pass, the q^w products and the forward first pass in
       // registers (the same (row, butterfly) task holds both ends)
@@ -671,6 +725,7 @@ k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
       bA[(p * RT + rr) * LD + pad_idx(k)] = packed(p, rr, k);
     }
     __syncthreads();
+    after_pass0();
     fft_ip<T, N, false, 3 * RT, NT, LD>(bA, tw);
   }
   if constexpr (!Tiles<T, N>::QFUSE) {
@@ -696,6 +751,56 @@ k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
     const T qk = (T)0.25 * (T)(k * k);
     S[scr_off(zb, 0, y, N, g.KXP) + k] = csub(P1, cscale(P2, qk));
     S[scr_off(zb, 1, y, N, g.KXP) + k] = P2;
+  }
+}
+
+// Rows of the batch for compute_qw: one item per CTA on a grid (N/RT,
+// levels), or persistent with the next item's four scratch rows
+// bulk-copied into shared memory during the current one (Tiles::QPRE), as
+// k_row_main.
+template <typename T, int N>
+__global__ void __launch_bounds__(Tiles<T, N>::QTHREADS, Tiles<T, N>::QMINB)
+k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg, int nitems, int* __restrict__ wflag) {
+  constexpr int RT = Tiles<T, N>::RRT, LD = Tiles<T, N>::LD, NT = Tiles<T, N>::QTHREADS;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
+  cplx<T>* bA = tw + N;               // [3][RT][LD]; then, in place, (P1, P2) in the first RT
+  load_tw<T, N>(tw, twg, NT);
+  if constexpr (Tiles<T, N>::QPRE) {
+    constexpr int NGY = N / RT;
+    cplx<T>* stg = bA + 3 * RT * LD;                 // [4][RT][KXP]: the item's scratch rows
+    const unsigned bar = smem_u32(stg + 4 * RT * g.KXP);
+    const unsigned fb = (unsigned)(RT * g.KXP * sizeof(cplx<T>));
+    auto issue = [&](int it) {
+      const int zb = it / NGY, y0 = (it % NGY) * RT;
+      mbar_expect_tx(bar, 4u * fb);
+#pragma unroll
+      for (int f = 0; f < 4; ++f) bulk_g2s(stg + f * RT * g.KXP, S + scr_off(zb, f, y0, N, g.KXP), fb, bar);
+    };
+    if (threadIdx.x == 0) {
+      mbar_init(bar, 1);
+      if ((int)blockIdx.x < nitems) issue(blockIdx.x);
+    }
+    __syncthreads();
+    unsigned ph = 0;
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x, ph ^= 1u) {
+      const bool ok = mbar_wait(bar, ph);
+      if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) { atomicOr(wflag, 1); (void)mbar_wait(bar, ph); }
+        return;
+      }
+      const int nxt = it + (int)gridDim.x;
+      row_qw_item<T, N>(g, S, tw, bA, it / NGY, (it % NGY) * RT,
+                        [&](int f, int rr) -> const cplx<T>* { return stg + (f * RT + rr) * g.KXP; },
+                        [&]() {
+                          if (threadIdx.x == 0 && nxt < nitems) { fence_proxy_async(); issue(nxt); }
+                        });
+    }
+  } else {
+    const int zb = blockIdx.y, y0 = blockIdx.x * RT;
+    row_qw_item<T, N>(g, S, tw, bA, zb, y0,
+                      [&](int f, int rr) -> const cplx<T>* { return S + scr_off(zb, f, y0 + rr, N, g.KXP); },
+                      []() {});
   }
 }
 
