@@ -301,6 +301,15 @@ int qg_autotune(const qg_config* cfg, int nsteps, qg_tuning* out);
  * nothing needs clearing between calls.  Errors: qg_last_error(NULL). */
 int qg_fft_c2r_noalloc(const double* kvar, double* rvar, int n, int nz, void* stream);
 
+/* Self-check of the mixed path's FP32 <-> FP64 conversions, which the FP64
+ * column solves (elliptic.f90:145-460) and diagnostics do with integer
+ * operations to keep the FP64 pipe free: every FP32 bit pattern and 2^32
+ * FP64 patterns (all sign/exponent fields, rounding-boundary mantissas)
+ * converted both ways on `device` and compared bit for bit with the
+ * hardware conversions.  Returns the mismatch counts (0 and 0 expected).
+ * Errors: qg_last_error(NULL). */
+int qg_selftest_conversions(int device, long long* mismatches32, long long* mismatches64);
+
 #ifdef __cplusplus
 }
 #endif

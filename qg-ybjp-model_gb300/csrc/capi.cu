@@ -274,6 +274,14 @@ int qg_destroy(qg_handle* h) {
   return QG_OK;
 }
 
+int qg_selftest_conversions(int device, long long* mismatches32, long long* mismatches64) {
+  if (!mismatches32 || !mismatches64) return fail(nullptr, QG_ERR_ARG, "qg_selftest_conversions: null pointer");
+  std::string e;
+  const int rc = qg::selftest_conversions(device, mismatches32, mismatches64, e);
+  if (rc) return fail(nullptr, rc, e);
+  return QG_OK;
+}
+
 const char* qg_last_error(const qg_handle* h) {
   if (!h) return g_create_err.c_str();
   if (!h->err.empty()) return h->err.c_str();

@@ -84,5 +84,8 @@ bool supported_n(int n);
 // Error text of calls made without a handle (qg_create, qg_fft_c2r_noalloc),
 // returned by qg_last_error(NULL) on the calling thread.
 void set_handleless_error(const std::string& msg);
+// mismatches of the integer FP32<->FP64 conversions of the mixed solve
+// against the hardware conversions (engine_fp32.cu)
+int selftest_conversions(int device, long long* bad32, long long* bad64, std::string& err);
 
 }  // namespace qg

@@ -899,22 +899,58 @@ __global__ void k_dissipation(Geom g, double nuz, double dz, const cplx<T>* __re
 //     substitution is one fused multiply-add on the recurrence,
 //     x_i = fma(-(u_i/d'_i), x_{i+1}, (s/d'_i) c_i).
 // The FP32 <-> FP64 conversions of the mixed path are done with integer
-// operations (exact, round-to-nearest-even like the hardware conversions),
-// which keeps them off the FP64 pipe that bounds this kernel.
+// operations only (exact, round-to-nearest-even like the hardware
+// conversions, every class of input included), which keeps them off the
+// FP64 pipe that bounds this kernel: a fallback to the hardware conversion
+// for the rare classes would be predicated into every conversion and still
+// take an FP64-pipe issue slot.  qg_selftest_conversions compares both with
+// the hardware conversions bit for bit.
 __device__ __forceinline__ double f32_to_f64(float v) {
   const unsigned b = __float_as_uint(v);
-  const unsigned e = (b >> 23) & 0xffu;
-  if (e == 0u || e == 0xffu) return (double)v;              // zero, subnormal, inf, nan: hardware
-  const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
-  return __hiloint2double((int)hi, (int)(b << 29));
+  const unsigned s = b & 0x80000000u, e = (b >> 23) & 0xffu, m = b & 0x7fffffu;
+  unsigned hi, lo;
+  if (e - 1u < 0xfeu) {                       // normal: rebias 127 -> 1023
+    hi = s | ((e + 896u) << 20) | (m >> 3);
+    lo = m << 29;
+  } else if (e == 0xffu) {                    // inf; nan made quiet
+    hi = s | 0x7ff00000u | (m >> 3) | (m ? 0x80000u : 0u);
+    lo = m << 29;
+  } else if (m == 0u) {                       // signed zero
+    hi = s;
+    lo = 0u;
+  } else {                                    // subnormal m * 2^-149: normalise
+    const int p = 31 - __clz((int)m);         // leading one, 0..22
+    const unsigned long long f = (unsigned long long)(m ^ (1u << p)) << (52 - p);
+    hi = s | ((unsigned)(p + 874) << 20) | (unsigned)(f >> 32);
+    lo = (unsigned)f;
+  }
+  return __hiloint2double((int)hi, (int)lo);
 }
 __device__ __forceinline__ float f64_to_f32(double v) {
   const unsigned hi = (unsigned)__double2hiint(v), lo = (unsigned)__double2loint(v);
-  const int e = (int)((hi >> 20) & 0x7ffu) - 896;
-  if (e <= 0 || e >= 255) return (float)v;                  // zero, subnormal, overflow, inf, nan: hardware
-  unsigned r = (hi & 0x80000000u) | ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
-  const unsigned rest = lo & 0x1fffffffu;                   // the 29 dropped mantissa bits
-  if (rest > 0x10000000u || (rest == 0x10000000u && (r & 1u))) r += 1u;   // nearest, ties to even
+  const unsigned s = hi & 0x80000000u;
+  const int E = (int)((hi >> 20) & 0x7ffu);
+  const int e = E - 896;                      // float exponent field if normal
+  unsigned r;
+  if (E == 0x7ff) {                           // inf; nan made quiet
+    const unsigned mh = hi & 0xfffffu;
+    r = (mh | lo) ? (s | 0x7fc00000u | (mh << 3) | (lo >> 29)) : (s | 0x7f800000u);
+  } else if (e >= 255) {                      // overflow
+    r = s | 0x7f800000u;
+  } else if (e > 0) {                         // normal: keep 23 bits, round to nearest even
+    r = s | ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned rest = lo & 0x1fffffffu;   // the 29 dropped mantissa bits
+    if (rest > 0x10000000u || (rest == 0x10000000u && (r & 1u))) r += 1u;   // may carry into inf
+  } else {                                    // float subnormal or zero: round(M * 2^(E-926))
+    const int sh = 926 - E;                   // >= 30
+    if (sh > 54 || E == 0) {
+      r = s;                                  // below half the smallest subnormal
+    } else {
+      const unsigned long long M = (1ull << 52) | ((unsigned long long)(hi & 0xfffffu) << 32) | lo;
+      const unsigned long long q = M >> sh, rem = M & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+      r = s | (unsigned)(q + ((rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull));
+    }
+  }
   return __uint_as_float(r);
 }
 template <typename T> __device__ __forceinline__ double to64(T v) { return (double)v; }

@@ -365,3 +365,15 @@ def test_autotune_picks_a_timed_candidate():
     assert np.array_equal(outs[0], outs[1])
     with pytest.raises(QgError):
         Simulation(p2, "mixed", solve_columns=48)
+
+
+def test_integer_conversions_match_hardware():
+    """The FP32 <-> FP64 conversions the mixed path's FP64 solves and
+    diagnostics do with integer operations equal the hardware conversions
+    bit for bit: every FP32 pattern, 2^32 FP64 patterns with rounding ties."""
+    import ctypes as C
+
+    from qgybj._lib import QG_OK, lib
+    a, b = C.c_longlong(-1), C.c_longlong(-1)
+    assert lib().qg_selftest_conversions(0, C.byref(a), C.byref(b)) == QG_OK
+    assert (a.value, b.value) == (0, 0)
