@@ -29,6 +29,15 @@ __host__ __device__ __forceinline__ long long scr_off(int zb, int f, int y, int 
   return (((long long)zb * kNScr + f) * n + y) * KXP;
 }
 
+// Programmatic dependent launch: pdl_trigger lets the next kernel of the
+// stream be scheduled once every CTA of this one has started (its CTAs then
+// take the SM slots this kernel's last wave leaves free); pdl_wait blocks
+// until the previous kernel has completed and its writes are visible.  Both
+// are no-ops for a launch without a programmatic dependency.  Every step
+// kernel calls pdl_wait before it reads or writes global data.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+
 // ---------------------------------------------------------------------------
 // column helpers
 // ---------------------------------------------------------------------------
@@ -54,6 +63,7 @@ constexpr bool kRowPass0 = true;   // row kernels: first inverse pass fed from r
 constexpr bool kRowFuse = true;    // k_row_main: inverse last pass, products, forward first pass in registers
 constexpr int kRowMainMinB = 2;    // k_row_main CTAs per SM when fused
 constexpr bool kRowPrefetch = true; // fused row kernels: persistent, next item's rows bulk-copied ahead
+constexpr bool kStepPdl = true;     // step kernels launched with programmatic dependencies
 constexpr bool kUpdLean = true;    // k_col_update (FP32): smaller shared footprint ...
 constexpr bool kUpdStage16 = true; // k_col_update (FP32): state staged by 16-byte copies
 constexpr int kUpdMinB = 2;        // ... for this many CTAs per SM
@@ -157,7 +167,9 @@ k_col_inv(Geom g, int zbase, const cplx<T>* __restrict__ psi, const cplx<T>* __r
   cplx<T>* sm = tw + N;                        // [3][FS]
   const int zb = blockIdx.y, z = zbase + zb;
   const int kx0 = blockIdx.x * CT;
+  pdl_trigger();
   load_tw<T, N>(tw, twg, NT);
+  pdl_wait();
   __syncthreads();
   const long long zoff = (long long)z * g.plane;
   // u = -i ky psi (derivatives.f90:1309), v = i kx psi (1310), zeta = -kh^2 psi (842)
@@ -361,7 +373,9 @@ k_row_main(Geom g, StepParams sp, cplx<T>* __restrict__ S, const cplx<T>* __rest
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   // [4][RT][LD]: (u,v), (zeta,q), (br,bi); then, in place, the 4 products
   cplx<T>* bA = tw + N;
+  pdl_trigger();
   load_tw<T, N>(tw, twg, NT);
+  pdl_wait();
   if constexpr (Tiles<T, N>::RPRE) {
     constexpr int NGY = N / RT;
     cplx<T>* stg = bA + 4 * RT * LD;                 // [6][RT][KXP]: the item's scratch rows
@@ -466,7 +480,9 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
   const int zb = blockIdx.y, z = zbase + zb;
   const int kx0 = blockIdx.x * CT;
   const int KY = g.KY;
+  pdl_trigger();
   load_tw<T, N>(tw, twg, NT);
+  pdl_wait();
   const T inv_n2 = (T)1 / ((T)N * (T)N);
   const long long zoff = (long long)z * g.plane;
   const T dt = (T)sp.delt;
@@ -765,7 +781,9 @@ k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg, int n
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* bA = tw + N;               // [3][RT][LD]; then, in place, (P1, P2) in the first RT
+  pdl_trigger();
   load_tw<T, N>(tw, twg, NT);
+  pdl_wait();
   if constexpr (Tiles<T, N>::QPRE) {
     constexpr int NGY = N / RT;
     cplx<T>* stg = bA + 3 * RT * LD;                 // [4][RT][KXP]: the item's scratch rows
@@ -818,7 +836,9 @@ k_col_qw(Geom g, StepParams sp, int zbase, const cplx<T>* __restrict__ q, cplx<T
   cplx<T>* sm = tw + N;                 // [2][FS]
   const int zb = blockIdx.y, z = zbase + zb;
   const int kx0 = blockIdx.x * CT;
+  pdl_trigger();
   load_tw<T, N>(tw, twg, NT);
+  pdl_wait();
   __syncthreads();
   const T inv_n2 = (T)1 / ((T)N * (T)N);
   const T s = (T)sp.Ro * (T)sp.W2F;
@@ -984,6 +1004,8 @@ k_solve(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
   constexpr bool EXACT = sizeof(T) == 8;
   constexpr int TC = kSolveTC, NTH = kSolveThreads, S = kSeg;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  pdl_trigger();
+  pdl_wait();
   const int n3 = g.n3;
   double* du_s = reinterpret_cast<double*>(smem_raw);
   double* ck = du_s + n3 + threadIdx.x;           // checkpoint of segment j at ck[j*NTH]
@@ -1078,6 +1100,8 @@ k_solve_st(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
   constexpr bool EXACT = sizeof(T) == 8;
   constexpr int S = kSeg, NTH = 6 * TC;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  pdl_trigger();
+  pdl_wait();
   const int n3 = g.n3;
   double* du_s = reinterpret_cast<double*>(smem_raw);
   for (int i = threadIdx.x; i < n3; i += NTH) du_s[i] = du[i];
