@@ -41,11 +41,11 @@ FALLBACK_HBM_GBS = 6800.0
 # levels it covers, so the roofline entry scales it by the levels per launch
 # of the run.
 MEASURED_TRAFFIC_PER_LEVEL = {
-    ("col_inv", 512, "mixed"): 66.61e6 / 13,
-    ("row_main", 512, "mixed"): 8.451e6 / 13,
-    ("col_update", 512, "mixed"): 117.89e6 / 13,
-    ("row_qw", 512, "mixed"): 8.739e6 / 13,
-    ("col_qw", 512, "mixed"): 9.774e6 / 13,
+    ("col_inv", 512, "mixed"): 66.63e6 / 13,
+    ("row_main", 512, "mixed"): 12.48e6 / 13,
+    ("col_update", 512, "mixed"): 121.15e6 / 13,
+    ("row_qw", 512, "mixed"): 8.810e6 / 13,
+    ("col_qw", 512, "mixed"): 9.815e6 / 13,
 }
 
 
@@ -582,7 +582,8 @@ def run_reference(args, world, rank, local):
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 300; c4: the 50 steps the adjoint objective is defined over)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--config", default="c2")
@@ -601,6 +602,8 @@ def main(argv=None):
     ap.add_argument("--ckpt", type=int, default=10, help="c4: checkpoint spacing of the adjoint")
     ap.add_argument("--levels-per-batch", type=int, default=0, help="override the phase-A batch depth")
     args = ap.parse_args(argv)
+    if args.steps is None:
+        args.steps = 50 if args.config == "c4" else 300
     if args.warmup < 3:
         args.warmup = 3
     world, rank, local = dist_env()
