@@ -704,38 +704,38 @@ class Engine : public EngineBase {
         const dim3 gc(g.KXP / Tiles<T, NN>::CT, zc), gr(g.n / Tiles<T, NN>::RRT, zc),
             grm(g.n / Tiles<T, NN>::RTM, zc);
         if (int rc0 = pbeg(QG_K_COL_INV)) return rc0;
-        if (int rc0 = launch_pdl(k_col_inv<T, NN>, gc, kColThreads, sm_ci<NN>(3), g, z0, F[F_PSI], F[F_Q], F[F_BR],
-                                 F[F_BI], S, tw)) return rc0;
+        k_col_inv<T, NN><<<gc, kColThreads, sm_ci<NN>(3), st>>>(g, z0, F[F_PSI], F[F_Q], F[F_BR], F[F_BI], S, tw);
+        QG_LAUNCHED();
         if (int rc0 = pend()) return rc0;
         if (int rc0 = pbeg(QG_K_ROW_MAIN)) return rc0;
         if constexpr (Tiles<T, NN>::RPRE) {
           const int items = zc * (NN / Tiles<T, NN>::RTM);
-          if (int rc0 = launch_pdl(k_row_main<T, NN>, dim3(std::min(items, nsm * occ_rm)), kRowThreads,
-                                   sm_rm<NN>(g.KXP), g, s, S, tw, items, wflag)) return rc0;
+          k_row_main<T, NN><<<std::min(items, nsm * occ_rm), kRowThreads, sm_rm<NN>(g.KXP), st>>>(g, s, S, tw, items,
+                                                                                                 wflag);
         } else {
-          if (int rc0 = launch_pdl(k_row_main<T, NN>, grm, kRowThreads, sm_rm<NN>(g.KXP), g, s, S, tw, 0, wflag))
-            return rc0;
+          k_row_main<T, NN><<<grm, kRowThreads, sm_rm<NN>(g.KXP), st>>>(g, s, S, tw, 0, wflag);
         }
+        QG_LAUNCHED();
         if (int rc0 = pend()) return rc0;
         if (int rc0 = pbeg(QG_K_COL_UPDATE)) return rc0;
-        if (int rc0 = launch_pdl(k_col_update<T, NN>, gc, kColThreads, UpdLay<T, NN>::bytes(), g, s, z0, sptr,
-                                 (const T*)e1, (const T*)e2, (const T*)e1w, (const T*)e2w, S, tw, need_qw ? 1 : 0))
-          return rc0;
+        k_col_update<T, NN><<<gc, kColThreads, UpdLay<T, NN>::bytes(), st>>>(g, s, z0, sptr, e1, e2, e1w, e2w, S, tw,
+                                                                need_qw ? 1 : 0);
+        QG_LAUNCHED();
         if (int rc0 = pend()) return rc0;
         if (need_qw) {
           if (int rc0 = pbeg(QG_K_ROW_QW)) return rc0;
           if constexpr (Tiles<T, NN>::QPRE) {
             const int items = zc * (NN / Tiles<T, NN>::RRT);
-            if (int rc0 = launch_pdl(k_row_qw<T, NN>, dim3(std::min(items, nsm * occ_rq)), Tiles<T, NN>::QTHREADS,
-                                     sm_rq<NN>(g.KXP), g, S, tw, items, wflag)) return rc0;
+            k_row_qw<T, NN><<<std::min(items, nsm * occ_rq), Tiles<T, NN>::QTHREADS, sm_rq<NN>(g.KXP), st>>>(
+                g, S, tw, items, wflag);
           } else {
-            if (int rc0 = launch_pdl(k_row_qw<T, NN>, gr, Tiles<T, NN>::QTHREADS, sm_rq<NN>(g.KXP), g, S, tw, 0, wflag))
-              return rc0;
+            k_row_qw<T, NN><<<gr, Tiles<T, NN>::QTHREADS, sm_rq<NN>(g.KXP), st>>>(g, S, tw, 0, wflag);
           }
+          QG_LAUNCHED();
           if (int rc0 = pend()) return rc0;
           if (int rc0 = pbeg(QG_K_COL_QW)) return rc0;
-          if (int rc0 = launch_pdl(k_col_qw<T, NN>, gc, kThreadsB, sm_ci<NN>(2), g, s, z0, (const C*)F[F_Q],
-                                   F[F_QSTAR], (const C*)S, tw)) return rc0;
+          k_col_qw<T, NN><<<gc, kThreadsB, sm_ci<NN>(2), st>>>(g, s, z0, F[F_Q], F[F_QSTAR], S, tw);
+          QG_LAUNCHED();
           if (int rc0 = pend()) return rc0;
         }
       });
@@ -753,25 +753,6 @@ class Engine : public EngineBase {
     return pend();
   }
 
-  // Launch on st with a programmatic dependency on the stream's previous
-  // kernel (the step kernels call pdl_wait before touching global data, so
-  // only their launch and preamble overlap the previous kernel's tail).
-  template <typename... KP, typename... A>
-  int launch_pdl(void (*k)(KP...), dim3 grid, dim3 block, size_t smem, A&&... args) {
-    cudaLaunchConfig_t lc = {};
-    lc.gridDim = grid;
-    lc.blockDim = block;
-    lc.dynamicSmemBytes = smem;
-    lc.stream = st;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = kStepPdl ? 1 : 0;
-    lc.attrs = at;
-    lc.numAttrs = 1;
-    QG_CK(cudaLaunchKernelEx(&lc, k, std::forward<A>(args)...));
-    return QG_OK;
-  }
-
   int launch_solve(C* qs, int do_psi, int do_A) {
     return solve_generic(qs, F[F_BR], F[F_BI], F[F_PSI], F[F_AR], F[F_AI], do_psi, do_A);
   }
@@ -780,13 +761,14 @@ class Engine : public EngineBase {
     if (!do_psi && !do_A) return QG_OK;
     if (kSolveStore && vbuf) {
 #define QG_SOLVE_ST(TCV)                                                                                   \
-  launch_pdl(k_solve_st<T, TCV>, dim3((unsigned)((g.plane + TCV - 1) / TCV)), 6 * TCV, (size_t)g.n3 * 8, g, cfg.dz, \
-             cfg.Bu, (const int*)tab_idx, (const double4*)fac_psi, (const double4*)fac_A, (const double*)du, qs, br, \
-             bi, psi, ar, ai, do_psi, do_A, vbuf)
-      if (solve_tc == 16) return QG_SOLVE_ST(16);
-      if (solve_tc == 64) return QG_SOLVE_ST(64);
-      return QG_SOLVE_ST(32);
+  k_solve_st<T, TCV><<<(unsigned)((g.plane + TCV - 1) / TCV), 6 * TCV, (size_t)g.n3 * 8, st>>>(           \
+      g, cfg.dz, cfg.Bu, tab_idx, fac_psi, fac_A, du, qs, br, bi, psi, ar, ai, do_psi, do_A, vbuf)
+      if (solve_tc == 16) QG_SOLVE_ST(16);
+      else if (solve_tc == 64) QG_SOLVE_ST(64);
+      else QG_SOLVE_ST(32);
 #undef QG_SOLVE_ST
+      QG_LAUNCHED();
+      return QG_OK;
     }
     k_solve<T><<<(unsigned)((g.plane + kSolveTC - 1) / kSolveTC), kSolveThreads, solve_smem(g.n3), st>>>(g, cfg.dz, cfg.Bu, tab_idx, fac_psi, fac_A,
                                                                            du, qs, br, bi, psi, ar, ai, do_psi, do_A);

@@ -29,15 +29,6 @@ __host__ __device__ __forceinline__ long long scr_off(int zb, int f, int y, int 
   return (((long long)zb * kNScr + f) * n + y) * KXP;
 }
 
-// Programmatic dependent launch: pdl_trigger lets the next kernel of the
-// stream be scheduled once every CTA of this one has started (its CTAs then
-// take the SM slots this kernel's last wave leaves free); pdl_wait blocks
-// until the previous kernel has completed and its writes are visible.  Both
-// are no-ops for a launch without a programmatic dependency.  Every step
-// kernel calls pdl_wait before it reads or writes global data.
-__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
-
 // ---------------------------------------------------------------------------
 // column helpers
 // ---------------------------------------------------------------------------
@@ -63,7 +54,7 @@ constexpr bool kRowPass0 = true;   // row kernels: first inverse pass fed from r
 constexpr bool kRowFuse = true;    // k_row_main: inverse last pass, products, forward first pass in registers
 constexpr int kRowMainMinB = 2;    // k_row_main CTAs per SM when fused
 constexpr bool kRowPrefetch = true; // fused row kernels: persistent, next item's rows bulk-copied ahead
-constexpr bool kStepPdl = true;     // step kernels launched with programmatic dependencies
+constexpr bool kUpdTablesSmem = true;   // k_col_update (FP32 lean): IF tables staged in shared memory
 constexpr bool kUpdLean = true;    // k_col_update (FP32): smaller shared footprint ...
 constexpr bool kUpdStage16 = true; // k_col_update (FP32): state staged by 16-byte copies
 constexpr int kUpdMinB = 2;        // ... for this many CTAs per SM
@@ -167,9 +158,7 @@ k_col_inv(Geom g, int zbase, const cplx<T>* __restrict__ psi, const cplx<T>* __r
   cplx<T>* sm = tw + N;                        // [3][FS]
   const int zb = blockIdx.y, z = zbase + zb;
   const int kx0 = blockIdx.x * CT;
-  pdl_trigger();
   load_tw<T, N>(tw, twg, NT);
-  pdl_wait();
   __syncthreads();
   const long long zoff = (long long)z * g.plane;
   // u = -i ky psi (derivatives.f90:1309), v = i kx psi (1310), zeta = -kh^2 psi (842)
@@ -373,9 +362,7 @@ k_row_main(Geom g, StepParams sp, cplx<T>* __restrict__ S, const cplx<T>* __rest
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   // [4][RT][LD]: (u,v), (zeta,q), (br,bi); then, in place, the 4 products
   cplx<T>* bA = tw + N;
-  pdl_trigger();
   load_tw<T, N>(tw, twg, NT);
-  pdl_wait();
   if constexpr (Tiles<T, N>::RPRE) {
     constexpr int NGY = N / RT;
     cplx<T>* stg = bA + 4 * RT * LD;                 // [6][RT][KXP]: the item's scratch rows
@@ -435,13 +422,15 @@ template <typename T, int N> struct UpdLay {
   // the four q^w inverse transforms reuse the transform and staging regions
   static constexpr int PAD = 4 * ColLay<N, CT>::FS > 2 * ColLay<N, CT>::FS + 3 * FE
                                  ? 4 * ColLay<N, CT>::FS - 2 * ColLay<N, CT>::FS - 3 * FE : 0;
-  // lean (FP32): IF tables read from global memory, B^{n+1} re-read from
-  // global memory for the q^w transforms (two passes of two), so that three
-  // CTAs fit per SM
+  // lean (FP32): B^{n+1} re-read from global memory for the q^w transforms
+  // (two passes of two) instead of kept in shared memory
   static constexpr bool LEAN = kUpdLean && sizeof(T) == 4;
   static constexpr int MINB = LEAN ? kUpdMinB : Tiles<T, N>::MINB;
+  // lean with the IF tables of the variable staged after the state
+  // (kUpdTablesSmem) or read from global memory in the epilogue
+  static constexpr bool GTAB = LEAN && !kUpdTablesSmem;
   static constexpr size_t bytes() {
-    return LEAN ? (size_t)(N + 2 * ColLay<N, CT>::FS + 3 * FE) * sizeof(cplx<T>)
+    return LEAN ? (size_t)(N + 2 * ColLay<N, CT>::FS + 3 * FE) * sizeof(cplx<T>) + (GTAB ? 0 : (size_t)2 * FE * sizeof(T))
                 : (size_t)(N + 2 * ColLay<N, CT>::FS + 5 * FE + PAD) * sizeof(cplx<T>) + (size_t)2 * FE * sizeof(T);
   }
 };
@@ -475,14 +464,13 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
   cplx<T>* sm = tw + N;                          // [2][FS]
   cplx<T>* stg = sm + 2 * ColLay<N, CT>::FS;     // [3][FE]: x, x_old, third (dq / AI / AR)
   cplx<T>* bnew = stg + 3 * FE + L::PAD;         // [2][FE]: BR, BI at n+1 (not LEAN)
-  T* tab = reinterpret_cast<T*>(bnew + 2 * FE);  // [2][FE]: e1, e2 or e1w, e2w (not LEAN)
+  // [2][FE]: e1, e2 or e1w, e2w (not GTAB)
+  T* tab = reinterpret_cast<T*>(L::LEAN ? stg + 3 * FE : bnew + 2 * FE);
   const int tid = threadIdx.x;
   const int zb = blockIdx.y, z = zbase + zb;
   const int kx0 = blockIdx.x * CT;
   const int KY = g.KY;
-  pdl_trigger();
   load_tw<T, N>(tw, twg, NT);
-  pdl_wait();
   const T inv_n2 = (T)1 / ((T)N * (T)N);
   const long long zoff = (long long)z * g.plane;
   const T dt = (T)sp.delt;
@@ -519,8 +507,17 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
         if (need3) cp_async_c<T>(stg + 2 * FE + e, in ? X3 + m : X3, in);
       }
     }
-    if constexpr (!L::LEAN) {
-      if (which < 2) {
+    if constexpr (!L::GTAB) {
+      if (which < 2 && sizeof(T) == 4 && CT * sizeof(T) == 16) {
+        // FP32: one 16-byte copy per row of the tile (the tables' rows hold KXP entries)
+        const T* t1 = which == 0 ? e1t : e1wt;
+        const T* t2 = which == 0 ? e2t : e2wt;
+        for (int e = tid; e < 2 * KY; e += NT) {
+          const int row = e >> 1;
+          const long long mt = (long long)row * g.KXP + kx0;
+          cp_async_16(tab + (e & 1) * FE + row * CT, ((e & 1) ? t2 : t1) + mt, 16);
+        }
+      } else if (which < 2) {
         for (int e = tid; e < CT * KY; e += NT) {
           const int c = e % CT, row = e / CT;
           const int kx = kx0 + c;
@@ -572,7 +569,7 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
           if (which == 0) {
             const cplx<T> dqv = sp.use_dq ? stg[2 * FE + e] : mk<T>(0, 0);
             const long long mt = (long long)row * g.KXP + kx;
-            const T e1 = L::LEAN ? e1t[mt] : tab[e], e2 = L::LEAN ? e2t[mt] : tab[FE + e];
+            const T e1 = L::GTAB ? e1t[mt] : tab[e], e2 = L::GTAB ? e2t[mt] : tab[FE + e];
             if (eul) {
               xn = cscale(cadd(csub(xo, cscale(tnd, dt)), cscale(dqv, dt)), e1);
             } else {
@@ -580,7 +577,7 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
             }
           } else {
             const long long mt = (long long)row * g.KXP + kx;
-            const T e1w = L::LEAN ? e1wt[mt] : tab[e], e2w = L::LEAN ? e2wt[mt] : tab[FE + e];
+            const T e1w = L::GTAB ? e1wt[mt] : tab[e], e2w = L::GTAB ? e2wt[mt] : tab[FE + e];
             const T ck = cdisp * (T)(kx * kx + ky * ky);
             // nBR - 0.5 rBI + c kh2 AI ; nBI + 0.5 rBR - c kh2 AR
             const cplx<T> a3 = stg[2 * FE + e];
@@ -781,9 +778,7 @@ k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg, int n
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* bA = tw + N;               // [3][RT][LD]; then, in place, (P1, P2) in the first RT
-  pdl_trigger();
   load_tw<T, N>(tw, twg, NT);
-  pdl_wait();
   if constexpr (Tiles<T, N>::QPRE) {
     constexpr int NGY = N / RT;
     cplx<T>* stg = bA + 3 * RT * LD;                 // [4][RT][KXP]: the item's scratch rows
@@ -836,9 +831,7 @@ k_col_qw(Geom g, StepParams sp, int zbase, const cplx<T>* __restrict__ q, cplx<T
   cplx<T>* sm = tw + N;                 // [2][FS]
   const int zb = blockIdx.y, z = zbase + zb;
   const int kx0 = blockIdx.x * CT;
-  pdl_trigger();
   load_tw<T, N>(tw, twg, NT);
-  pdl_wait();
   __syncthreads();
   const T inv_n2 = (T)1 / ((T)N * (T)N);
   const T s = (T)sp.Ro * (T)sp.W2F;
@@ -1004,8 +997,6 @@ k_solve(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
   constexpr bool EXACT = sizeof(T) == 8;
   constexpr int TC = kSolveTC, NTH = kSolveThreads, S = kSeg;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  pdl_trigger();
-  pdl_wait();
   const int n3 = g.n3;
   double* du_s = reinterpret_cast<double*>(smem_raw);
   double* ck = du_s + n3 + threadIdx.x;           // checkpoint of segment j at ck[j*NTH]
@@ -1100,8 +1091,6 @@ k_solve_st(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
   constexpr bool EXACT = sizeof(T) == 8;
   constexpr int S = kSeg, NTH = 6 * TC;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  pdl_trigger();
-  pdl_wait();
   const int n3 = g.n3;
   double* du_s = reinterpret_cast<double*>(smem_raw);
   for (int i = threadIdx.x; i < n3; i += NTH) du_s[i] = du[i];
