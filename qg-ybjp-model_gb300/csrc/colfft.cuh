@@ -167,7 +167,7 @@ __device__ __forceinline__ void col_fft(cplx<T>* __restrict__ sm, const cplx<T>*
 // v[f][r] with the input at index j + r*N/R0.  Threads take tasks (rr, j)
 // with j fastest (coalesced row reads).  The remaining passes are
 // ip_passes<..., radix_of(N)> after a barrier.
-template <typename T, int N, bool FWD, int NF, int RT, int NT, int LD, class Pro>
+template <typename T, int N, bool FWD, int NF, int RT, int NT, int LD, int LAY = 0, class Pro>
 __device__ __forceinline__ void row_pass0(cplx<T>* __restrict__ sm, Pro pro) {
   constexpr int R = radix_of(N);
   constexpr int NB = N / R;
@@ -184,7 +184,7 @@ __device__ __forceinline__ void row_pass0(cplx<T>* __restrict__ sm, Pro pro) {
       for (int f = 0; f < NF; ++f) {
         dftR<T, R, FWD>(v[f]);
 #pragma unroll
-        for (int r = 0; r < R; ++r) sm[(f * RT + rr) * LD + pad_idx(j * R + r)] = v[f][r];
+        for (int r = 0; r < R; ++r) sm[(f * RT + rr) * LD + lay_idx<LAY>(j * R + r)] = v[f][r];
       }
     }
   }
@@ -192,12 +192,12 @@ __device__ __forceinline__ void row_pass0(cplx<T>* __restrict__ sm, Pro pro) {
 
 // In-place Stockham passes (ip_pass) from stride NS up to, not including,
 // the last pass.
-template <typename T, int N, bool FWD, int BATCH, int NT, int LD, int NS>
+template <typename T, int N, bool FWD, int BATCH, int NT, int LD, int NS, int LAY = 0>
 __device__ __forceinline__ void ip_passes_but_last(cplx<T>* buf, const cplx<T>* tw) {
   if constexpr (NS < LastNS<N>::value) {
     constexpr int R = radix_of(N / NS);
-    ip_pass<T, N, R, NS, FWD, BATCH, NT, LD>(buf, tw);
-    ip_passes_but_last<T, N, FWD, BATCH, NT, LD, NS * R>(buf, tw);
+    ip_pass<T, N, R, NS, FWD, BATCH, NT, LD, LAY>(buf, tw);
+    ip_passes_but_last<T, N, FWD, BATCH, NT, LD, NS * R, LAY>(buf, tw);
   }
 }
 

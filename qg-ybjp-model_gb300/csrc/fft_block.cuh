@@ -138,6 +138,22 @@ namespace qg {
 __host__ __device__ __forceinline__ constexpr int pad_idx(int i) { return i + (i >> 4); }
 template <int N> struct PadLD { static constexpr int value = N + (N >> 4); };
 
+// Element placement of a transform: LAY 0 is pad_idx; LAY 1 (radix-8
+// transforms of N = 512, one task per butterfly) permutes each aligned group
+// of 16 elements, i ^ h(i/16) with h(m) = (m & 7) | ((m & 4) << 1): the
+// first pass's writes (index 8j + r), the middle pass's writes (index
+// 64(j/8) + j%8 + 8r) and all reads (index j + 64r) of 16 consecutive tasks
+// then fall on 16 distinct 8-byte bank pairs, where pad_idx leaves the middle
+// pass's writes two-way conflicted.  No padding: N entries per transform.
+template <int LAY> __host__ __device__ __forceinline__ constexpr int lay_idx(int i) {
+  if constexpr (LAY == 0) {
+    return pad_idx(i);
+  } else {
+    const int m = i >> 4;
+    return i ^ ((m & 7) | ((m & 4) << 1));
+  }
+}
+
 // Twiddles laid out per pass: the pass with stride NS and radix R reads
 // W_N^{k r N/(NS R)} at tw[off(NS) + (r-1)*NS + k], so the threads of a warp
 // (consecutive k) read consecutive words.  Fewer than N entries in total.
@@ -163,7 +179,7 @@ __device__ __forceinline__ void load_tw_passes(cplx<T>* tw_s, const cplx<T>* __r
   }
 }
 
-template <typename T, int N, int R, int NS, bool FWD, int BATCH, int NT, int LD>
+template <typename T, int N, int R, int NS, bool FWD, int BATCH, int NT, int LD, int LAY = 0>
 __device__ __forceinline__ void ip_pass(cplx<T>* __restrict__ buf, const cplx<T>* __restrict__ tw) {
   constexpr int NB = N / R;
   constexpr int TASKS = BATCH * NB;
@@ -177,7 +193,7 @@ __device__ __forceinline__ void ip_pass(cplx<T>* __restrict__ buf, const cplx<T>
       const int b = t / NB, j = t % NB;
       const cplx<T>* s = buf + b * LD;
 #pragma unroll
-      for (int r = 0; r < R; ++r) v[p][r] = s[pad_idx(j + r * NB)];
+      for (int r = 0; r < R; ++r) v[p][r] = s[lay_idx<LAY>(j + r * NB)];
     }
   }
   __syncthreads();
@@ -200,18 +216,18 @@ __device__ __forceinline__ void ip_pass(cplx<T>* __restrict__ buf, const cplx<T>
       cplx<T>* d = buf + b * LD;
       const int base = (j - k) * R + k;
 #pragma unroll
-      for (int r = 0; r < R; ++r) d[pad_idx(base + r * NS)] = v[p][r];
+      for (int r = 0; r < R; ++r) d[lay_idx<LAY>(base + r * NS)] = v[p][r];
     }
   }
   __syncthreads();
 }
 
-template <typename T, int N, bool FWD, int BATCH, int NT, int LD, int NS>
+template <typename T, int N, bool FWD, int BATCH, int NT, int LD, int NS, int LAY = 0>
 __device__ __forceinline__ void ip_passes(cplx<T>* buf, const cplx<T>* tw) {
   if constexpr (NS < N) {
     constexpr int R = PassRadix<N / NS>::value;
-    ip_pass<T, N, R, NS, FWD, BATCH, NT, LD>(buf, tw);
-    ip_passes<T, N, FWD, BATCH, NT, LD, NS * R>(buf, tw);
+    ip_pass<T, N, R, NS, FWD, BATCH, NT, LD, LAY>(buf, tw);
+    ip_passes<T, N, FWD, BATCH, NT, LD, NS * R, LAY>(buf, tw);
   }
 }
 

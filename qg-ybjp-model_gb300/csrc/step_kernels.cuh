@@ -54,6 +54,8 @@ constexpr bool kRowPass0 = true;   // row kernels: first inverse pass fed from r
 constexpr bool kRowFuse = true;    // k_row_main: inverse last pass, products, forward first pass in registers
 constexpr int kRowMainMinB = 2;    // k_row_main CTAs per SM when fused
 constexpr bool kRowPrefetch = true; // fused row kernels: persistent, next item's rows bulk-copied ahead
+constexpr bool kRowSwizzle = true;  // k_row_qw (N = 512): conflict-free XOR placement (lay_idx<1>)
+constexpr bool kRowMainSwizzle = false;  // k_row_main: the same (its index arithmetic spills at 128 registers)
 constexpr bool kUpdTablesSmem = true;   // k_col_update (FP32 lean): IF tables staged in shared memory
 constexpr bool kUpdLean = true;    // k_col_update (FP32): smaller shared footprint ...
 constexpr bool kUpdStage16 = true; // k_col_update (FP32): state staged by 16-byte copies
@@ -106,6 +108,9 @@ template <typename T, int N> struct Tiles {
   // shared memory during the current item (the fused FP32 row kernels)
   static constexpr bool RPRE = kRowPrefetch && RFUSE;
   static constexpr bool QPRE = kRowPrefetch && QFUSE;
+  // element placement of the fused row kernels' transforms (lay_idx)
+  static constexpr int RLAY = kRowMainSwizzle && RFUSE && N == 512 ? 1 : 0;
+  static constexpr int QLAY = kRowSwizzle && QFUSE && N == 512 ? 1 : 0;
   static constexpr int CIMINB = imin(CB == 8 ? kColInvMinB : 2, smem_ctas((N + 3 * FSC) * CB));
   static constexpr int CQMINB = imin(CB == 8 ? kColQwMinB : 2, smem_ctas((N + 2 * FSC) * CB));
 };
@@ -220,10 +225,10 @@ __device__ __forceinline__ void unpack_spec(const cplx<T>* F, int k, int n, cplx
   X = mk<T>((a.x + b.x) * (T)0.5, (a.y - b.y) * (T)0.5);
   Y = mk<T>((a.y + b.y) * (T)0.5, (b.x - a.x) * (T)0.5);
 }
-// the same on a padded shared-memory transform
-template <typename T>
+// the same on a shared-memory transform laid out by lay_idx<LAY>
+template <typename T, int LAY = 0>
 __device__ __forceinline__ void unpack_pad(const cplx<T>* F, int k, int n, cplx<T>& X, cplx<T>& Y) {
-  const cplx<T> a = F[pad_idx(k)], b = F[pad_idx(k == 0 ? 0 : n - k)];
+  const cplx<T> a = F[lay_idx<LAY>(k)], b = F[lay_idx<LAY>(k == 0 ? 0 : n - k)];
   X = mk<T>((a.x + b.x) * (T)0.5, (a.y - b.y) * (T)0.5);
   Y = mk<T>((a.y + b.y) * (T)0.5, (b.x - a.x) * (T)0.5);
 }
@@ -239,12 +244,12 @@ template <typename T, int N, class Src, class After>
 __device__ __forceinline__ void row_main_item(const Geom& g, const StepParams& sp, cplx<T>* __restrict__ S,
                                               const cplx<T>* __restrict__ tw, cplx<T>* __restrict__ bA, int zb,
                                               int y0, Src src, After after_pass0) {
-  constexpr int RT = Tiles<T, N>::RTM, LD = Tiles<T, N>::LD, NT = kRowThreads;
+  constexpr int RT = Tiles<T, N>::RTM, LD = Tiles<T, N>::LD, NT = kRowThreads, LAY = Tiles<T, N>::RLAY;
   const int tid = threadIdx.x;
   const int K = g.K;
   constexpr int R0 = radix_of(N), NB0 = N / R0;
   if constexpr (Tiles<T, N>::RPASS0) {
-    row_pass0<T, N, false, 3, RT, NT, LD>(bA, [&](int rr, int j, cplx<T> (&v)[3][R0]) {
+    row_pass0<T, N, false, 3, RT, NT, LD, LAY>(bA, [&](int rr, int j, cplx<T> (&v)[3][R0]) {
 #pragma unroll
       for (int p = 0; p < 3; ++p) {
         const cplx<T>* X = src(2 * p, rr);
@@ -257,7 +262,7 @@ __device__ __forceinline__ void row_main_item(const Geom& g, const StepParams& s
     after_pass0();
     if constexpr (Tiles<T, N>::RFUSE) {
       constexpr int NS = LastNS<N>::value, R = N / NS;     // == R0, NS == NB0
-      ip_passes_but_last<T, N, false, 3 * RT, NT, LD, R0>(bA, tw);
+      ip_passes_but_last<T, N, false, 3 * RT, NT, LD, R0, LAY>(bA, tw);
       // last inverse pass into registers: task (row, j) holds the physical
       // values at x = j + r*NS of the three packed pairs
       const int j = tid % NS, rr = tid / NS;
@@ -266,7 +271,7 @@ __device__ __forceinline__ void row_main_item(const Geom& g, const StepParams& s
 #pragma unroll
       for (int f = 0; f < 3; ++f) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[f][r] = bA[(f * RT + rr) * LD + pad_idx(j + r * NS)];
+        for (int r = 0; r < R; ++r) v[f][r] = bA[(f * RT + rr) * LD + lay_idx<LAY>(j + r * NS)];
 #pragma unroll
         for (int r = 1; r < R; ++r) {
           cplx<T> w = tw[off + (r - 1) * NS + j];
@@ -291,12 +296,12 @@ __device__ __forceinline__ void row_main_item(const Geom& g, const StepParams& s
         }
         dftR<T, R, true>(w);
 #pragma unroll
-        for (int r = 0; r < R; ++r) bA[(f * RT + rr) * LD + pad_idx(j * R + r)] = w[r];
+        for (int r = 0; r < R; ++r) bA[(f * RT + rr) * LD + lay_idx<LAY>(j * R + r)] = w[r];
       }
       __syncthreads();
-      ip_passes<T, N, true, 4 * RT, NT, LD, R0>(bA, tw);
+      ip_passes<T, N, true, 4 * RT, NT, LD, R0, LAY>(bA, tw);
     } else {
-      ip_passes<T, N, false, 3 * RT, NT, LD, R0>(bA, tw);
+      ip_passes<T, N, false, 3 * RT, NT, LD, R0, LAY>(bA, tw);
     }
   } else {
 #pragma unroll 4
@@ -331,10 +336,10 @@ __device__ __forceinline__ void row_main_item(const Geom& g, const StepParams& s
     const int k = e % (K + 1), rr = e / (K + 1);
     const int y = y0 + rr;
     cplx<T> uq, vq, ubr, vbr, ubi, vbi, zbr, zbi;
-    unpack_pad<T>(bA + (0 * RT + rr) * LD, k, N, uq, vq);
-    unpack_pad<T>(bA + (1 * RT + rr) * LD, k, N, ubr, vbr);
-    unpack_pad<T>(bA + (2 * RT + rr) * LD, k, N, ubi, vbi);
-    unpack_pad<T>(bA + (3 * RT + rr) * LD, k, N, zbr, zbi);
+    unpack_pad<T, LAY>(bA + (0 * RT + rr) * LD, k, N, uq, vq);
+    unpack_pad<T, LAY>(bA + (1 * RT + rr) * LD, k, N, ubr, vbr);
+    unpack_pad<T, LAY>(bA + (2 * RT + rr) * LD, k, N, ubi, vbi);
+    unpack_pad<T, LAY>(bA + (3 * RT + rr) * LD, k, N, zbr, zbi);
     const T kx = (T)k;
     // G = i kx F(uX) (+- refraction), H = F(vX); tendency = F_y(G) + i ky F_y(H)
     S[scr_off(zb, 0, y, N, g.KXP) + k] = cscale(cmul_i(uq), kx * adv);
@@ -670,7 +675,7 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
 template <typename T, int N, class Src, class After>
 __device__ __forceinline__ void row_qw_item(const Geom& g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ tw,
                                             cplx<T>* __restrict__ bA, int zb, int y0, Src src, After after_pass0) {
-  constexpr int RT = Tiles<T, N>::RRT, LD = Tiles<T, N>::LD, NT = Tiles<T, N>::QTHREADS;
+  constexpr int RT = Tiles<T, N>::RRT, LD = Tiles<T, N>::LD, NT = Tiles<T, N>::QTHREADS, LAY = Tiles<T, N>::QLAY;
   const int tid = threadIdx.x;
   const int K = g.K;
   // packed: (BR, BI), (BRx, BIx), (BRy, BIy)
@@ -688,7 +693,7 @@ __device__ __forceinline__ void row_qw_item(const Geom& g, cplx<T>* __restrict__
   };
   if constexpr (Tiles<T, N>::RPASS0) {
     constexpr int R0 = radix_of(N), NB0 = N / R0;
-    row_pass0<T, N, false, 3, RT, NT, LD>(bA, [&](int rr, int j, cplx<T> (&v)[3][R0]) {
+    row_pass0<T, N, false, 3, RT, NT, LD, LAY>(bA, [&](int rr, int j, cplx<T> (&v)[3][R0]) {
 #pragma unroll
       for (int p = 0; p < 3; ++p)
 #pragma unroll
@@ -700,14 +705,14 @@ __device__ __forceinline__ void row_qw_item(const Geom& g, cplx<T>* __restrict__
       // inverse last pass, the q^w products and the forward first pass in
       // registers (the same (row, butterfly) task holds both ends)
       constexpr int R0 = radix_of(N), NS = LastNS<N>::value, R = N / NS;
-      ip_passes_but_last<T, N, false, 3 * RT, NT, LD, R0>(bA, tw);
+      ip_passes_but_last<T, N, false, 3 * RT, NT, LD, R0, LAY>(bA, tw);
       const int j = tid % NS, rr = tid / NS;
       cplx<T> v[3][R];
       constexpr int off = tw_off<N>(NS);
 #pragma unroll
       for (int f = 0; f < 3; ++f) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[f][r] = bA[(f * RT + rr) * LD + pad_idx(j + r * NS)];
+        for (int r = 0; r < R; ++r) v[f][r] = bA[(f * RT + rr) * LD + lay_idx<LAY>(j + r * NS)];
 #pragma unroll
         for (int r = 1; r < R; ++r) {
           cplx<T> w = tw[off + (r - 1) * NS + j];
@@ -725,11 +730,11 @@ __device__ __forceinline__ void row_qw_item(const Geom& g, cplx<T>* __restrict__
       }
       dftR<T, R, true>(w);
 #pragma unroll
-      for (int r = 0; r < R; ++r) bA[rr * LD + pad_idx(j * R + r)] = w[r];
+      for (int r = 0; r < R; ++r) bA[rr * LD + lay_idx<LAY>(j * R + r)] = w[r];
       __syncthreads();
-      ip_passes<T, N, true, RT, NT, LD, R0>(bA, tw);
+      ip_passes<T, N, true, RT, NT, LD, R0, LAY>(bA, tw);
     } else {
-      ip_passes<T, N, false, 3 * RT, NT, LD, radix_of(N)>(bA, tw);
+      ip_passes<T, N, false, 3 * RT, NT, LD, radix_of(N), LAY>(bA, tw);
     }
   } else {
 #pragma unroll 4
@@ -760,7 +765,7 @@ __device__ __forceinline__ void row_qw_item(const Geom& g, cplx<T>* __restrict__
     const int k = e % (K + 1), rr = e / (K + 1);
     const int y = y0 + rr;
     cplx<T> P1, P2;
-    unpack_pad<T>(bA + rr * LD, k, N, P1, P2);
+    unpack_pad<T, LAY>(bA + rr * LD, k, N, P1, P2);
     const T qk = (T)0.25 * (T)(k * k);
     S[scr_off(zb, 0, y, N, g.KXP) + k] = csub(P1, cscale(P2, qk));
     S[scr_off(zb, 1, y, N, g.KXP) + k] = P2;
