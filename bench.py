@@ -525,7 +525,7 @@ def sim_batch(sim) -> int:
     n, n3 = sim.n, sim.n3
     kxp = ((kmax(n) + 1 + 7) // 8) * 8
     per = 6 * n * kxp * (8 if sim.precision == "mixed" else 16)
-    zb = sim.cfg.levels_per_batch or max(1, (48 << 20) // per)
+    zb = sim.cfg.levels_per_batch or max(1, (1280 << 20) // per)
     zb = min(zb, n3)
     nb = (n3 + zb - 1) // zb
     return (n3 + nb - 1) // nb

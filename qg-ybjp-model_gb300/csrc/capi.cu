@@ -577,15 +577,17 @@ int qg_autotune(const qg_config* cfg, int nsteps, qg_tuning* out) {
   qg_handle* h = nullptr;
   int rc = qg_create(&c, &h);
   if (rc) return rc;
-  // candidate depths: powers of two and the depths whose column-kernel grids
-  // fill an integral number of waves best, capped by a 96 MB scratch budget
+  // candidate depths: powers of two and depths whose kernel grids fill an
+  // integral number of waves well, capped by a 1.25 GB scratch budget (past
+  // L2: deep batches trade scratch traffic for fuller waves, longer
+  // persistent row kernels and fewer launches, which the timing settles)
   std::vector<int> cand;
   const int n = c.n1, n3 = c.n3;
   const size_t cbytes = c.precision == QG_PREC_FP64 ? 16 : 8;
   const int K = (int)((float)(int)((float)n / 3.0f + 0.5f) - 0.5f);
   const size_t per_level = (size_t)6 * n * (((K + 1 + 7) / 8) * 8) * cbytes;
-  const int zmax = (int)std::max<size_t>(1, std::min<size_t>((size_t)n3, (size_t)(96u << 20) / per_level));
-  for (int z : {1, 2, 3, 4, 6, 8, 11, 13, 16, 20, 24, 32, 48, 64})
+  const int zmax = (int)std::max<size_t>(1, std::min<size_t>((size_t)n3, (size_t)(1280u << 20) / per_level));
+  for (int z : {1, 2, 4, 8, 13, 16, 20, 26, 32, 43, 64, 86, 128, 192, 256})
     if (z <= zmax && (int)cand.size() < 16) cand.push_back(z);
   cudaStream_t st = (cudaStream_t)h->eng->stream();
   cudaEvent_t a, b;

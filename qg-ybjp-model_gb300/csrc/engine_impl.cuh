@@ -105,10 +105,13 @@ class Engine : public EngineBase {
     *wflag_h = 0;
     QG_CK(cudaHostGetDevicePointer(&wflag, wflag_h, 0));
     QG_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, cfg.device));
-    // phase-A batching: keep the scratch planes of one batch L2-sized
+    // phase-A batching: by default as many levels per batch as 1.25 GB of
+    // scratch planes hold (deep batches run fewer, fuller waves and longer
+    // persistent row kernels; on GB300 the 512^2x256 step is fastest with
+    // all 256 levels in one batch although its scratch outgrows L2)
     const size_t per_level = (size_t)kNScr * g.n * g.KXP * sizeof(C);
     int zb = cfg.levels_per_batch;
-    if (zb <= 0) zb = (int)std::max<size_t>(1, (size_t)(48u << 20) / per_level);
+    if (zb <= 0) zb = (int)std::max<size_t>(1, (size_t)(1280u << 20) / per_level);
     zb = std::min(zb, g.n3);
     const int nb = (g.n3 + zb - 1) / zb;
     Zb = (g.n3 + nb - 1) / nb;

@@ -109,10 +109,11 @@ class RunConfig:
 CONFIGS = {
     "c0": RunConfig("c0_64x64x64_fp64", 64, 64, "fp64", steps=200, seed=0, k0=3.0),
     # levels_per_batch, solve_columns: the choices of qg_autotune on GB300 for these sizes
+    # (0: the library's default depth)
     "c1": RunConfig("c1_256x256x128_fp64", 256, 128, "fp64", steps=200, seed=1, k0=6.0,
-                    stratification="exponential", levels_per_batch=32, solve_columns=16),
+                    stratification="exponential", levels_per_batch=0, solve_columns=16),
     "c2": RunConfig("c2_512x512x256_mixed", 512, 256, "mixed", steps=100, seed=2, k0=8.0,
-                    stratification="exponential", levels_per_batch=13, solve_columns=16),
+                    stratification="exponential", levels_per_batch=256, solve_columns=16),
     "c4": RunConfig("c4_128x128x64_fp64", 128, 64, "fp64", steps=50, seed=4, k0=3.0),
 }
 
