@@ -36,16 +36,15 @@ for _p in (str(ROOT), str(PKG)):
 FALLBACK_HBM_GBS = 6800.0
 # DRAM bytes per level of a launch (dram__bytes_read.sum + dram__bytes_write.sum,
 # L2 not flushed) of each phase-A kernel, from the ncu capture summarised in
-# profiles/dram_per_launch_512x512x26_mixed.md (512^2 levels, 13 levels per
-# launch, mean of two launches).  The traffic of a launch grows with the
-# levels it covers, so the roofline entry scales it by the levels per launch
-# of the run.
+# profiles/dram_per_launch_512x512x64_mixed.md (512^2 levels, one batch of 64
+# levels whose scratch planes outgrow L2 as the 256-level batch's do).  The
+# roofline entry scales it by the levels per launch of the run.
 MEASURED_TRAFFIC_PER_LEVEL = {
-    ("col_inv", 512, "mixed"): 66.63e6 / 13,
-    ("row_main", 512, "mixed"): 12.48e6 / 13,
-    ("col_update", 512, "mixed"): 121.15e6 / 13,
-    ("row_qw", 512, "mixed"): 8.810e6 / 13,
-    ("col_qw", 512, "mixed"): 9.815e6 / 13,
+    ("col_inv", 512, "mixed"): 6.073e6,
+    ("row_main", 512, "mixed"): 8.501e6,
+    ("col_update", 512, "mixed"): 14.065e6,
+    ("row_qw", 512, "mixed"): 4.356e6,
+    ("col_qw", 512, "mixed"): 2.701e6,
 }
 
 
