@@ -179,7 +179,8 @@ __device__ __forceinline__ void load_tw_passes(cplx<T>* tw_s, const cplx<T>* __r
   }
 }
 
-template <typename T, int N, int R, int NS, bool FWD, int BATCH, int NT, int LD, int LAY = 0>
+// reads in layout LAY, writes in layout LAYW (lay_idx)
+template <typename T, int N, int R, int NS, bool FWD, int BATCH, int NT, int LD, int LAY = 0, int LAYW = LAY>
 __device__ __forceinline__ void ip_pass(cplx<T>* __restrict__ buf, const cplx<T>* __restrict__ tw) {
   constexpr int NB = N / R;
   constexpr int TASKS = BATCH * NB;
@@ -216,18 +217,22 @@ __device__ __forceinline__ void ip_pass(cplx<T>* __restrict__ buf, const cplx<T>
       cplx<T>* d = buf + b * LD;
       const int base = (j - k) * R + k;
 #pragma unroll
-      for (int r = 0; r < R; ++r) d[lay_idx<LAY>(base + r * NS)] = v[p][r];
+      for (int r = 0; r < R; ++r) d[lay_idx<LAYW>(base + r * NS)] = v[p][r];
     }
   }
   __syncthreads();
 }
 
-template <typename T, int N, bool FWD, int BATCH, int NT, int LD, int NS, int LAY = 0>
+// MID: the second-to-last pass writes, and the last pass reads, layout 1
+// (the other hand-offs stay in LAY)
+template <typename T, int N, bool FWD, int BATCH, int NT, int LD, int NS, int LAY = 0, int MID = 0>
 __device__ __forceinline__ void ip_passes(cplx<T>* buf, const cplx<T>* tw) {
   if constexpr (NS < N) {
     constexpr int R = PassRadix<N / NS>::value;
-    ip_pass<T, N, R, NS, FWD, BATCH, NT, LD, LAY>(buf, tw);
-    ip_passes<T, N, FWD, BATCH, NT, LD, NS * R, LAY>(buf, tw);
+    constexpr bool last = NS * R == N;
+    constexpr bool pen = !last && NS * R * PassRadix<(last ? 1 : N / (NS * R))>::value == N;
+    ip_pass<T, N, R, NS, FWD, BATCH, NT, LD, (MID && last) ? 1 : LAY, (MID && pen) ? 1 : LAY>(buf, tw);
+    ip_passes<T, N, FWD, BATCH, NT, LD, NS * R, LAY, MID>(buf, tw);
   }
 }
 

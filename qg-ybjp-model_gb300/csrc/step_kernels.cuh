@@ -56,6 +56,8 @@ constexpr int kRowMainMinB = 2;    // k_row_main CTAs per SM when fused
 constexpr bool kRowPrefetch = true; // fused row kernels: persistent, next item's rows bulk-copied ahead
 constexpr bool kRowSwizzle = true;  // k_row_qw (N = 512): conflict-free XOR placement (lay_idx<1>)
 constexpr bool kRowMainSwizzle = false;  // k_row_main: the same (its index arithmetic spills at 128 registers)
+constexpr bool kRowMainMidSwz = false;   // k_row_main forward transforms: XOR placement between the last two passes (measured slower: spills)
+constexpr bool kRowMainMidSwzInv = false;  // the same for its inverse transforms (spills: the last pass feeds the products)
 constexpr bool kUpdTablesSmem = true;   // k_col_update (FP32 lean): IF tables staged in shared memory
 constexpr bool kUpdLean = true;    // k_col_update (FP32): smaller shared footprint ...
 constexpr bool kUpdStage16 = true; // k_col_update (FP32): state staged by 16-byte copies
@@ -110,6 +112,8 @@ template <typename T, int N> struct Tiles {
   static constexpr bool QPRE = kRowPrefetch && QFUSE;
   // element placement of the fused row kernels' transforms (lay_idx)
   static constexpr int RLAY = kRowMainSwizzle && RFUSE && N == 512 ? 1 : 0;
+  static constexpr int RMID = !kRowMainSwizzle && kRowMainMidSwz && RFUSE && N == 512 ? 1 : 0;
+  static constexpr int RMIDI = !kRowMainSwizzle && kRowMainMidSwzInv && RFUSE && N == 512 ? 1 : 0;
   static constexpr int QLAY = kRowSwizzle && QFUSE && N == 512 ? 1 : 0;
   static constexpr int CIMINB = imin(CB == 8 ? kColInvMinB : 2, smem_ctas((N + 3 * FSC) * CB));
   static constexpr int CQMINB = imin(CB == 8 ? kColQwMinB : 2, smem_ctas((N + 2 * FSC) * CB));
@@ -245,6 +249,9 @@ __device__ __forceinline__ void row_main_item(const Geom& g, const StepParams& s
                                               const cplx<T>* __restrict__ tw, cplx<T>* __restrict__ bA, int zb,
                                               int y0, Src src, After after_pass0) {
   constexpr int RT = Tiles<T, N>::RTM, LD = Tiles<T, N>::LD, NT = kRowThreads, LAY = Tiles<T, N>::RLAY;
+  // MID / MIDI: forward / inverse hand-off before the last pass in layout 1;
+  // LL: layout the inverse's last pass reads
+  constexpr int MID = Tiles<T, N>::RMID, MIDI = Tiles<T, N>::RMIDI, LL = MIDI ? 1 : LAY;
   const int tid = threadIdx.x;
   const int K = g.K;
   constexpr int R0 = radix_of(N), NB0 = N / R0;
@@ -262,7 +269,7 @@ __device__ __forceinline__ void row_main_item(const Geom& g, const StepParams& s
     after_pass0();
     if constexpr (Tiles<T, N>::RFUSE) {
       constexpr int NS = LastNS<N>::value, R = N / NS;     // == R0, NS == NB0
-      ip_passes_but_last<T, N, false, 3 * RT, NT, LD, R0, LAY>(bA, tw);
+      ip_passes_but_last<T, N, false, 3 * RT, NT, LD, R0, LAY, MIDI>(bA, tw);
       // last inverse pass into registers: task (row, j) holds the physical
       // values at x = j + r*NS of the three packed pairs
       const int j = tid % NS, rr = tid / NS;
@@ -271,7 +278,7 @@ __device__ __forceinline__ void row_main_item(const Geom& g, const StepParams& s
 #pragma unroll
       for (int f = 0; f < 3; ++f) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[f][r] = bA[(f * RT + rr) * LD + lay_idx<LAY>(j + r * NS)];
+        for (int r = 0; r < R; ++r) v[f][r] = bA[(f * RT + rr) * LD + lay_idx<LL>(j + r * NS)];
 #pragma unroll
         for (int r = 1; r < R; ++r) {
           cplx<T> w = tw[off + (r - 1) * NS + j];
@@ -299,7 +306,7 @@ __device__ __forceinline__ void row_main_item(const Geom& g, const StepParams& s
         for (int r = 0; r < R; ++r) bA[(f * RT + rr) * LD + lay_idx<LAY>(j * R + r)] = w[r];
       }
       __syncthreads();
-      ip_passes<T, N, true, 4 * RT, NT, LD, R0, LAY>(bA, tw);
+      ip_passes<T, N, true, 4 * RT, NT, LD, R0, LAY, MID>(bA, tw);
     } else {
       ip_passes<T, N, false, 3 * RT, NT, LD, R0, LAY>(bA, tw);
     }
@@ -1123,20 +1130,26 @@ k_solve_st(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
   };
   const int nseg = (n3 + S - 1) / S;
   double x = 0.0;
-  for (int j = 0; j < nseg; ++j) {
-    T r[S];
-    double f[S];
+  auto load_seg = [&](int j, T (&r)[S], double (&f)[S]) {
 #pragma unroll
     for (int k = 0; k < S; ++k) {
       const int i = j * S + k;
       r[k] = i < n3 ? rhs[2 * (i * P + m)] : (T)0;
       f[k] = (i > 0 && i < n3) ? F[i - 1].x : 0.0;
     }
+  };
+  auto run_seg = [&](int j, const T (&r)[S], const double (&f)[S]) {
 #pragma unroll
     for (int k = 0; k < S; ++k) {
       const int i = j * S + k;
       if (i < n3) { x = fwd(x, f[k], r[k]); vb[(long long)i * P] = x; }
     }
+  };
+  for (int j = 0; j < nseg; ++j) {
+    T r[S];
+    double f[S];
+    load_seg(j, r, f);
+    run_seg(j, r, f);
   }
   double xn = 0.0;
   for (int j = nseg - 1; j >= 0; --j) {
