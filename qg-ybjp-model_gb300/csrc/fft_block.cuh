@@ -154,6 +154,40 @@ template <int LAY> __host__ __device__ __forceinline__ constexpr int lay_idx(int
   }
 }
 
+// Compile-time proof of the claims for N = 512: lay_idx<1> permutes
+// [0, 512), and each group of 16 consecutive tasks j (one half-warp's 8-byte
+// accesses, r fixed) of the three access patterns hits 16 distinct bank pairs
+// (slot = index mod 16).
+namespace lay_check {
+constexpr bool permutes512() {
+  bool seen[512] = {};
+  for (int i = 0; i < 512; ++i) {
+    const int p = lay_idx<1>(i);
+    if (p < 0 || p >= 512 || seen[p]) return false;
+    seen[p] = true;
+  }
+  return true;
+}
+constexpr bool conflict_free512() {
+  for (int pat = 0; pat < 3; ++pat)
+    for (int r = 0; r < 8; ++r)
+      for (int j0 = 0; j0 < 64; j0 += 16) {
+        bool hit[16] = {};
+        for (int j = j0; j < j0 + 16; ++j) {
+          const int i = pat == 0 ? 8 * j + r                            // first pass writes
+                      : pat == 1 ? 64 * (j >> 3) + (j & 7) + 8 * r      // middle pass writes
+                                 : j + 64 * r;                          // every read, last writes
+          const int slot = lay_idx<1>(i) & 15;
+          if (hit[slot]) return false;
+          hit[slot] = true;
+        }
+      }
+  return true;
+}
+static_assert(permutes512(), "lay_idx<1> is not a permutation of [0, 512)");
+static_assert(conflict_free512(), "lay_idx<1> leaves a bank conflict");
+}  // namespace lay_check
+
 // Twiddles laid out per pass: the pass with stride NS and radix R reads
 // W_N^{k r N/(NS R)} at tw[off(NS) + (r-1)*NS + k], so the threads of a warp
 // (consecutive k) read consecutive words.  Fewer than N entries in total.
