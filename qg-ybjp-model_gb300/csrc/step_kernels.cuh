@@ -1093,15 +1093,17 @@ k_solve(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
 // TC columns per CTA (16, 32 or 64: the block shape the autotuner picks),
 // 6*TC threads, the register budget of 4 CTAs of 192 threads.
 constexpr bool kSolveStore = true;
+constexpr int kSegSt = 8;          // k_solve_st: levels per register segment of the sweeps
+constexpr int kSolveStBlocks = 128;  // k_solve_st: register target of 128/TC CTAs of 6*TC threads per SM
 template <typename T, int TC>
-__global__ void __launch_bounds__(6 * TC, 128 / TC)
+__global__ void __launch_bounds__(6 * TC, kSolveStBlocks / TC)
 k_solve_st(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
            const double4* __restrict__ fac_psi, const double4* __restrict__ fac_A, const double* __restrict__ du,
            const cplx<T>* __restrict__ qs, const cplx<T>* __restrict__ BR, const cplx<T>* __restrict__ BI,
            cplx<T>* __restrict__ psi, cplx<T>* __restrict__ AR, cplx<T>* __restrict__ AI,
            int do_psi, int do_A, double* __restrict__ vbuf) {
   constexpr bool EXACT = sizeof(T) == 8;
-  constexpr int S = kSeg, NTH = 6 * TC;
+  constexpr int S = kSegSt, NTH = 6 * TC;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n3 = g.n3;
   double* du_s = reinterpret_cast<double*>(smem_raw);
