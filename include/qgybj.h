@@ -136,6 +136,12 @@ int qg_step(qg_handle* h, int euler_first);
 int qg_steps_async(qg_handle* h, int nsteps, int euler_first);
 int qg_synchronize(qg_handle* h);
 
+/* Failure-path check of the bounded device-side waits: runs on h's stream a
+ * kernel whose wait (the mbarrier wait the row kernels use for their bulk
+ * copies) nothing completes; it gives up after ~0.5 s of SM clocks and the
+ * call returns QG_ERR_TIMEOUT, with h still usable. */
+int qg_selftest_wait(qg_handle* h);
+
 /* The handle's cudaStream_t (as void*) for event timing by the host. */
 int qg_get_stream(qg_handle* h, void** stream);
 

@@ -55,4 +55,20 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
 
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
 
+// Sets the flag a host reads after the stream drains (mapped page-locked
+// word: a plain store, no system-scope atomic needed).
+__device__ __forceinline__ void raise_wait_flag(int* wflag) { *reinterpret_cast<volatile int*>(wflag) = 1; }
+
+// The failure path of the bounded waits, on demand: one CTA waits on an
+// mbarrier phase that nothing completes, gives up after kMbarWaitCycles and
+// raises the flag, as a row kernel does when a bulk copy never lands.
+static __global__ void k_wait_expire(int* wflag) {
+  __shared__ __align__(8) unsigned long long bar;
+  const unsigned b = smem_u32(&bar);
+  if (threadIdx.x == 0) mbar_init(b, 1);
+  __syncthreads();
+  const bool ok = mbar_wait(b, 0);
+  if (__syncthreads_or(!ok) && threadIdx.x == 0) raise_wait_flag(wflag);
+}
+
 }  // namespace qg

@@ -322,6 +322,10 @@ int qg_synchronize(qg_handle* h) {
   QG_ENTRY(h);
   return fwd(h, h->eng->synchronize());
 }
+int qg_selftest_wait(qg_handle* h) {
+  QG_ENTRY(h);
+  return fwd(h, h->eng->selftest_wait());
+}
 int qg_get_stream(qg_handle* h, void** stream) {
   QG_ENTRY(h);
   if (!stream) return fail(h, QG_ERR_ARG, "null stream pointer");

@@ -35,6 +35,8 @@ struct EngineBase {
   virtual int step(int euler) = 0;
   virtual int steps_async(int nsteps, int euler) = 0;
   virtual int synchronize() = 0;
+  // runs k_wait_expire on the stream; QG_ERR_TIMEOUT expected
+  virtual int selftest_wait() = 0;
   virtual void* stream() = 0;
   virtual int diagnostics(qg_energy* out) = 0;
   virtual int profile_step(int euler, double* ms, int* launches, int nclasses) = 0;

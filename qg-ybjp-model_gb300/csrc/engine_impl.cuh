@@ -179,6 +179,12 @@ class Engine : public EngineBase {
     return check_waits();
   }
 
+  int selftest_wait() override {
+    k_wait_expire<<<1, 32, 0, st>>>(wflag);
+    QG_LAUNCHED();
+    return synchronize();
+  }
+
   // QG_ERR_TIMEOUT when a kernel's bounded wait expired since the last check
   // (call after the stream has drained)
   int check_waits() {

@@ -396,7 +396,7 @@ k_row_main(Geom g, StepParams sp, cplx<T>* __restrict__ S, const cplx<T>* __rest
       // also orders the previous item's last reads of bA before this one's writes
       const bool ok = mbar_wait(bar, ph);
       if (__syncthreads_or(!ok)) {
-        if (threadIdx.x == 0) { atomicOr(wflag, 1); (void)mbar_wait(bar, ph); }
+        if (threadIdx.x == 0) { raise_wait_flag(wflag); (void)mbar_wait(bar, ph); }
         return;
       }
       const int nxt = it + (int)gridDim.x;
@@ -811,7 +811,7 @@ k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg, int n
     for (int it = blockIdx.x; it < nitems; it += gridDim.x, ph ^= 1u) {
       const bool ok = mbar_wait(bar, ph);
       if (__syncthreads_or(!ok)) {
-        if (threadIdx.x == 0) { atomicOr(wflag, 1); (void)mbar_wait(bar, ph); }
+        if (threadIdx.x == 0) { raise_wait_flag(wflag); (void)mbar_wait(bar, ph); }
         return;
       }
       const int nxt = it + (int)gridDim.x;

@@ -28,7 +28,7 @@ EXPORTS = (
     "qg_ensemble_get_stream", "qg_ensemble_destroy", "qg_ensemble_last_error", "qg_autotune",
     "qg_adjoint_run", "qg_adjoint_step", "qg_dump_psi", "qg_dump_la",
     "qg_omega_eqn_rhs", "qg_omega_equation", "qg_omega", "qg_ensemble_set_lanes",
-    "qg_selftest_conversions",
+    "qg_selftest_conversions", "qg_selftest_wait",
 )
 KERNEL_CLASSES = ("dissipation", "col_inv", "row_main", "col_update", "row_qw", "col_qw", "solve")
 
@@ -95,6 +95,7 @@ def lib() -> C.CDLL:
         "qg_profile_step": (ip, [vp, ip, dp, C.POINTER(C.c_int), ip]),
         "qg_fft_c2r_noalloc": (ip, [vp, vp, ip, ip, vp]),
         "qg_selftest_conversions": (ip, [ip, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
+        "qg_selftest_wait": (ip, [vp]),
         "qg_ensemble_create": (ip, [C.POINTER(QgConfig), ip, C.POINTER(vp)]),
         "qg_ensemble_member": (ip, [vp, ip, C.POINTER(vp)]),
         "qg_ensemble_step": (ip, [vp, ip, ip]),

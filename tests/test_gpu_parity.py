@@ -377,3 +377,18 @@ def test_integer_conversions_match_hardware():
     a, b = C.c_longlong(-1), C.c_longlong(-1)
     assert lib().qg_selftest_conversions(0, C.byref(a), C.byref(b)) == QG_OK
     assert (a.value, b.value) == (0, 0)
+
+
+def test_bounded_wait_expiry_reports_timeout():
+    """A device-side wait that nothing completes gives up after its bound
+    (~0.5 s of SM clocks) and the call returns QG_ERR_TIMEOUT; the handle then
+    still steps and matches the oracle.  No GPU fault is involved."""
+    from qgybj._lib import QG_ERR_TIMEOUT, lib
+    rc = scaled(CONFIGS["c0"], 32, 8)
+    model, st, sim = pair(rc, "mixed")
+    assert lib().qg_selftest_wait(sim.h) == QG_ERR_TIMEOUT
+    sim.steps_async(3, True)
+    sim.synchronize()
+    st = model.run(st, 3, first=True)
+    compare(sim, st, TOL["mixed"])
+    sim.close()
