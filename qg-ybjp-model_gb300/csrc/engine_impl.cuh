@@ -138,6 +138,17 @@ class Engine : public EngineBase {
       vbuf = nullptr;
       (void)cudaGetLastError();
     }
+    // mixed path: per-column copies of the solve factors (coalesced reads);
+    // without them the solves read the per-kh^2 tables
+    if (kSolvePerColumn && sizeof(T) == 4 && vbuf) {
+      if (cudaMalloc(&pcfac, (size_t)6 * g.n3 * g.plane * sizeof(double)) != cudaSuccess) {
+        pcfac = nullptr;
+        (void)cudaGetLastError();
+      } else {
+        k_expand_fac<<<grid_for((long long)g.n3 * g.plane), 256, 0, st>>>(g, tab_idx, fac_psi, fac_A, pcfac);
+        QG_LAUNCHED();
+      }
+    }
     QG_CK(cudaStreamSynchronize(st));
     return QG_OK;
   }
@@ -532,6 +543,7 @@ class Engine : public EngineBase {
   C* tw = nullptr;
   int* tab_idx = nullptr;
   double4 *fac_psi = nullptr, *fac_A = nullptr;
+  double* pcfac = nullptr;   // per-column solve factors of the mixed path (k_expand_fac), or null
   double* vbuf = nullptr;    // forward values of the column solves (k_solve_st)
   int solve_tc = 32;         // columns per CTA of k_solve_st
   double *du = nullptr, *cu = nullptr, *cl = nullptr, *r2 = nullptr;
@@ -560,7 +572,7 @@ class Engine : public EngineBase {
     if (st) cudaStreamSynchronize(st);
     for (auto& x : gexec) if (x) { cudaGraphExecDestroy(x); x = nullptr; }
     for (auto& p : F) if (p) { cudaFree(p); p = nullptr; }
-    void* ps[] = {e1, e2, e1w, e2w, tw, tab_idx, fac_psi, fac_A, vbuf, du, cu, cl, r2, diag_part, diag_out, S, stage,
+    void* ps[] = {e1, e2, e1w, e2w, tw, tab_idx, fac_psi, fac_A, pcfac, vbuf, du, cu, cl, r2, diag_part, diag_out, S, stage,
                   W, dstage, psi64, om_t1, om_du, om_dl, om_a, om_scr, sig[0], sig[1]};
     for (void* p : ps) if (p) cudaFree(p);
     for (auto& p : D) if (p) cudaFree(p);
@@ -769,12 +781,18 @@ class Engine : public EngineBase {
   int solve_generic(const C* qs, const C* br, const C* bi, C* psi, C* ar, C* ai, int do_psi, int do_A) {
     if (!do_psi && !do_A) return QG_OK;
     if (kSolveStore && vbuf) {
-#define QG_SOLVE_ST(TCV)                                                                                   \
-  k_solve_st<T, TCV><<<(unsigned)((g.plane + TCV - 1) / TCV), 6 * TCV, (size_t)g.n3 * 8, st>>>(           \
-      g, cfg.dz, cfg.Bu, tab_idx, fac_psi, fac_A, du, qs, br, bi, psi, ar, ai, do_psi, do_A, vbuf)
-      if (solve_tc == 16) QG_SOLVE_ST(16);
-      else if (solve_tc == 64) QG_SOLVE_ST(64);
-      else QG_SOLVE_ST(32);
+#define QG_SOLVE_ST(TCV, PCV)                                                                              \
+  k_solve_st<T, TCV, PCV><<<(unsigned)((g.plane + TCV - 1) / TCV), 6 * TCV, (size_t)g.n3 * 8, st>>>(      \
+      g, cfg.dz, cfg.Bu, tab_idx, fac_psi, fac_A, du, qs, br, bi, psi, ar, ai, do_psi, do_A, vbuf, pcfac)
+      if (pcfac) {
+        if (solve_tc == 16) QG_SOLVE_ST(16, true);
+        else if (solve_tc == 64) QG_SOLVE_ST(64, true);
+        else QG_SOLVE_ST(32, true);
+      } else {
+        if (solve_tc == 16) QG_SOLVE_ST(16, false);
+        else if (solve_tc == 64) QG_SOLVE_ST(64, false);
+        else QG_SOLVE_ST(32, false);
+      }
 #undef QG_SOLVE_ST
       QG_LAUNCHED();
       return QG_OK;

@@ -1093,16 +1093,49 @@ k_solve(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
 // TC columns per CTA (16, 32 or 64: the block shape the autotuner picks),
 // 6*TC threads, the register budget of 4 CTAs of 192 threads.
 constexpr bool kSolveStore = true;
+constexpr bool kSolvePerColumn = true;  // mixed solves read per-column factor copies (k_expand_fac)
 constexpr int kSegSt = 8;          // k_solve_st: levels per register segment of the sweeps
 constexpr int kSolveStBlocks = 128;  // k_solve_st: register target of 128/TC CTAs of 6*TC threads per SM
-template <typename T, int TC>
+// Per-column copies of the mixed path's elimination factors, expanded from
+// the per-kh^2 tables so that the consecutive columns of a warp read
+// consecutive words (the per-kh^2 rows of neighbouring columns are scattered:
+// one 32-byte sector per column and level).  pc[(o*3 + q)*L + i*P + m],
+// L = n3*P, operator o (0 psi, 1 A), q = 0: f_{i-1} (0 at i = 0),
+// 1: s/d'_i, 2: u_i/d'_i; zeros where the column holds no retained mode.
+static __global__ void k_expand_fac(Geom g, const int* __restrict__ tab_idx, const double4* __restrict__ fac_psi,
+                                    const double4* __restrict__ fac_A, double* __restrict__ pc) {
+  const long long P = g.plane, L = (long long)g.n3 * P;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < L; e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e / P);
+    const long long m = e - (long long)i * P;
+    const int idx = tab_idx[m];
+#pragma unroll
+    for (int o = 0; o < 2; ++o) {
+      double f = 0.0, y = 0.0, z = 0.0;
+      if (idx >= 0) {
+        const double4* Fc = (o == 0 ? fac_psi : fac_A) + (long long)idx * g.n3;
+        f = i > 0 ? Fc[i - 1].x : 0.0;
+        y = Fc[i].y;
+        z = Fc[i].z;
+      }
+      pc[(o * 3 + 0) * L + e] = f;
+      pc[(o * 3 + 1) * L + e] = y;
+      pc[(o * 3 + 2) * L + e] = z;
+    }
+  }
+}
+
+// PC (mixed path): factors from the per-column copies pc (k_expand_fac)
+// instead of the per-kh^2 tables; the same values, so the same results.
+template <typename T, int TC, bool PC>
 __global__ void __launch_bounds__(6 * TC, kSolveStBlocks / TC)
 k_solve_st(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
            const double4* __restrict__ fac_psi, const double4* __restrict__ fac_A, const double* __restrict__ du,
            const cplx<T>* __restrict__ qs, const cplx<T>* __restrict__ BR, const cplx<T>* __restrict__ BI,
            cplx<T>* __restrict__ psi, cplx<T>* __restrict__ AR, cplx<T>* __restrict__ AI,
-           int do_psi, int do_A, double* __restrict__ vbuf) {
+           int do_psi, int do_A, double* __restrict__ vbuf, const double* __restrict__ pc) {
   constexpr bool EXACT = sizeof(T) == 8;
+  constexpr bool USEPC = PC && !EXACT;
   constexpr int S = kSegSt, NTH = 6 * TC;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n3 = g.n3;
@@ -1127,6 +1160,9 @@ k_solve_st(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
   const double4* F = (rhs_id == 0 ? fac_psi : fac_A) + (long long)idx * n3;
   const double s = rhs_id == 0 ? __dmul_rn(dz, dz) : __dmul_rn(__dmul_rn(dz, dz), Bu);
   double* vb = vbuf + (long long)chain * n3 * P + m;
+  const long long L = (long long)n3 * P;
+  // (USEPC) f_{i-1}, s/d'_i, u_i/d'_i of this column at + q*L + i*P
+  const double* pcf = USEPC ? pc + (rhs_id == 0 ? 0 : 3) * L + m : nullptr;
   auto fwd = [&](double x, double f, T r) -> double {
     return EXACT ? __dsub_rn(__dmul_rn(s, to64<T>(r)), __dmul_rn(f, x)) : fma(-f, x, to64<T>(r));
   };
@@ -1137,7 +1173,8 @@ k_solve_st(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
     for (int k = 0; k < S; ++k) {
       const int i = j * S + k;
       r[k] = i < n3 ? rhs[2 * (i * P + m)] : (T)0;
-      f[k] = (i > 0 && i < n3) ? F[i - 1].x : 0.0;
+      if constexpr (USEPC) f[k] = i < n3 ? pcf[(long long)i * P] : 0.0;
+      else f[k] = (i > 0 && i < n3) ? F[i - 1].x : 0.0;
     }
   };
   auto run_seg = [&](int j, const T (&r)[S], const double (&f)[S]) {
@@ -1155,21 +1192,27 @@ k_solve_st(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
   }
   double xn = 0.0;
   for (int j = nseg - 1; j >= 0; --j) {
-    double v[S];
-    double4 fl[S];
+    double v[S], yk[S], zk[S];
 #pragma unroll
     for (int k = 0; k < S; ++k) {
       const int i = j * S + k;
       v[k] = i < n3 ? vb[(long long)i * P] : 0.0;
-      fl[k] = i < n3 ? F[i] : make_double4(0, 1, 0, 0);
+      if constexpr (USEPC) {
+        yk[k] = i < n3 ? pcf[L + (long long)i * P] : 1.0;
+        zk[k] = i < n3 ? pcf[2 * L + (long long)i * P] : 0.0;
+      } else {
+        const double4 fl = i < n3 ? F[i] : make_double4(0, 1, 0, 0);
+        yk[k] = fl.y;
+        zk[k] = fl.z;
+      }
     }
 #pragma unroll
     for (int k = S - 1; k >= 0; --k) {
       const int i = j * S + k;
       if (i < n3) {
-        if (i == n3 - 1) xn = EXACT ? __ddiv_rn(v[k], fl[k].y) : fl[k].y * v[k];
-        else if (EXACT) xn = __ddiv_rn(__dsub_rn(v[k], __dmul_rn(du_s[i], xn)), fl[k].y);
-        else xn = fma(-fl[k].z, xn, fl[k].y * v[k]);
+        if (i == n3 - 1) xn = EXACT ? __ddiv_rn(v[k], yk[k]) : yk[k] * v[k];
+        else if (EXACT) xn = __ddiv_rn(__dsub_rn(v[k], __dmul_rn(du_s[i], xn)), yk[k]);
+        else xn = fma(-zk[k], xn, yk[k] * v[k]);
         out[2 * (i * P + m)] = from64<T>(xn);
       }
     }
