@@ -16,6 +16,7 @@
 #include <vector>
 #include "dense_kernels.cuh"
 #include "engine.h"
+#include "noalloc_check.h"
 
 namespace {
 
@@ -99,11 +100,40 @@ int setup_device(int dev, DeviceSetup** out) {
   return QG_OK;
 }
 
-bool is_device_pointer(const void* p) {
+// QG_OK when p is memory a kernel on device `dev` can read or write at
+// `align`-byte alignment; otherwise QG_ERR_ARG with the reason.
+int check_device_pointer(const void* p, int dev, uintptr_t align, const char* name) {
   cudaPointerAttributes a;
-  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  int type = 0, owner = -1;
+  if (cudaPointerGetAttributes(&a, p) == cudaSuccess) {
+    type = (int)a.type;
+    owner = a.device;
+  } else {
+    cudaGetLastError();   // the query's own error (an unregistered host pointer)
+  }
+  switch (qgna::check_pointer(type, owner, dev, p, align)) {
+    case qgna::kPointerOk: return QG_OK;
+    case qgna::kPointerNotDevice:
+      return fail(QG_ERR_ARG, std::string("qg_fft_c2r_noalloc: ") + name + " must be device memory");
+    case qgna::kPointerOtherDevice:
+      return fail(QG_ERR_ARG, std::string("qg_fft_c2r_noalloc: ") + name +
+                                  " belongs to another device than the current one");
+    default:
+      return fail(QG_ERR_ARG, std::string("qg_fft_c2r_noalloc: ") + name + " must be " +
+                                  std::to_string((unsigned long long)align) + "-byte aligned");
+  }
 }
+
+// the launch just made: its configuration error, if any (no earlier error
+// was pending when the call began, so whatever is pending now is this call's)
+#define NA_LAUNCH_CK()                                                                          \
+  do {                                                                                          \
+    cudaError_t e_ = cudaPeekAtLastError();                                                     \
+    if (e_ != cudaSuccess) {                                                                    \
+      cudaGetLastError();                                                                       \
+      return fail(QG_ERR_CUDA, std::string("qg_fft_c2r_noalloc launch: ") + cudaGetErrorString(e_)); \
+    }                                                                                           \
+  } while (0)
 
 template <int N>
 int launch_chunks(const double2* in, double* out, int nz, cudaStream_t st, const DeviceSetup& s) {
@@ -118,10 +148,10 @@ int launch_chunks(const double2* in, double* out, int nz, cudaStream_t st, const
     const int zc = nz - z0 < chunk ? nz - z0 : chunk;
     qg::k_dcol_inv<double, N><<<dim3(ip / ct, zc), qg::kThreads, sm_col, st>>>(
         ip, in + (size_t)z0 * N * (N / 2 + 1), s.scratch, tw);
-    NA_CK(cudaGetLastError());
+    NA_LAUNCH_CK();
     qg::k_drow_c2r_pad<double, N><<<dim3(N / 2, zc), qg::kThreads, sm_row, st>>>(
         ip, s.scratch, out + (size_t)z0 * N * (N + 2), tw);
-    NA_CK(cudaGetLastError());
+    NA_LAUNCH_CK();
   }
   return QG_OK;
 }
@@ -134,13 +164,24 @@ extern "C" int qg_fft_c2r_noalloc(const double* kvar, double* rvar, int n, int n
   if (n < 16 || n > 512 || (n & (n - 1)))
     return fail(QG_ERR_UNSUPPORTED, "qg_fft_c2r_noalloc: n must be a power of two in [16, 512] (one level's "
                                     "(kx,y) plane must fit the 8 MiB static scratch)");
-  if (!is_device_pointer(kvar) || !is_device_pointer(rvar))
-    return fail(QG_ERR_ARG, "qg_fft_c2r_noalloc: kvar and rvar must be device memory");
   int dev = 0;
   NA_CK(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) return fail(QG_ERR_UNSUPPORTED, "qg_fft_c2r_noalloc: device ordinal too large");
+  // an error left pending by the caller's earlier work stays the caller's:
+  // refuse without consuming it
+  {
+    const cudaError_t pend = cudaPeekAtLastError();
+    if (pend != cudaSuccess)
+      return fail(QG_ERR_CUDA, std::string("qg_fft_c2r_noalloc: a CUDA error from earlier work is pending "
+                                           "(left for its owner to read): ") + cudaGetErrorString(pend));
+  }
+  // kvar is read as 16-byte complex values, rvar written as doubles
+  int rc = check_device_pointer(kvar, dev, 16, "kvar");
+  if (rc) return rc;
+  rc = check_device_pointer(rvar, dev, 8, "rvar");
+  if (rc) return rc;
   DeviceSetup* s = nullptr;
-  int rc = setup_device(dev, &s);
+  rc = setup_device(dev, &s);
   if (rc) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const double2* in = reinterpret_cast<const double2*>(kvar);

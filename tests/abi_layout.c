@@ -3,13 +3,21 @@
 #include <stddef.h>
 #include <stdio.h>
 #include "qgybj.h"
-#define OFF(f) printf("%s %zu\n", #f, offsetof(qg_config, f))
+#define OFF(s, f) printf("%s.%s %zu\n", #s, #f, offsetof(s, f))
 int main(void) {
-  printf("sizeof %zu\n", sizeof(qg_config));
-  OFF(n1); OFF(n3); OFF(precision); OFF(device); OFF(ybj_plus); OFF(inviscid); OFF(dz); OFF(Bu); OFF(delt);
-  OFF(gamma); OFF(nuh1); OFF(nuh2w); OFF(ilap1); OFF(ilap2w); OFF(nuz); OFF(a_ell_ut); OFF(rho_ut); OFF(rho_st);
-  OFF(r_2ut); OFF(levels_per_batch); OFF(use_graphs); OFF(solve_columns);
-  printf("tuning %zu\n", sizeof(qg_tuning));
-  printf("energy %zu\n", sizeof(qg_energy));
+  printf("sizeof.qg_config %zu\n", sizeof(qg_config));
+  OFF(qg_config, n1); OFF(qg_config, n3); OFF(qg_config, precision); OFF(qg_config, device);
+  OFF(qg_config, ybj_plus); OFF(qg_config, inviscid); OFF(qg_config, dz); OFF(qg_config, Bu);
+  OFF(qg_config, delt); OFF(qg_config, gamma); OFF(qg_config, nuh1); OFF(qg_config, nuh2w);
+  OFF(qg_config, ilap1); OFF(qg_config, ilap2w); OFF(qg_config, nuz); OFF(qg_config, a_ell_ut);
+  OFF(qg_config, rho_ut); OFF(qg_config, rho_st); OFF(qg_config, r_2ut); OFF(qg_config, levels_per_batch);
+  OFF(qg_config, use_graphs); OFF(qg_config, solve_columns);
+  printf("sizeof.qg_tuning %zu\n", sizeof(qg_tuning));
+  OFF(qg_tuning, levels_per_batch); OFF(qg_tuning, ms_per_step); OFF(qg_tuning, ncandidates);
+  OFF(qg_tuning, candidates); OFF(qg_tuning, candidate_ms); OFF(qg_tuning, solve_columns);
+  OFF(qg_tuning, nsolve); OFF(qg_tuning, solve_candidates); OFF(qg_tuning, solve_candidate_ms);
+  printf("sizeof.qg_energy %zu\n", sizeof(qg_energy));
+  OFF(qg_energy, wke); OFF(qg_energy, wpe); OFF(qg_energy, wce); OFF(qg_energy, ke); OFF(qg_energy, pe);
+  OFF(qg_energy, zeta2); OFF(qg_energy, omegah2);
   return 0;
 }

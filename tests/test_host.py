@@ -42,11 +42,49 @@ def test_struct_layout_matches_header(tmp_path):
     subprocess.run([cc, "-I", str(ROOT / "include"), str(ROOT / "tests" / "abi_layout.c"), "-o", str(exe)], check=True)
     out = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True,
                                                         check=True).stdout.splitlines())
-    assert int(out.pop("sizeof")) == C.sizeof(_lib.QgConfig)
-    assert int(out.pop("energy")) == C.sizeof(_lib.QgEnergy)
-    assert int(out.pop("tuning")) == C.sizeof(_lib.QgTuning)
-    for f, off in out.items():
-        assert getattr(_lib.QgConfig, f).offset == int(off), f
+    structs = {"qg_config": _lib.QgConfig, "qg_tuning": _lib.QgTuning, "qg_energy": _lib.QgEnergy}
+    for name, cls in structs.items():
+        assert int(out.pop(f"sizeof.{name}")) == C.sizeof(cls), name
+    seen = set()
+    for key, off in out.items():
+        name, f = key.split(".")
+        assert getattr(structs[name], f).offset == int(off), key
+        seen.add(name)
+    assert seen == set(structs)
+
+
+def test_noalloc_pointer_checks(tmp_path):
+    """The argument checks of qg_fft_c2r_noalloc (csrc/noalloc_check.h) on
+    every branch, host-only: device memory of the current GPU passes; host
+    memory, another GPU's memory and misaligned pointers are refused."""
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    src = tmp_path / "check.cc"
+    src.write_text(r'''
+#include <stdio.h>
+#include "noalloc_check.h"
+int main() {
+  alignas(16) static char buf[64];
+  const void* a16 = buf; const void* a8 = buf + 8;
+  printf("%d %d %d %d %d %d %d %d\n",
+         qgna::check_pointer(2, 0, 0, a16, 16),   /* device memory, current GPU */
+         qgna::check_pointer(3, 1, 0, a16, 16),   /* managed memory: any GPU */
+         qgna::check_pointer(0, -1, 0, a16, 16),  /* unregistered host memory */
+         qgna::check_pointer(1, 0, 0, a16, 16),   /* page-locked host memory */
+         qgna::check_pointer(2, 1, 0, a16, 16),   /* another GPU's memory */
+         qgna::check_pointer(2, 0, 0, a8, 16),    /* 8-byte aligned complex input */
+         qgna::check_pointer(2, 0, 0, a8, 8),     /* 8-byte aligned real output */
+         qgna::check_pointer(2, 0, 0, buf + 4, 8));
+  return 0;
+}
+''')
+    exe = tmp_path / "check"
+    subprocess.run([cxx, "-std=c++17", "-I", str(ROOT / "qg-ybjp-model_gb300" / "csrc"), str(src), "-o", str(exe)],
+                   check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    ok, not_dev, other, misaligned = 0, 1, 2, 3
+    assert got == [ok, ok, not_dev, not_dev, other, misaligned, ok, misaligned]
 
 
 def test_create_without_device_reports_status():

@@ -17,7 +17,8 @@ import pytest
 from qgybj import Simulation, lib
 from qgybj._lib import QG_ERR_ARG, QG_ERR_UNSUPPORTED
 from qgybj.config import CONFIGS, make_initial_condition, model_parameters, scaled
-from tests.helpers import random_masked, rel_l2
+from oracle import qgybj_oracle as orc
+from tests.helpers import oracle_params, random_masked, rel_l2
 
 pytestmark = pytest.mark.gpu
 
@@ -40,7 +41,9 @@ def test_noalloc_c2r_matches_handle_path_on_two_calls(n, nz):
     torch = pytest.importorskip("torch")
     rc = scaled(CONFIGS["c0"], n, 4)
     ic = make_initial_condition(rc)
-    sim = Simulation(model_parameters(rc, ic.delt), "fp64")
+    params = model_parameters(rc, ic.delt)
+    sim = Simulation(params, "fp64")
+    model = orc.Model(oracle_params(params))
     for seed in (11, 12):        # two calls in a row, different inputs
         spec = random_masked(n, nz, seed, masked=False)
         expect = sim.fft_c2r(spec)
@@ -48,6 +51,8 @@ def test_noalloc_c2r_matches_handle_path_on_two_calls(n, nz):
         assert np.isfinite(got).all()
         assert rel_l2(got[:, :, :n], expect[:, :, :n]) <= TOL
         assert np.abs(got[:, :, n:]).max() == 0
+        # and directly against the oracle's c2r (fft.f90:71-83, realit included)
+        assert rel_l2(got[:, :, :n], model.fft_c2r(spec)) <= TOL
     sim.close()
 
 
@@ -61,3 +66,12 @@ def test_noalloc_rejects_what_it_cannot_do():
     host = np.zeros((1, 64, 33), dtype=np.complex128)
     hr = np.zeros((1, 64, 66))
     assert lib().qg_fft_c2r_noalloc(host.ctypes.data, hr.ctypes.data, 64, 1, None) == QG_ERR_ARG
+    # complex input read in 16-byte pairs: an input offset by one double is refused, not launched
+    k64 = torch.zeros((1, 64, 33, 2), dtype=torch.float64, device="cuda")
+    r64 = torch.zeros((1, 64, 66), dtype=torch.float64, device="cuda")
+    assert lib().qg_fft_c2r_noalloc(C.c_void_p(k64.data_ptr() + 8), C.c_void_p(r64.data_ptr()), 64, 1, None) \
+        == QG_ERR_ARG
+    assert b"16-byte aligned" in lib().qg_last_error(None)
+    assert lib().qg_fft_c2r_noalloc(C.c_void_p(k64.data_ptr()), C.c_void_p(r64.data_ptr() + 4), 64, 1, None) \
+        == QG_ERR_ARG
+    torch.cuda.synchronize()
