@@ -155,28 +155,114 @@ def measured_peak_hbm() -> tuple[float, str]:
 # algorithmic bytes
 # ---------------------------------------------------------------------------
 def algorithmic_bytes(n: int, n3: int, zb: int, precision: str) -> dict:
-    """Compulsory bytes per launch of each kernel class.
+    """Algorithmic bytes per launch of each kernel class: the retained-mode
+    field passes the kernel performs, one field = one level of the retained
+    modes (the 2/3 disk, L=1) x s bytes, s = 8 (FP32 complex, mixed) or 16
+    (FP64).  The step as a whole moves 22 field passes (reads of q, q_old, BR,
+    BI, BR_old, BI_old, psi, AR, AI and writes of the seven phase-A results;
+    reads of q*, BR, BI and writes of psi, AR, AI in the solves); k_col_inv and
+    k_col_update each read q, BR and BI, so the kernels' passes add up to 25.
+    Kernels that touch only the (kx,y) scratch planes perform no field pass:
+    those planes are intermediate traffic (see traffic_model)."""
+    from qgybj.config import dealias_mask
+    s = 8 if precision == "mixed" else 16
+    fld = int(dealias_mask(n).sum()) * s      # one state field, one level
+    return {
+        "col_inv": zb * 4 * fld,              # psi, q, BR, BI
+        "row_main": 0,
+        "col_update": zb * 14 * fld,          # 8 read (q, qo, BR, BI, BRo, BIo, AR, AI), 6 written
+        "row_qw": 0,
+        "col_qw": zb * 2 * fld,               # q read, q* written
+        "solve": n3 * 6 * fld,                # q*, BR, BI read; psi, AR, AI written (one launch)
+        "solve_A": n3 * 4 * fld,              # BR, BI read; AR, AI written (the A solves on their own)
+        "dissipation": n3 * 2 * fld,
+        "step": 22 * fld * n3,
+        "step_dense": 22 * (n // 2 + 1) * n * n3 * s,
+    }
 
-    State fields count the retained modes (the 2/3 disk, L=1) once per read
-    or write; (kx,y) scratch planes count n*(K+1) complex values.  s = bytes
-    per complex value (8 mixed, 16 FP64)."""
+
+def traffic_model(n: int, zb: int, precision: str) -> dict:
+    """Bytes per launch each phase-A kernel moves when the (kx,y) scratch
+    planes round-trip through DRAM (one plane = n x (K+1) complex values of
+    one level): the state fields it reads and writes plus its plane reads and
+    writes.  Measured DRAM traffic per launch is compared with this."""
     from qgybj.config import dealias_mask, kmax
     s = 8 if precision == "mixed" else 16
-    retained = int(dealias_mask(n).sum())
-    K = kmax(n)
-    fld = retained * s              # one state field, one level
-    pln = n * (K + 1) * s           # one scratch plane, one level
+    fld = int(dealias_mask(n).sum()) * s
+    pln = n * (kmax(n) + 1) * s
     return {
         "col_inv": zb * (4 * fld + 6 * pln),
         "row_main": zb * (6 * pln + 6 * pln),
         "col_update": zb * (6 * pln + 14 * fld + 4 * pln),
         "row_qw": zb * (4 * pln + 2 * pln),
         "col_qw": zb * (2 * pln + 2 * fld),
-        "solve": n3 * 6 * fld,
-        "dissipation": n3 * 2 * fld,
-        "step": 22 * fld * n3,
-        "step_dense": 22 * (n // 2 + 1) * n * n3 * s,
     }
+
+
+def transform_flops(n: int, n3: int) -> dict:
+    """Floating-point operations of the transforms of one step as the kernels
+    execute them: radix-8/4/2 Stockham passes (a radix-8 butterfly is 56 real
+    additions/multiplications, a twiddle 6), 18 column transforms per retained
+    kx and level and 11 complex row transforms (two real rows each) per y and
+    level, plus the FP64 column solves (6 recurrences of 3 operations per
+    level and column, an FMA counted as 2)."""
+    from qgybj.config import dealias_mask, kmax
+    rad, rem = [], n
+    while rem > 1:
+        r = 8 if rem >= 8 else (4 if rem >= 4 else 2)
+        rad.append(r)
+        rem //= r
+    bfly = {8: 56, 4: 16, 2: 4}
+    per_fft, ns = 0, 1
+    for r in rad:
+        per_fft += (n // r) * (bfly[r] + (6 * (r - 1) if ns > 1 else 0))
+        ns *= r
+    K = kmax(n)
+    fft = (18 * (K + 1) + 11 * n) * per_fft * n3
+    solve = 6 * n3 * int(dealias_mask(n).sum()) * 5
+    return {"transforms": fft, "solve_fp64": solve, "per_complex_fft": per_fft}
+
+
+# ---------------------------------------------------------------------------
+# parity helpers
+# ---------------------------------------------------------------------------
+CHECK_STEPS = 3          # steps after which the oracle checks the full-size state (Euler + 2 leapfrog)
+PARITY_FIELDS = ("psi", "q", "LAr", "LAi", "BR", "BI")
+
+
+def rel_l2(a, b) -> float:
+    import numpy as np
+    nb = float(np.linalg.norm(b))
+    return float(np.linalg.norm(a - b)) / nb if nb else float(np.linalg.norm(a))
+
+
+def state_fields(sim, Bu: float) -> dict:
+    """psi, q, B and the wave field LA = B + kh^2 A/(4 Bu) (the field the
+    reference writes, diagnostics.f90:1698-1706) in the reference layout."""
+    from qgybj.config import la_from_b
+    g = {f: sim.get_state(f) for f in ("psi", "q", "BR", "BI", "AR", "AI")}
+    return {"psi": g["psi"], "q": g["q"], "BR": g["BR"], "BI": g["BI"],
+            "LAr": la_from_b(sim.n, Bu, g["BR"], g["AR"]), "LAi": la_from_b(sim.n, Bu, g["BI"], g["AI"])}
+
+
+def measured_fp64_peak(dev) -> float:
+    """FP64 TFLOP/s of cuBLAS DGEMM (8192^3, best of 3) on this GPU."""
+    import torch
+    a = torch.randn(8192, 8192, dtype=torch.float64, device=dev)
+    b = torch.randn(8192, 8192, dtype=torch.float64, device=dev)
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b
+    torch.cuda.empty_cache()
+    return 2.0 * 8192 ** 3 / (best / 1e3) / 1e12
 
 
 # ---------------------------------------------------------------------------
@@ -189,16 +275,21 @@ def run_ours(args, world, rank, local):
 
     dist = dist_setup(world, "nccl")
     torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
     rc = workload(args)
     precision = args.precision or rc.precision
     ic = make_initial_condition(rc)
     params = model_parameters(rc, ic.delt)
     sim = qgybj.Simulation(params, precision, device=local, levels_per_batch=rc.levels_per_batch,
                            solve_columns=rc.solve_columns)
-    sim.set_state("psi", ic.psi)
-    sim.set_state("BR", ic.BR)
-    sim.set_state("BI", ic.BI)
-    sim.init_state(True, True)
+
+    def init(s):
+        s.set_state("psi", ic.psi)
+        s.set_state("BR", ic.BR)
+        s.set_state("BI", ic.BI)
+        s.init_state(True, True)
+
+    init(sim)
     n, n3 = rc.n, rc.n3
     cells = n * n * n3
     # warm-up (the first step is the forward Euler start)
@@ -208,7 +299,7 @@ def run_ours(args, world, rank, local):
     prof = sim.profile_step(False)
     launches_per_step = sum(c for _, c in prof.values())
     # timed region
-    stream = torch.cuda.ExternalStream(sim.stream(), device=torch.device("cuda", local))
+    stream = torch.cuda.ExternalStream(sim.stream(), device=dev)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     clocks = ClockSampler(local)
@@ -225,7 +316,7 @@ def run_ours(args, world, rank, local):
     clk = clocks.stop()
     barrier(dist)
     ms = e0.elapsed_time(e1)
-    ms_max = reduce_max(dist, ms, device=torch.device("cuda", local))
+    ms_max = reduce_max(dist, ms, device=dev)
     value = whole_job_value(world, cells, args.steps, ms_max / 1e3)
     st = sim.diagnostics_fp64()
     finite = all(math.isfinite(v) for v in st.values())
@@ -279,34 +370,64 @@ def run_ours(args, world, rank, local):
                "ms": {"set_state_x9": (ta - t0) * 1e3, "steps": (tc - ta - t_diag) * 1e3,
                       "diagnostics": t_diag * 1e3, "get_state_x3": (t1 - tc) * 1e3}}
 
-    # FP64 GPU step on the same workload (the metric compares the two)
-    fp64 = None
+    # FP64 GPU step on the same workload (the metric compares the two), and
+    # parity: the mixed path against the FP64 path after the configuration's
+    # step count, per field; snapshots after CHECK_STEPS for the oracle check
+    fp64 = parity = None
+    snapshots = {}
     if not args.no_fp64 and precision == "mixed":
+        psteps = max(rc.steps, CHECK_STEPS + 1)
         sim64 = qgybj.Simulation(params, "fp64", device=local, levels_per_batch=CONFIGS["c1"].levels_per_batch,
-                                 solve_columns=CONFIGS["c1"].solve_columns)
-        sim64.set_state("psi", ic.psi); sim64.set_state("BR", ic.BR); sim64.set_state("BI", ic.BI)
-        sim64.init_state(True, True)
-        sim64.steps_async(2, True)
+                                 solve_columns=rc.solve_columns)
+        init(sim64)
+        s64 = torch.cuda.ExternalStream(sim64.stream(), device=dev)
+        k64 = max(2, min(args.fp64_steps, psteps - CHECK_STEPS - 1))
+        sim64.steps_async(CHECK_STEPS, True)
         sim64.synchronize()
-        s64 = torch.cuda.ExternalStream(sim64.stream(), device=torch.device("cuda", local))
-        k64 = max(2, min(args.steps, args.fp64_steps))
+        snapshots["fp64"] = state_fields(sim64, params["Bu"])
+        sim64.steps_async(1, False)          # warm: the leapfrog graph exists
+        sim64.synchronize()
         a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a0.record(s64)
         sim64.steps_async(k64, False)
         a1.record(s64)
         sim64.synchronize()
         ms64 = a0.elapsed_time(a1)
-        fp64 = {"value": cells * k64 / (ms64 / 1e3), "ms_per_step": ms64 / k64, "steps": k64}
+        sim64.steps_async(psteps - CHECK_STEPS - 1 - k64, False)
+        sim64.synchronize()
+        ref = state_fields(sim64, params["Bu"])
         sim64.close()
+        fl = transform_flops(n, n3)
+        peak64 = measured_fp64_peak(dev)
+        fp64 = {"value": cells * k64 / (ms64 / 1e3), "ms_per_step": ms64 / k64, "steps": k64,
+                "flops_per_step": fl["transforms"] + fl["solve_fp64"],
+                "achieved_tflops": (fl["transforms"] + fl["solve_fp64"]) / (ms64 / k64 / 1e3) / 1e12,
+                "peak_tflops": peak64, "peak_kind": "cuBLAS DGEMM 8192^3, best of 3, measured in this run",
+                "frac": (fl["transforms"] + fl["solve_fp64"]) / (ms64 / k64 / 1e3) / 1e12 / peak64}
+        init(sim)
+        sim.steps_async(CHECK_STEPS, True)
+        sim.synchronize()
+        snapshots["mixed"] = state_fields(sim, params["Bu"])
+        sim.steps_async(psteps - CHECK_STEPS, False)
+        sim.synchronize()
+        got = state_fields(sim, params["Bu"])
+        parity = {"mixed_vs_fp64_gpu": {"steps": psteps, "tolerance": 1e-5,
+                                        "relL2": {f: rel_l2(got[f], ref[f]) for f in PARITY_FIELDS}}}
 
     out = None
     if rank == 0:
         peak, peak_kind = measured_peak_hbm()
-        ab = algorithmic_bytes(n, n3, sim_batch(sim), precision)
+        zb = sim_batch(sim)
+        ab = algorithmic_bytes(n, n3, zb, precision)
+        if prof.get("solve_A", (0, 0))[1]:       # the psi solve alone: q* read, psi written
+            ab["solve"] = ab["solve"] // 3
+        tm = traffic_model(n, zb, precision)
         dom = max((k for k in prof if prof[k][1] > 0), key=lambda k: prof[k][0])
         dom_ms = prof[dom][0] / prof[dom][1]
         achieved = ab[dom] / (dom_ms / 1e3) / 1e9
         step_ms = ms / args.steps
+        fl = transform_flops(n, n3)
+        meas = MEASURED_TRAFFIC_PER_LEVEL.get((dom, n, precision))
         out = {
             "metric": "cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
@@ -319,21 +440,23 @@ def run_ours(args, world, rank, local):
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                          "algorithmic_bytes_per_launch": ab[dom], "ms_per_launch": dom_ms,
-                         "traffic": (MEASURED_TRAFFIC_PER_LEVEL[(dom, n, precision)] * sim_batch(sim)
-                                     if (dom, n, precision) in MEASURED_TRAFFIC_PER_LEVEL else None)},
+                         "traffic": meas * zb if meas else None,
+                         "traffic_model": tm.get(dom)},
             "step_roofline": {"bytes_per_step": ab["step"], "achieved": ab["step"] / (step_ms / 1e3) / 1e9,
                               "frac": ab["step"] / (step_ms / 1e3) / 1e9 / peak, "unit": "GB/s",
                               "bytes_per_step_dense_layout": ab["step_dense"],
-                              "frac_dense_layout": ab["step_dense"] / (step_ms / 1e3) / 1e9 / peak},
+                              "frac_dense_layout": ab["step_dense"] / (step_ms / 1e3) / 1e9 / peak,
+                              "fp32_transform_tflops": fl["transforms"] / (step_ms / 1e3) / 1e12},
             "kernels_ms_per_step": {k: v[0] for k, v in prof.items() if v[1]},
             "launches_per_step": {k: v[1] for k, v in prof.items() if v[1]},
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clk, "e2e": e2e, "fp64_gpu": fp64,
             "mixed_over_fp64": (value / world / fp64["value"]) if fp64 else None,
+            "parity": parity,
             "state_finite": finite,
         }
     sim.close()
-    return out
+    return out, snapshots
 
 
 def workload(args):
@@ -554,6 +677,53 @@ def cpu_oracle_rate(rc, nz: int, steps: int, warm: int, workers: int):
     return rc.n * rc.n * nz * steps / dt, dt
 
 
+def cpu_baseline_leg(rc, snapshots: dict):
+    """The oracle on the host cores over the full workload: CHECK_STEPS steps
+    from the seeded initial condition (Euler start, then leapfrog steps), the
+    leapfrog steps timed as the CPU baseline; the states it reaches are the
+    checker of the GPU snapshots taken after the same steps (per-field
+    relative L2 of the mixed and FP64 paths)."""
+    from oracle import qgybj_oracle as orc
+    from qgybj.config import make_initial_condition, model_parameters
+    workers = os.cpu_count() or 1
+    orc.set_workers(workers)
+    ic = make_initial_condition(rc)
+    params = model_parameters(rc, ic.delt)
+    keys = ("n1", "n2", "n3", "dz", "Bu", "Ro", "W2F", "delt", "gamma", "nuh1", "nuh2", "ilap1", "ilap2",
+            "nuh1w", "nuh2w", "ilap1w", "ilap2w", "nuz", "a_ell_ut", "r_2ut")
+    model = orc.Model(orc.Params(**{k: params[k] for k in keys}))
+    st = orc.initial_state(model, ic.psi, ic.BR, ic.BI)
+    st = model.step(st, True)
+    t0 = time.perf_counter()
+    for _ in range(CHECK_STEPS - 1):
+        st = model.step(st, False)
+    secs = time.perf_counter() - t0
+    value = rc.n * rc.n * rc.n3 * (CHECK_STEPS - 1) / secs
+    base = {"value": value, "unit": "cell-steps/s", "cores": workers, "kind": "port",
+            "sample": f"oracle (FP64 numpy/scipy restatement of the reference step) on the full {rc.n}x{rc.n}x{rc.n3} "
+                      f"{rc.name} workload, {CHECK_STEPS - 1} leapfrog steps after the Euler start ({secs:.1f} s)"}
+    vs = None
+    if snapshots:
+        ref = {"psi": st.psi, "q": st.q, "BR": st.BR, "BI": st.BI,
+               "LAr": model.la_from_b(st.BR, st.AR), "LAi": model.la_from_b(st.BI, st.AI)}
+        vs = {"steps": CHECK_STEPS, "tolerance": {"mixed": 1e-5, "fp64": 1e-12}}
+        for prec, got in snapshots.items():
+            vs[prec] = {f: rel_l2(got[f], ref[f]) for f in PARITY_FIELDS}
+    return base, vs
+
+
+def adjoint_cost(args, local) -> dict:
+    """The adjoint-to-forward cost on the C4 workload (128^2 x 64 FP64, J
+    after 50 steps, checkpoints every 10), as --config c4 measures it."""
+    a = argparse.Namespace(**vars(args))
+    a.config, a.steps, a.warmup, a.ckpt, a.n, a.n3, a.levels_per_batch = "c4", 50, 3, 10, 0, 0, 0
+    r = run_adjoint(a, 1, 0, local)
+    return {k: r[k] for k in ("forward_ms", "gradient_ms", "forward_step_ms", "adjoint_step_ms",
+                              "adjoint_step_over_forward_step")} | {
+        "gradient_over_forward": r["value"], "workload": r["config"]["workload"], "steps": r["steps"],
+        "checkpoint_every": r["config"]["checkpoint_every"], "clocks": r["clocks"]}
+
+
 def run_reference(args, world, rank, local):
     if rank != 0:
         return None
@@ -571,7 +741,9 @@ def run_reference(args, world, rank, local):
         "metric": "cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": {"workload": rc.name, "n1": rc.n, "n2": rc.n, "n3": rc.n3, "sample_levels": nz},
+        "config": {"workload": f"{rc.name}:slab_{rc.n}x{rc.n}x{nz}", "n1": rc.n, "n2": rc.n, "n3": rc.n3,
+                   "sample_levels": nz,
+                   "note": "cost per cell-step is independent of the level count; the slab keeps the run short"},
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": workers, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -594,8 +766,7 @@ def main(argv=None):
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-baseline-levels", type=int, default=64)
-    ap.add_argument("--cpu-baseline-steps", type=int, default=6)
+    ap.add_argument("--no-adjoint", action="store_true", help="c2: skip the adjoint/forward cost measurement")
     ap.add_argument("--reference-budget-s", type=float, default=120.0)
     ap.add_argument("--members", type=int, default=0, help="c3: first M ensemble members only")
     ap.add_argument("--ckpt", type=int, default=10, help="c4: checkpoint spacing of the adjoint")
@@ -613,15 +784,13 @@ def main(argv=None):
     elif args.config == "c4":
         out = run_adjoint(args, world, rank, local)
     else:
-        out = run_ours(args, world, rank, local)
+        out, snapshots = run_ours(args, world, rank, local)
+        if out is not None and world == 1 and not args.no_adjoint and args.config == "c2":
+            out["adjoint"] = adjoint_cost(args, local)
         if out is not None and world == 1 and not args.no_cpu_baseline:
-            rc = workload(args)
-            workers = os.cpu_count() or 1
-            v, secs = cpu_oracle_rate(rc, args.cpu_baseline_levels, args.cpu_baseline_steps, 0, workers)
-            out["cpu_baseline"] = {
-                "value": v, "unit": "cell-steps/s", "cores": workers, "kind": "port",
-                "sample": f"oracle on a {rc.n}x{rc.n}x{args.cpu_baseline_levels} slab of {rc.name}, "
-                          f"{args.cpu_baseline_steps} leapfrog steps ({secs:.1f} s)"}
+            out["cpu_baseline"], vs_oracle = cpu_baseline_leg(workload(args), snapshots)
+            if vs_oracle and out.get("parity") is not None:
+                out["parity"]["vs_oracle"] = vs_oracle
     if out is not None:
         print(json.dumps(out), flush=True)
 

@@ -28,7 +28,9 @@ enum qg_status {
   QG_OK = 0,
   QG_ERR_ARG = 1,          /* bad dimensions, null pointer, unknown field id       */
   QG_ERR_CUDA = 2,         /* a CUDA runtime call or kernel launch failed          */
-  QG_ERR_NONFINITE = 3,    /* NaN/Inf in an input array                            */
+  QG_ERR_NONFINITE = 3,    /* NaN/Inf in an input array (configuration, or a       *
+                            * retained mode given to qg_set_state), or a step     *
+                            * that produced a non-finite q*                       */
   QG_ERR_PIVOT = 4,        /* zero or non-dominant pivot in a tridiagonal factor   */
                            /*   (the DGTSV INFO>0 case, elliptic.f90:192,209)      */
   QG_ERR_TIMEOUT = 5,      /* a bounded device-side wait expired                   */
@@ -115,7 +117,9 @@ const char* qg_last_error(const qg_handle* h);
 
 /* Host <-> device copies of the resident state, levels [level0, level0+nlev).
  * kvar is [nlev][ikty][iktx] interleaved complex.  Values on modes with L=0
- * are discarded by qg_set_state (every step of the reference zeroes them). */
+ * are discarded by qg_set_state (every step of the reference zeroes them);
+ * a NaN or infinity on a retained mode makes qg_set_state return
+ * QG_ERR_NONFINITE (the values are stored all the same). */
 int qg_set_state(qg_handle* h, int field, const double* kvar, int level0, int nlev);
 int qg_get_state(qg_handle* h, int field, double* kvar, int level0, int nlev);
 
@@ -128,12 +132,18 @@ int qg_init_state(qg_handle* h, int apply_sumB, int q_from_psi);
 /* With fixed_flow = 1, q is set to 0 instead (main_waqg.f90:141-146). */
 
 /* One full time step on the device: main_waqg.f90:202-317 (euler_first=1,
- * forward Euler) or 331-467 (leapfrog + Robert-Asselin filter). */
+ * forward Euler) or 331-467 (leapfrog + Robert-Asselin filter).  Returns
+ * QG_ERR_NONFINITE when the step's q* (= q - q^w, which depends on q and B)
+ * holds a NaN or infinity on a retained mode: the run has blown up (the
+ * reference would carry on and write NaN to its dumps). */
 int qg_step(qg_handle* h, int euler_first);
 
 /* nsteps steps; the first is forward Euler when euler_first=1.  Asynchronous:
  * returns once the work is queued on the handle's stream. */
 int qg_steps_async(qg_handle* h, int nsteps, int euler_first);
+/* Waits for h's stream; reports what its kernels raised since the last
+ * check: QG_ERR_TIMEOUT (a bounded wait expired) or QG_ERR_NONFINITE (a
+ * queued step produced a non-finite q*). */
 int qg_synchronize(qg_handle* h);
 
 /* Failure-path check of the bounded device-side waits: runs on h's stream a
@@ -156,8 +166,10 @@ enum qg_kernel_class {
   QG_K_COL_UPDATE = 3,   /* y-forward transforms, leapfrog/filter, q^w y-inverse    */
   QG_K_ROW_QW = 4,       /* x-transforms and products of compute_qw                 */
   QG_K_COL_QW = 5,       /* y-forward transforms of q^w, q* = q - q^w               */
-  QG_K_SOLVE = 6,        /* FP64 tridiagonal solves q*->psi, B->A                   */
-  QG_K_NCLASSES = 7
+  QG_K_SOLVE = 6,        /* FP64 tridiagonal solves q*->psi (and B->A when not split) */
+  QG_K_SOLVE_A = 7,      /* FP64 tridiagonal solves B->A on their own: they run beside *
+                          * the q^w kernels in a step, one after another when profiled */
+  QG_K_NCLASSES = 8
 };
 
 /* Profiling aid (no counterpart in the reference): runs one step without the
@@ -258,6 +270,9 @@ int qg_ensemble_step(qg_ensemble* e, int nsteps, int euler_first);
  * largest first, each to the chain with the fewest cells so far.  Drops the
  * captured graphs; results do not depend on it. */
 int qg_ensemble_set_lanes(qg_ensemble* e, int lanes);
+/* Waits for the ensemble's stream; QG_ERR_TIMEOUT / QG_ERR_NONFINITE as
+ * qg_synchronize for the first member that raised one (named in the error
+ * text); every member's status is cleared. */
 int qg_ensemble_synchronize(qg_ensemble* e);
 int qg_ensemble_get_stream(qg_ensemble* e, void** stream);
 int qg_ensemble_destroy(qg_ensemble* e);
@@ -291,8 +306,14 @@ int qg_autotune(const qg_config* cfg, int nsteps, qg_tuning* out);
  * synchronises the whole device and would stall work on other streams).
  * The caller owns both buffers; the call allocates nothing (no cudaMalloc,
  * cudaFree or allocating library routine).  FP64.
- *   kvar: device pointer, interleaved complex [nz][n][n/2+1] (read only)
- *   rvar: device pointer, double [nz][n][n+2]; the two padding values per row are 0
+ *   kvar: device pointer, interleaved complex [nz][n][n/2+1] (read only),
+ *         16-byte aligned (read as complex pairs)
+ *   rvar: device pointer, double [nz][n][n+2], 8-byte aligned; the two
+ *         padding values per row are 0
+ * Both must be memory of the current device (or managed memory); anything
+ * else, and a misaligned pointer, is QG_ERR_ARG before any launch.  A CUDA
+ * error already pending from the caller's earlier work is left in place and
+ * the call returns QG_ERR_CUDA without launching.
  * The (kx,y) intermediate lives in a file-scope 8 MiB static device array,
  * held by every GPU that loads the library until the process exits: n must
  * be a power of two in [16, 512] so that one level's plane fits, otherwise

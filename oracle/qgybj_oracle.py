@@ -39,6 +39,19 @@ def set_workers(n: int) -> None:
     _WORKERS = max(1, int(n))
 
 
+# Floating type the 2D FFTs compute in: float64 (the reference's FFTW in
+# double precision), or np.longdouble for a sensitivity check: the transforms
+# then round differently (80-bit extended on x86-64) while every other
+# operation stays FP64, so the difference between the two runs measures how
+# far FP64 roundoff of the transforms alone carries through the step.
+_FFT_DTYPE = np.float64
+
+
+def set_fft_dtype(dtype) -> None:
+    global _FFT_DTYPE
+    _FFT_DTYPE = np.dtype(dtype).type
+
+
 # ---------------------------------------------------------------------------
 # L0: grid, dealiasing mask, base state, integrating-factor tables
 # ---------------------------------------------------------------------------
@@ -212,6 +225,9 @@ class Model:
     # -- spectral transforms (fft.f90) -------------------------------------
     def fft_r2c(self, r: np.ndarray) -> np.ndarray:
         """fft.f90:55-66: per-level 2D r2c, then divided by n1*n2."""
+        if _FFT_DTYPE is not np.float64:
+            k = sfft.rfft2(r.astype(_FFT_DTYPE), axes=(-2, -1), norm="forward", workers=_WORKERS)
+            return k.astype(np.complex128)
         return sfft.rfft2(r, axes=(-2, -1), norm="forward", workers=_WORKERS)
 
     def realit(self, k: np.ndarray) -> np.ndarray:
@@ -225,6 +241,10 @@ class Model:
     def fft_c2r(self, k: np.ndarray) -> np.ndarray:
         """fft.f90:71-83: realit, then unnormalised per-level 2D c2r."""
         k = self.realit(k)
+        if _FFT_DTYPE is not np.float64:
+            kd = k.astype(np.result_type(_FFT_DTYPE, np.complex64))
+            r = sfft.irfft2(kd, s=(self.p.n2, self.p.n1), axes=(-2, -1), norm="forward", workers=_WORKERS)
+            return r.astype(np.float64)
         return sfft.irfft2(k, s=(self.p.n2, self.p.n1), axes=(-2, -1),
                            norm="forward", workers=_WORKERS)
 

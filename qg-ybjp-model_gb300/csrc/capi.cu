@@ -529,7 +529,7 @@ static int ens_capture(qg_ensemble* e, int euler) {
   cudaError_t ce = cudaStreamEndCapture(e->master, &graph);
   if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
   if (ce != cudaSuccess) return ens_fail(e, QG_ERR_CUDA, std::string("ensemble capture: ") + cudaGetErrorString(ce));
-  ce = cudaGraphInstantiate(&e->gexec[euler], graph, 0);
+  ce = cudaGraphInstantiate(&e->gexec[euler], graph, cudaGraphInstantiateFlagUseNodePriority);
   cudaGraphDestroy(graph);
   if (ce != cudaSuccess) return ens_fail(e, QG_ERR_CUDA, std::string("ensemble instantiate: ") + cudaGetErrorString(ce));
   return QG_OK;
@@ -561,7 +561,16 @@ int qg_ensemble_set_lanes(qg_ensemble* e, int lanes) {
 int qg_ensemble_synchronize(qg_ensemble* e) {
   if (!e) return QG_ERR_ARG;
   ENS_CK(cudaStreamSynchronize(e->master));
-  return QG_OK;
+  // every member's device-raised status (expired wait, non-finite q*)
+  int first = QG_OK;
+  for (size_t m = 0; m < e->members.size(); ++m) {
+    const int rc = e->members[m]->eng->check_waits();
+    if (rc && !first) {
+      first = rc;
+      e->err = "member " + std::to_string(m) + ": " + e->members[m]->eng->err;
+    }
+  }
+  return first;
 }
 
 int qg_ensemble_get_stream(qg_ensemble* e, void** stream) {

@@ -202,4 +202,60 @@ __device__ __forceinline__ void ip_passes_but_last(cplx<T>* buf, const cplx<T>* 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Forward row transforms of N = 512 (radices 8 x 8 x 8) ending in registers.
+//
+// A packed transform F = FFT(x + i y) of two real rows is split into the half
+// spectra X[k] = (F[k] + conj F[N-k])/2, Y[k] = (F[k] - conj F[N-k])/(2i),
+// k <= K.  The last Stockham pass (NS = 64) leaves task j holding F at
+// k = j + 64 r, r = 0..7, and F[N-k] at task 64 - j, r' = 7 - r (task 0 and
+// task 32 hold both).  Tasks are placed so that j and 64 - j sit in lanes l
+// and l ^ 16 of one warp: warp half h = 0 takes j = 0..15, 32, 63..49 and
+// h = 1 takes j = 16..31, 48..33.  The partner values then come by three
+// shuffles per transform instead of a round trip through shared memory.
+// ---------------------------------------------------------------------------
+struct RowLastTask {
+  int j;      // butterfly index of the last pass
+  bool self;  // j == 0 or j == 32: F[N-k] is this task's own value
+};
+__device__ __forceinline__ RowLastTask row_last_task(int t) {
+  const int l = t & 31, h = (t >> 5) & 1;
+  RowLastTask r;
+  r.j = h == 0 ? (l < 16 ? l : (l == 16 ? 32 : 80 - l)) : (l < 16 ? 16 + l : 64 - l);
+  r.self = r.j == 0 || r.j == 32;
+  return r;
+}
+
+// Last forward pass of one transform stored at tr (layout LAY) for task j:
+// w[r] = F[j + 64 r]; then b[r] = F[N - (j + 64 r)] for r = 0, 1, 2.  Every
+// lane of the warp must call (the shuffles are warp-wide).
+template <typename T, int LAY>
+__device__ __forceinline__ void row_last_fwd512(const cplx<T>* __restrict__ tr, const cplx<T>* __restrict__ tw,
+                                                RowLastTask tk, cplx<T> (&w)[8], cplx<T> (&b)[3]) {
+  constexpr int N = 512, NS = 64, R = 8;
+  constexpr int off = tw_off<N>(NS);
+  const int j = tk.j;
+#pragma unroll
+  for (int r = 0; r < R; ++r) w[r] = tr[lay_idx<LAY>(j + r * NS)];
+#pragma unroll
+  for (int r = 1; r < R; ++r) w[r] = cmul(w[r], tw[off + (r - 1) * NS + j]);
+  dftR<T, R, true>(w);
+  cplx<T> t[3];
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    t[q].x = __shfl_xor_sync(0xffffffffu, w[7 - q].x, 16);
+    t[q].y = __shfl_xor_sync(0xffffffffu, w[7 - q].y, 16);
+  }
+  if (j == 0) { b[0] = w[0]; b[1] = w[7]; b[2] = w[6]; }
+  else if (j == 32) { b[0] = w[7]; b[1] = w[6]; b[2] = w[5]; }
+  else { b[0] = t[0]; b[1] = t[1]; b[2] = t[2]; }
+}
+
+// the half spectra at k from a = F[k], b = F[N-k] (unpack_spec's arithmetic)
+template <typename T>
+__device__ __forceinline__ void split_pair(cplx<T> a, cplx<T> b, cplx<T>& X, cplx<T>& Y) {
+  X = mk<T>((a.x + b.x) * (T)0.5, (a.y - b.y) * (T)0.5);
+  Y = mk<T>((a.y + b.y) * (T)0.5, (b.x - a.x) * (T)0.5);
+}
+
 }  // namespace qg

@@ -35,6 +35,9 @@ struct EngineBase {
   virtual int step(int euler) = 0;
   virtual int steps_async(int nsteps, int euler) = 0;
   virtual int synchronize() = 0;
+  // status flags raised on the device since the last check (the stream must
+  // have drained): QG_ERR_TIMEOUT, QG_ERR_NONFINITE or QG_OK
+  virtual int check_waits() = 0;
   // runs k_wait_expire on the stream; QG_ERR_TIMEOUT expected
   virtual int selftest_wait() = 0;
   virtual void* stream() = 0;

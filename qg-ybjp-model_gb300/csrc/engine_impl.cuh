@@ -51,7 +51,15 @@ class Engine : public EngineBase {
     g.n = t.n; g.n3 = t.n3; g.K = t.K; g.KX = t.KX; g.KY = t.KY; g.KXP = t.KXP; g.kmax2 = t.kmax2;
     g.plane = t.plane;
     QG_CK(cudaSetDevice(cfg.device));
-    QG_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    // the step's stream at the highest priority, the overlapped A solves on
+    // a second stream at the lowest: pending CTAs of the FP32 kernels are
+    // placed first and the solves fill the room they leave
+    int prio_low = 0, prio_high = 0;
+    QG_CK(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
+    QG_CK(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, prio_high));
+    QG_CK(cudaStreamCreateWithPriority(&st2, cudaStreamNonBlocking, prio_low));
+    QG_CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    QG_CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
     const size_t fbytes = (size_t)g.n3 * g.plane * sizeof(C);
     for (int f = 0; f < F_NINT; ++f) {
       if (f == F_DQ && !(cfg.inviscid == 0 && cfg.nuz != 0.0)) continue;
@@ -101,9 +109,11 @@ class Engine : public EngineBase {
     QG_CK(cudaMalloc(&diag_part, (size_t)g.n3 * kDiagChunks * kNDiag * sizeof(double)));
     QG_CK(cudaMalloc(&diag_out, kNDiag * sizeof(double)));
     QG_CK(cudaMallocHost(&diag_host, kNDiag * sizeof(double)));
-    QG_CK(cudaHostAlloc(&wflag_h, sizeof(int), cudaHostAllocMapped));
-    *wflag_h = 0;
+    QG_CK(cudaHostAlloc(&wflag_h, 3 * sizeof(int), cudaHostAllocMapped));
+    wflag_h[0] = wflag_h[1] = wflag_h[2] = 0;
     QG_CK(cudaHostGetDevicePointer(&wflag, wflag_h, 0));
+    nflag = wflag + 1;
+    iflag = wflag + 2;
     QG_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, cfg.device));
     // phase-A batching: by default as many levels per batch as 1.25 GB of
     // scratch planes hold (deep batches run fewer, fuller waves and longer
@@ -196,13 +206,19 @@ class Engine : public EngineBase {
     return synchronize();
   }
 
-  // QG_ERR_TIMEOUT when a kernel's bounded wait expired since the last check
-  // (call after the stream has drained)
-  int check_waits() {
+  // QG_ERR_TIMEOUT when a kernel's bounded wait expired since the last check,
+  // QG_ERR_NONFINITE when a step produced a NaN or infinite q* (call after
+  // the stream has drained)
+  int check_waits() override {
     if (wflag_h && *(volatile int*)wflag_h) {
       *(volatile int*)wflag_h = 0;
       err = "a bounded device-side wait expired (bulk copy of the row kernels)";
       return QG_ERR_TIMEOUT;
+    }
+    if (wflag_h && *(volatile int*)(wflag_h + 1)) {
+      *(volatile int*)(wflag_h + 1) = 0;
+      err = "non-finite q* after a step: the state has blown up (time step too large?)";
+      return QG_ERR_NONFINITE;
     }
     return QG_OK;
   }
@@ -222,7 +238,8 @@ class Engine : public EngineBase {
       QG_CK(cudaMemcpyAsync(stage, kvar, bytes, cudaMemcpyDefault, st));
       src = (const double2*)stage;
     }
-    k_dense_to_compact<T><<<grid_for((long long)nlev * g.plane), 256, 0, st>>>(g, level0, nlev, src, F[f]);
+    *(volatile int*)(wflag_h + 2) = 0;
+    k_dense_to_compact<T><<<grid_for((long long)nlev * g.plane), 256, 0, st>>>(g, level0, nlev, src, F[f], iflag);
     QG_LAUNCHED();
     if (f == F_PSI && sizeof(T) == 4) {
       // mixed path: keep psi in FP64 until qg_init_state has built q from it
@@ -232,6 +249,11 @@ class Engine : public EngineBase {
       QG_LAUNCHED();
     }
     QG_CK(cudaStreamSynchronize(st));
+    if (*(volatile int*)(wflag_h + 2)) {
+      *(volatile int*)(wflag_h + 2) = 0;
+      err = "non-finite value (NaN or Inf) on a retained mode of the input array";
+      return QG_ERR_NONFINITE;
+    }
     return QG_OK;
   }
 
@@ -538,6 +560,8 @@ class Engine : public EngineBase {
   Geom g{};
   StepParams sp{};
   cudaStream_t st = nullptr;
+  cudaStream_t st2 = nullptr;                          // the overlapped A solves
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;   // B^{n+1} ready / A solves done
   C* F[F_NINT] = {};
   T *e1 = nullptr, *e2 = nullptr, *e1w = nullptr, *e2w = nullptr;
   C* tw = nullptr;
@@ -549,8 +573,13 @@ class Engine : public EngineBase {
   double *du = nullptr, *cu = nullptr, *cl = nullptr, *r2 = nullptr;
   double *diag_part = nullptr, *diag_out = nullptr, *diag_host = nullptr;
   // set by a kernel whose bounded wait expired (mapped page-locked word)
+  // mapped page-locked words raised on the device: [0] a bounded wait
+  // expired, [1] a step produced a non-finite q*, [2] qg_set_state's input
+  // held a non-finite retained mode (wflag, nflag, iflag: device views)
   int* wflag_h = nullptr;
   int* wflag = nullptr;
+  int* nflag = nullptr;
+  int* iflag = nullptr;
   int nsm = 1, occ_rm = 1, occ_rq = 1;   // SMs; resident CTAs per SM of the persistent row kernels
   double *om_t1 = nullptr, *om_du = nullptr, *om_dl = nullptr, *om_a = nullptr, *om_scr = nullptr;
   C* sig[2] = {};     // regular YBJ: per-level sigma terms
@@ -582,6 +611,14 @@ class Engine : public EngineBase {
     if (wflag_h) cudaFreeHost(wflag_h);
     wflag_h = nullptr;
     wflag = nullptr;
+    nflag = nullptr;
+    iflag = nullptr;
+    if (st2) cudaStreamSynchronize(st2);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    ev_fork = ev_join = nullptr;
+    if (st2) cudaStreamDestroy(st2);
+    st2 = nullptr;
     if (st) cudaStreamDestroy(st);
     st = nullptr;
   }
@@ -668,17 +705,17 @@ class Engine : public EngineBase {
   // Profiling: events around each launch when prof_on is set.
   bool prof_on = false;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_ev;
-  int pbeg(int kind) {
+  int pbeg(int kind, cudaStream_t on = nullptr) {
     if (!prof_on) return QG_OK;
     cudaEvent_t a, b;
     QG_CK(cudaEventCreate(&a)); QG_CK(cudaEventCreate(&b));
-    QG_CK(cudaEventRecord(a, st));
+    QG_CK(cudaEventRecord(a, on ? on : st));
     prof_ev.push_back({kind, {a, b}});
     return QG_OK;
   }
-  int pend() {
+  int pend(cudaStream_t on = nullptr) {
     if (!prof_on) return QG_OK;
-    QG_CK(cudaEventRecord(prof_ev.back().second.second, st));
+    QG_CK(cudaEventRecord(prof_ev.back().second.second, on ? on : st));
     return QG_OK;
   }
 
@@ -719,8 +756,15 @@ class Engine : public EngineBase {
       if (int rc0 = pend()) return rc0;
     }
     StateP<T> sptr = state_ptrs();
+    const int do_psi = cfg.fixed_flow ? 0 : 1;
+    const int do_A = (cfg.passive_scalar || !cfg.ybj_plus) ? 0 : 1;
+    // A solves beside the q^w kernels (a second stream; serialised while
+    // profiling so that every launch is timed alone)
+    const bool split = kSolveOverlap && need_qw && do_psi && do_A && kSolveStore && vbuf;
+    const bool overlap = split && !prof_on;
     for (int z0 = 0; z0 < g.n3; z0 += Zb) {
       const int zc = std::min(Zb, g.n3 - z0);
+      const bool last = z0 + Zb >= g.n3;
       QG_SWITCH_N(g.n, {
         const dim3 gc(g.KXP / Tiles<T, NN>::CT, zc), gr(g.n / Tiles<T, NN>::RRT, zc),
             grm(g.n / Tiles<T, NN>::RTM, zc);
@@ -743,11 +787,19 @@ class Engine : public EngineBase {
                                                                 need_qw ? 1 : 0);
         QG_LAUNCHED();
         if (int rc0 = pend()) return rc0;
+        if (overlap && last) {
+          // B^{n+1} of every level is written: fork the A solves
+          QG_CK(cudaEventRecord(ev_fork, st));
+          QG_CK(cudaStreamWaitEvent(st2, ev_fork, 0));
+          if (int rc0 = solve_generic(nullptr, F[F_BR], F[F_BI], nullptr, F[F_AR], F[F_AI], 0, 1, st2)) return rc0;
+          QG_CK(cudaEventRecord(ev_join, st2));
+        }
         if (need_qw) {
           if (int rc0 = pbeg(QG_K_ROW_QW)) return rc0;
           if constexpr (Tiles<T, NN>::QPRE) {
             const int items = zc * (NN / Tiles<T, NN>::RRT);
-            k_row_qw<T, NN><<<std::min(items, nsm * occ_rq), Tiles<T, NN>::QTHREADS, sm_rq<NN>(g.KXP), st>>>(
+            const int per_sm = (split && last) ? std::max(1, occ_rq - kQwReserve) : occ_rq;
+            k_row_qw<T, NN><<<std::min(items, nsm * per_sm), Tiles<T, NN>::QTHREADS, sm_rq<NN>(g.KXP), st>>>(
                 g, S, tw, items, wflag);
           } else {
             k_row_qw<T, NN><<<gr, Tiles<T, NN>::QTHREADS, sm_rq<NN>(g.KXP), st>>>(g, S, tw, 0, wflag);
@@ -755,16 +807,22 @@ class Engine : public EngineBase {
           QG_LAUNCHED();
           if (int rc0 = pend()) return rc0;
           if (int rc0 = pbeg(QG_K_COL_QW)) return rc0;
-          k_col_qw<T, NN><<<gc, kThreadsB, sm_ci<NN>(2), st>>>(g, s, z0, F[F_Q], F[F_QSTAR], S, tw);
+          k_col_qw<T, NN><<<gc, kThreadsB, sm_ci<NN>(2), st>>>(g, s, z0, F[F_Q], F[F_QSTAR], S, tw, nflag);
           QG_LAUNCHED();
           if (int rc0 = pend()) return rc0;
         }
       });
     }
     if (int rc0 = pbeg(QG_K_SOLVE)) return rc0;
-    int rc = launch_solve(need_qw ? F[F_QSTAR] : F[F_Q], cfg.fixed_flow ? 0 : 1,
-                          (cfg.passive_scalar || !cfg.ybj_plus) ? 0 : 1);
+    int rc = launch_solve(need_qw ? F[F_QSTAR] : F[F_Q], do_psi, split ? 0 : do_A);
     if (rc) return rc;
+    if (overlap) {
+      QG_CK(cudaStreamWaitEvent(st, ev_join, 0));
+    } else if (split) {
+      if (int rc0 = pend()) return rc0;
+      if (int rc0 = pbeg(QG_K_SOLVE_A)) return rc0;
+      if ((rc = launch_solve(nullptr, 0, 1))) return rc;
+    }
     if (!cfg.ybj_plus && !cfg.passive_scalar) {
       // regular YBJ: sumB on B^{n+1}, then A from the vertical integral (main_waqg.f90:449-460)
       k_ybj_A<T><<<(unsigned)((g.plane + 127) / 128), 128, 0, st>>>(g, cfg.dz, cfg.Bu, cfg.Ro, r2, F[F_BR], F[F_BI],
@@ -778,11 +836,14 @@ class Engine : public EngineBase {
     return solve_generic(qs, F[F_BR], F[F_BI], F[F_PSI], F[F_AR], F[F_AI], do_psi, do_A);
   }
 
-  int solve_generic(const C* qs, const C* br, const C* bi, C* psi, C* ar, C* ai, int do_psi, int do_A) {
+  int solve_generic(const C* qs, const C* br, const C* bi, C* psi, C* ar, C* ai, int do_psi, int do_A,
+                    cudaStream_t on = nullptr) {
     if (!do_psi && !do_A) return QG_OK;
+    if (!on) on = st;
     if (kSolveStore && vbuf) {
+      const int nrec = (do_psi ? 2 : 0) + (do_A ? 4 : 0);   // recurrences per column
 #define QG_SOLVE_ST(TCV, PCV)                                                                              \
-  k_solve_st<T, TCV, PCV><<<(unsigned)((g.plane + TCV - 1) / TCV), 6 * TCV, (size_t)g.n3 * 8, st>>>(      \
+  k_solve_st<T, TCV, PCV><<<(unsigned)((g.plane + TCV - 1) / TCV), nrec * TCV, (size_t)g.n3 * 8, on>>>(   \
       g, cfg.dz, cfg.Bu, tab_idx, fac_psi, fac_A, du, qs, br, bi, psi, ar, ai, do_psi, do_A, vbuf, pcfac)
       if (pcfac) {
         if (solve_tc == 16) QG_SOLVE_ST(16, true);
@@ -797,7 +858,7 @@ class Engine : public EngineBase {
       QG_LAUNCHED();
       return QG_OK;
     }
-    k_solve<T><<<(unsigned)((g.plane + kSolveTC - 1) / kSolveTC), kSolveThreads, solve_smem(g.n3), st>>>(g, cfg.dz, cfg.Bu, tab_idx, fac_psi, fac_A,
+    k_solve<T><<<(unsigned)((g.plane + kSolveTC - 1) / kSolveTC), kSolveThreads, solve_smem(g.n3), on>>>(g, cfg.dz, cfg.Bu, tab_idx, fac_psi, fac_A,
                                                                            du, qs, br, bi, psi, ar, ai, do_psi, do_A);
     QG_LAUNCHED();
     return QG_OK;
@@ -812,7 +873,7 @@ class Engine : public EngineBase {
       cudaError_t e = cudaStreamEndCapture(st, &graph);
       if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
       if (e != cudaSuccess) { err = std::string("graph capture: ") + cudaGetErrorString(e); return QG_ERR_CUDA; }
-      e = cudaGraphInstantiate(&gexec[euler], graph, 0);
+      e = cudaGraphInstantiate(&gexec[euler], graph, cudaGraphInstantiateFlagUseNodePriority);
       cudaGraphDestroy(graph);
       if (e != cudaSuccess) { err = std::string("graph instantiate: ") + cudaGetErrorString(e); return QG_ERR_CUDA; }
     }

@@ -58,6 +58,11 @@ constexpr bool kRowSwizzle = true;  // k_row_qw (N = 512): conflict-free XOR pla
 constexpr bool kRowMainSwizzle = false;  // k_row_main: the same (its index arithmetic spills at 128 registers)
 constexpr bool kRowMainMidSwz = false;   // k_row_main forward transforms: XOR placement between the last two passes (measured slower: spills)
 constexpr bool kRowMainMidSwzInv = false;  // the same for its inverse transforms (spills: the last pass feeds the products)
+#ifndef QG_ROW_SHFL_LAST
+#define QG_ROW_SHFL_LAST 1
+#endif
+// fused row kernels (N = 512): last forward pass and spectrum split in registers (warp shuffles)
+constexpr bool kRowShflLast = QG_ROW_SHFL_LAST != 0;
 constexpr bool kUpdTablesSmem = true;   // k_col_update (FP32 lean): IF tables staged in shared memory
 constexpr bool kUpdLean = true;    // k_col_update (FP32): smaller shared footprint ...
 constexpr bool kUpdStage16 = true; // k_col_update (FP32): state staged by 16-byte copies
@@ -115,6 +120,10 @@ template <typename T, int N> struct Tiles {
   static constexpr int RMID = !kRowMainSwizzle && kRowMainMidSwz && RFUSE && N == 512 ? 1 : 0;
   static constexpr int RMIDI = !kRowMainSwizzle && kRowMainMidSwzInv && RFUSE && N == 512 ? 1 : 0;
   static constexpr int QLAY = kRowSwizzle && QFUSE && N == 512 ? 1 : 0;
+  // the forward transforms' last pass and the split of the packed spectra in
+  // registers (colfft.cuh:row_last_fwd512): one row per 64 threads
+  static constexpr bool RSHL = kRowShflLast && RFUSE && N == 512 && RTM * 64 == kRowThreads;
+  static constexpr bool QSHL = kRowShflLast && QFUSE && N == 512 && RRT * 64 == QTHREADS;
   static constexpr int CIMINB = imin(CB == 8 ? kColInvMinB : 2, smem_ctas((N + 3 * FSC) * CB));
   static constexpr int CQMINB = imin(CB == 8 ? kColQwMinB : 2, smem_ctas((N + 2 * FSC) * CB));
 };
@@ -306,7 +315,11 @@ __device__ __forceinline__ void row_main_item(const Geom& g, const StepParams& s
         for (int r = 0; r < R; ++r) bA[(f * RT + rr) * LD + lay_idx<LAY>(j * R + r)] = w[r];
       }
       __syncthreads();
-      ip_passes<T, N, true, 4 * RT, NT, LD, R0, LAY, MID>(bA, tw);
+      if constexpr (Tiles<T, N>::RSHL) {
+        ip_passes_but_last<T, N, true, 4 * RT, NT, LD, R0, LAY, MID>(bA, tw);
+      } else {
+        ip_passes<T, N, true, 4 * RT, NT, LD, R0, LAY, MID>(bA, tw);
+      }
     } else {
       ip_passes<T, N, false, 3 * RT, NT, LD, R0, LAY>(bA, tw);
     }
@@ -339,6 +352,34 @@ __device__ __forceinline__ void row_main_item(const Geom& g, const StepParams& s
   }
   const T adv = sp.adv ? (T)1 : (T)0;
   const T half = sp.refr ? (T)0.5 : (T)0;
+  if constexpr (Tiles<T, N>::RSHL) {
+    // last forward pass per task (row, j), spectra split by shuffles; the
+    // (zeta br, zeta bi) transform first: its halves enter planes 2 and 4
+    const RowLastTask tk = row_last_task(tid);
+    const int rr = tid / 64, y = y0 + rr;
+    constexpr int LL2 = MID ? 1 : LAY;
+    cplx<T> w[8], b[3], zr[3], zi[3];
+    row_last_fwd512<T, LL2>(bA + (3 * RT + rr) * LD, tw, tk, w, b);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) split_pair<T>(w[q], b[q], zr[q], zi[q]);
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+      row_last_fwd512<T, LL2>(bA + (f * RT + rr) * LD, tw, tk, w, b);
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const int k = tk.j + 64 * q;
+        if (k > K) continue;
+        cplx<T> X, Y;
+        split_pair<T>(w[q], b[q], X, Y);
+        const cplx<T> G = cscale(cmul_i(X), (T)k * adv);
+        // G = i kx F(uX) (+- refraction), H = F(vX), as below
+        S[scr_off(zb, 2 * f, y, N, g.KXP) + k] = f == 0 ? G : (f == 1 ? csub(G, cscale(zi[q], half))
+                                                                        : cadd(G, cscale(zr[q], half)));
+        S[scr_off(zb, 2 * f + 1, y, N, g.KXP) + k] = cscale(Y, adv);
+      }
+    }
+    return;
+  }
   for (int e = tid; e < RT * (K + 1); e += NT) {
     const int k = e % (K + 1), rr = e / (K + 1);
     const int y = y0 + rr;
@@ -739,7 +780,11 @@ __device__ __forceinline__ void row_qw_item(const Geom& g, cplx<T>* __restrict__
 #pragma unroll
       for (int r = 0; r < R; ++r) bA[rr * LD + lay_idx<LAY>(j * R + r)] = w[r];
       __syncthreads();
-      ip_passes<T, N, true, RT, NT, LD, R0, LAY>(bA, tw);
+      if constexpr (Tiles<T, N>::QSHL) {
+        ip_passes_but_last<T, N, true, RT, NT, LD, R0, LAY>(bA, tw);
+      } else {
+        ip_passes<T, N, true, RT, NT, LD, R0, LAY>(bA, tw);
+      }
     } else {
       ip_passes<T, N, false, 3 * RT, NT, LD, radix_of(N), LAY>(bA, tw);
     }
@@ -767,6 +812,24 @@ __device__ __forceinline__ void row_qw_item(const Geom& g, cplx<T>* __restrict__
     }
     __syncthreads();
     fft_ip<T, N, true, RT, NT, LD>(bA, tw);
+  }
+  if constexpr (Tiles<T, N>::QSHL) {
+    // last forward pass per task (row, j), spectrum split by shuffles
+    const RowLastTask tk = row_last_task(tid);
+    const int rr = tid / 64, y = y0 + rr;
+    cplx<T> w[8], b[3];
+    row_last_fwd512<T, LAY>(bA + rr * LD, tw, tk, w, b);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const int k = tk.j + 64 * q;
+      if (k > K) continue;
+      cplx<T> P1, P2;
+      split_pair<T>(w[q], b[q], P1, P2);
+      const T qk = (T)0.25 * (T)(k * k);
+      S[scr_off(zb, 0, y, N, g.KXP) + k] = csub(P1, cscale(P2, qk));
+      S[scr_off(zb, 1, y, N, g.KXP) + k] = P2;
+    }
+    return;
   }
   for (int e = tid; e < RT * (K + 1); e += NT) {
     const int k = e % (K + 1), rr = e / (K + 1);
@@ -835,14 +898,16 @@ k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg, int n
 template <typename T, int N>
 __global__ void __launch_bounds__(kThreadsB, Tiles<T, N>::CQMINB)
 k_col_qw(Geom g, StepParams sp, int zbase, const cplx<T>* __restrict__ q, cplx<T>* __restrict__ qstar,
-         const cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg) {
+         const cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg, int* __restrict__ nflag) {
   constexpr int CT = Tiles<T, N>::CT, NT = kThreadsB;
   constexpr int R0 = radix_of(N), NB0 = N / R0, NSL = LastNS<N>::value, RL = N / NSL;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* sm = tw + N;                 // [2][FS]
+  __shared__ int s_bad;   // a non-finite q* in this tile (the state has blown up)
   const int zb = blockIdx.y, z = zbase + zb;
   const int kx0 = blockIdx.x * CT;
+  if (threadIdx.x == 0) s_bad = 0;
   load_tw<T, N>(tw, twg, NT);
   __syncthreads();
   const T inv_n2 = (T)1 / ((T)N * (T)N);
@@ -872,11 +937,14 @@ k_col_qw(Geom g, StepParams sp, int zbase, const cplx<T>* __restrict__ q, cplx<T
         const cplx<T> R = csub(v[0][r], cscale(v[1][r], (T)0.25 * (T)ky * (T)ky));
         const cplx<T> qw = cscale(cscale(R, inv_n2), s);
         out = csub(q[m], qw);       // q* = q - q^w (main_waqg.f90:430-439)
+        if (!isfinite(out.x) || !isfinite(out.y)) s_bad = 1;
       }
       qstar[m] = out;
     }
   };
   col_fft<T, N, true, 2, CT, NT>(sm, tw, pro, epi);
+  __syncthreads();
+  if (threadIdx.x == 0 && s_bad) raise_wait_flag(nflag);
 }
 
 // q* = q where the feedback is off (no_feedback == 1)
@@ -1096,6 +1164,22 @@ constexpr bool kSolveStore = true;
 constexpr bool kSolvePerColumn = true;  // mixed solves read per-column factor copies (k_expand_fac)
 constexpr int kSegSt = 8;          // k_solve_st: levels per register segment of the sweeps
 constexpr int kSolveStBlocks = 128;  // k_solve_st: register target of 128/TC CTAs of 6*TC threads per SM
+// The A solves (B^{n+1} -> A, 4 of the 6 recurrences per column) depend only
+// on k_col_update's B^{n+1}: with kSolveOverlap they run on a second,
+// lower-priority stream beside k_row_qw / k_col_qw / the psi solve, and the
+// persistent k_row_qw takes kQwReserve fewer CTAs per SM than fit, leaving
+// registers for solve CTAs.  Off by default: at 512^2 x 256 the step is
+// 0.07-0.10 ms slower with it (the solves stream ~2 GB per step through DRAM
+// - q*, B, the per-column factors, their forward values - and contend with
+// the q^w kernels for bandwidth rather than only filling the idle FP64 pipe).
+#ifndef QG_SOLVE_OVERLAP
+#define QG_SOLVE_OVERLAP 0
+#endif
+#ifndef QG_QW_RESERVE
+#define QG_QW_RESERVE 1
+#endif
+constexpr bool kSolveOverlap = QG_SOLVE_OVERLAP != 0;
+constexpr int kQwReserve = QG_QW_RESERVE;
 // Per-column copies of the mixed path's elimination factors, expanded from
 // the per-kh^2 tables so that the consecutive columns of a warp read
 // consecutive words (the per-kh^2 rows of neighbouring columns are scattered:
@@ -1136,13 +1220,15 @@ k_solve_st(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
            int do_psi, int do_A, double* __restrict__ vbuf, const double* __restrict__ pc) {
   constexpr bool EXACT = sizeof(T) == 8;
   constexpr bool USEPC = PC && !EXACT;
-  constexpr int S = kSegSt, NTH = 6 * TC;
+  constexpr int S = kSegSt;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n3 = g.n3;
   double* du_s = reinterpret_cast<double*>(smem_raw);
-  for (int i = threadIdx.x; i < n3; i += NTH) du_s[i] = du[i];
+  for (int i = threadIdx.x; i < n3; i += blockDim.x) du_s[i] = du[i];
   __syncthreads();
-  const int chain = threadIdx.x / TC, c = threadIdx.x % TC;
+  // the CTA runs the recurrences asked for: 2*TC threads per right-hand
+  // side, psi's first (chains 0, 1: psi; 2, 3: AR; 4, 5: AI)
+  const int chain = (do_psi ? 0 : 2) + threadIdx.x / TC, c = threadIdx.x % TC;
   const int rhs_id = chain >> 1, part = chain & 1;
   if (rhs_id == 0 ? !do_psi : !do_A) return;
   const long long m = (long long)blockIdx.x * TC + c;
@@ -1223,10 +1309,14 @@ k_solve_st(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
 // Conversions between the reference layout and the compact layout
 // ===========================================================================
 // dense: double2 [nlev][ikty][iktx]
+// nflag (optional, mapped page-locked word): set to 1 when a retained mode
+// of the input is NaN or infinite (modes with L=0 are discarded unread).
 template <typename T>
-static __global__ void k_dense_to_compact(Geom g, int level0, int nlev, const double2* __restrict__ dense, cplx<T>* __restrict__ f) {
+static __global__ void k_dense_to_compact(Geom g, int level0, int nlev, const double2* __restrict__ dense,
+                                          cplx<T>* __restrict__ f, int* __restrict__ nflag = nullptr) {
   const int iktx = g.n / 2 + 1;
   const long long tot = (long long)nlev * g.plane;
+  bool bad = false;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
     const int l = (int)(i / g.plane);
     const long long m = i - (long long)l * g.plane;
@@ -1236,10 +1326,12 @@ static __global__ void k_dense_to_compact(Geom g, int level0, int nlev, const do
     if (g.mask(kx, ky)) {
       const int iky = ky >= 0 ? ky : g.n + ky;
       const double2 d = dense[((long long)l * g.n + iky) * iktx + kx];
+      bad |= !isfinite(d.x) || !isfinite(d.y);
       v = mk<T>((T)d.x, (T)d.y);
     }
     f[(long long)(level0 + l) * g.plane + m] = v;
   }
+  if (nflag && __syncthreads_or(bad) && threadIdx.x == 0) raise_wait_flag(nflag);
 }
 
 // mode: 0 plain copy, 1 vertical difference (A_z, elliptic.f90:437-450)

@@ -30,7 +30,7 @@ EXPORTS = (
     "qg_omega_eqn_rhs", "qg_omega_equation", "qg_omega", "qg_ensemble_set_lanes",
     "qg_selftest_conversions", "qg_selftest_wait",
 )
-KERNEL_CLASSES = ("dissipation", "col_inv", "row_main", "col_update", "row_qw", "col_qw", "solve")
+KERNEL_CLASSES = ("dissipation", "col_inv", "row_main", "col_update", "row_qw", "col_qw", "solve", "solve_A")
 
 
 class QgConfig(C.Structure):

@@ -203,6 +203,16 @@ def make_initial_condition(rc: RunConfig) -> InitialCondition:
     return InitialCondition(psi=psi.astype(np.complex128), BR=BR, BI=BI, delt=float(delt), umax=umax)
 
 
+def la_from_b(n: int, Bu: float, Bk: np.ndarray, Ak: np.ndarray) -> np.ndarray:
+    """YBJ+ wave field LA = B + kh^2 A / (4 Bu) on the retained modes, zero
+    elsewhere (diagnostics.f90:1698-1706), for arrays in the reference
+    layout [nz][n][n/2+1]."""
+    kxa, kya = wavenumbers(n)
+    KX, KY = np.meshgrid(kxa, kya)
+    kh2 = (KX * KX + KY * KY).astype(np.float64)
+    return np.where(dealias_mask(n)[None], Bk + ((0.25 * kh2)[None] * Ak) / Bu, 0)
+
+
 def first_baroclinic_mode(rc: RunConfig) -> np.ndarray:
     """First baroclinic eigenvector of the discrete vertical operator of
     psi_solver (elliptic.f90:177-189 without the kh^2 term, Neumann ends),

@@ -1,8 +1,10 @@
 """CUDA path vs the FP64 oracle, through the C-ABI (libqgybj.so).
 
 Tolerances (relative L2 per field):
-  FP64 path: 1e-12 (1e-11 for the exponential-stratification inversions,
-             whose condition number is ~1e5 larger);
+  FP64 path: 1e-12 (1e-11 for single exponential-stratification inversions,
+             whose condition number is ~1e5 larger; full-size runs in
+             test_gpu_fullsize.py state their bar from the oracle's own
+             FP64 roundoff floor);
   mixed path (FP32 transforms/update, FP64 solves): 1e-5 after 100 steps,
              2e-6 for single routine calls.
 """
@@ -178,38 +180,7 @@ def test_batching_and_graphs_are_bitwise_invariant():
             assert np.array_equal(a, b)
 
 
-# --- full sizes -----------------------------------------------------------------
-def test_c1_fp64_full_size_two_steps():
-    rc = CONFIGS["c1"]
-    orc.set_workers(16)
-    model, st, sim = pair(rc, "fp64")
-    sim.steps_async(2, True)
-    sim.synchronize()
-    st = model.run(st, 2, first=True)
-    compare(sim, st, 1e-11)
-    sim.close()
-    orc.set_workers(1)
-
-
-def test_c2_mixed_full_size_vs_fp64_gpu_100_steps():
-    """512^2 x 256: the mixed path after 100 steps against the FP64 GPU path
-    (itself checked against the oracle above), per-field relative L2 <= 1e-5."""
-    rc = CONFIGS["c2"]
-    ic = make_initial_condition(rc)
-    params = model_parameters(rc, ic.delt)
-    res = {}
-    for prec in ("fp64", "mixed"):
-        sim = Simulation(params, prec)
-        sim.set_state("psi", ic.psi); sim.set_state("BR", ic.BR); sim.set_state("BI", ic.BI)
-        sim.init_state(True, True)
-        sim.steps_async(rc.steps, True)
-        sim.synchronize()
-        res[prec] = {f: sim.get_state(f) for f in ("q", "psi", "BR", "BI", "AR", "AI")}
-        sim.close()
-    errs = {f: rel_l2(res["mixed"][f], res["fp64"][f]) for f in res["fp64"]}
-    assert all(e <= 1e-5 for e in errs.values()), errs
-    for f, a in res["mixed"].items():
-        assert np.isfinite(a).all()
+# --- full sizes: tests/test_gpu_fullsize.py ----------------------------------------
 
 
 # --- error statuses ---------------------------------------------------------------
