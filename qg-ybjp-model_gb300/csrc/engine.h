@@ -49,6 +49,9 @@ struct EngineBase {
   // levels per phase-A batch: current value and re-selection (drops graphs)
   virtual int batch_levels() const = 0;
   virtual int set_batch_levels(int zb) = 0;
+  // phase-A batches in flight at once: current value and re-selection (drops graphs)
+  virtual int batch_lanes() const = 0;
+  virtual int set_batch_lanes(int lanes) = 0;
   // columns per CTA of the column solves (16, 32, 64): current value and re-selection
   virtual int solve_columns() const = 0;
   virtual int set_solve_columns(int tc) = 0;

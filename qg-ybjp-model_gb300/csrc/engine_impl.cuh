@@ -125,7 +125,14 @@ class Engine : public EngineBase {
     zb = std::min(zb, g.n3);
     const int nb = (g.n3 + zb - 1) / zb;
     Zb = (g.n3 + nb - 1) / nb;
-    QG_CK(cudaMalloc(&S, (size_t)Zb * per_level));
+    lanes = std::max(1, std::min(kBatchLanes, nb));
+    QG_CK(cudaMalloc(&S, (size_t)lanes * Zb * per_level));
+    s_levels = lanes * Zb;
+    for (int i = 1; i < kMaxLanes; ++i) {
+      QG_CK(cudaStreamCreateWithPriority(&lst[i], cudaStreamNonBlocking, prio_high));
+      QG_CK(cudaEventCreateWithFlags(&lev[i], cudaEventDisableTiming));
+    }
+    QG_CK(cudaEventCreateWithFlags(&ev_start, cudaEventDisableTiming));
     sp.delt = cfg.delt; sp.gamma = cfg.gamma; sp.Bu = cfg.Bu; sp.Ro = cfg.Ro; sp.W2F = cfg.W2F;
     sp.dz = cfg.dz; sp.nuz = cfg.nuz; sp.cdisp = 0.5 / (cfg.Bu * cfg.Ro);
     sp.adv = cfg.linear ? 0 : 1;
@@ -176,13 +183,24 @@ class Engine : public EngineBase {
     zb = std::max(1, std::min(zb, g.n3));
     const int nb = (g.n3 + zb - 1) / zb;
     const int nz = (g.n3 + nb - 1) / nb;
-    if (nz > Zb) {
+    const int nl = std::max(1, std::min(want_lanes, nb));
+    if (nl * nz > s_levels) {
       cudaFree(S);
       S = nullptr;
-      QG_CK(cudaMalloc(&S, (size_t)nz * per_level));
+      QG_CK(cudaMalloc(&S, (size_t)nl * nz * per_level));
+      s_levels = nl * nz;
     }
     Zb = nz;
+    lanes = nl;
     return QG_OK;
+  }
+
+  // phase-A batches in flight at once (each on its own stream and scratch)
+  int batch_lanes() const override { return lanes; }
+  int set_batch_lanes(int nl) override {
+    if (nl < 1 || nl > kMaxLanes) { err = "batch lanes must be in [1, 8]"; return QG_ERR_ARG; }
+    want_lanes = nl;
+    return set_batch_levels(Zb);
   }
 
   int solve_columns() const override { return solve_tc; }
@@ -583,9 +601,17 @@ class Engine : public EngineBase {
   int nsm = 1, occ_rm = 1, occ_rq = 1;   // SMs; resident CTAs per SM of the persistent row kernels
   double *om_t1 = nullptr, *om_du = nullptr, *om_dl = nullptr, *om_a = nullptr, *om_scr = nullptr;
   C* sig[2] = {};     // regular YBJ: per-level sigma terms
-  C* S = nullptr;
+  C* S = nullptr;              // [lanes][Zb][kNScr][n][KXP] scratch planes
+  int s_levels = 0;            // levels of scratch allocated
   double2* psi64 = nullptr;
   int Zb = 1;
+  // phase-A batches run on `lanes` streams (lane 0: st), batch b on lane
+  // b % lanes with its own scratch slot; they join st before the solves
+  static constexpr int kMaxLanes = 8;
+  int lanes = 1, want_lanes = kBatchLanes;
+  cudaStream_t lst[kMaxLanes] = {};
+  cudaEvent_t lev[kMaxLanes] = {};
+  cudaEvent_t ev_start = nullptr;
   bool need_qw = true;
   void* stage = nullptr; size_t stage_bytes = 0;
   // dense drop-in buffers
@@ -613,6 +639,11 @@ class Engine : public EngineBase {
     wflag = nullptr;
     nflag = nullptr;
     iflag = nullptr;
+    for (int i = 1; i < kMaxLanes; ++i) {
+      if (lst[i]) { cudaStreamSynchronize(lst[i]); cudaStreamDestroy(lst[i]); lst[i] = nullptr; }
+      if (lev[i]) { cudaEventDestroy(lev[i]); lev[i] = nullptr; }
+    }
+    if (ev_start) { cudaEventDestroy(ev_start); ev_start = nullptr; }
     if (st2) cudaStreamSynchronize(st2);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
@@ -760,58 +791,72 @@ class Engine : public EngineBase {
     const int do_A = (cfg.passive_scalar || !cfg.ybj_plus) ? 0 : 1;
     // A solves beside the q^w kernels (a second stream; serialised while
     // profiling so that every launch is timed alone)
-    const bool split = kSolveOverlap && need_qw && do_psi && do_A && kSolveStore && vbuf;
+    const int nbat = (g.n3 + Zb - 1) / Zb;
+    const int L = prof_on ? 1 : std::min(lanes, nbat);   // serialised while profiling
+    const bool split = kSolveOverlap && need_qw && do_psi && do_A && kSolveStore && vbuf && L == 1;
     const bool overlap = split && !prof_on;
-    for (int z0 = 0; z0 < g.n3; z0 += Zb) {
+    if (L > 1) {
+      QG_CK(cudaEventRecord(ev_start, st));
+      for (int i = 1; i < L; ++i) QG_CK(cudaStreamWaitEvent(lst[i], ev_start, 0));
+    }
+    const size_t slot = (size_t)Zb * kNScr * g.n * g.KXP;
+    for (int z0 = 0, b = 0; z0 < g.n3; z0 += Zb, ++b) {
       const int zc = std::min(Zb, g.n3 - z0);
       const bool last = z0 + Zb >= g.n3;
+      const int lane = b % L;
+      cudaStream_t bs = lane == 0 ? st : lst[lane];
+      C* Sb = S + lane * slot;
       QG_SWITCH_N(g.n, {
         const dim3 gc(g.KXP / Tiles<T, NN>::CT, zc), gr(g.n / Tiles<T, NN>::RRT, zc),
             grm(g.n / Tiles<T, NN>::RTM, zc);
-        if (int rc0 = pbeg(QG_K_COL_INV)) return rc0;
-        k_col_inv<T, NN><<<gc, kColThreads, sm_ci<NN>(3), st>>>(g, z0, F[F_PSI], F[F_Q], F[F_BR], F[F_BI], S, tw);
+        if (int rc0 = pbeg(QG_K_COL_INV, bs)) return rc0;
+        k_col_inv<T, NN><<<gc, kColThreads, sm_ci<NN>(3), bs>>>(g, z0, F[F_PSI], F[F_Q], F[F_BR], F[F_BI], Sb, tw);
         QG_LAUNCHED();
-        if (int rc0 = pend()) return rc0;
-        if (int rc0 = pbeg(QG_K_ROW_MAIN)) return rc0;
+        if (int rc0 = pend(bs)) return rc0;
+        if (int rc0 = pbeg(QG_K_ROW_MAIN, bs)) return rc0;
         if constexpr (Tiles<T, NN>::RPRE) {
           const int items = zc * (NN / Tiles<T, NN>::RTM);
-          k_row_main<T, NN><<<std::min(items, nsm * occ_rm), kRowThreads, sm_rm<NN>(g.KXP), st>>>(g, s, S, tw, items,
+          k_row_main<T, NN><<<std::min(items, std::max(1, nsm * occ_rm / L)), kRowThreads, sm_rm<NN>(g.KXP), bs>>>(g, s, Sb, tw, items,
                                                                                                  wflag);
         } else {
-          k_row_main<T, NN><<<grm, kRowThreads, sm_rm<NN>(g.KXP), st>>>(g, s, S, tw, 0, wflag);
+          k_row_main<T, NN><<<grm, kRowThreads, sm_rm<NN>(g.KXP), bs>>>(g, s, Sb, tw, 0, wflag);
         }
         QG_LAUNCHED();
-        if (int rc0 = pend()) return rc0;
-        if (int rc0 = pbeg(QG_K_COL_UPDATE)) return rc0;
-        k_col_update<T, NN><<<gc, kColThreads, UpdLay<T, NN>::bytes(), st>>>(g, s, z0, sptr, e1, e2, e1w, e2w, S, tw,
+        if (int rc0 = pend(bs)) return rc0;
+        if (int rc0 = pbeg(QG_K_COL_UPDATE, bs)) return rc0;
+        k_col_update<T, NN><<<gc, kColThreads, UpdLay<T, NN>::bytes(), bs>>>(g, s, z0, sptr, e1, e2, e1w, e2w, Sb, tw,
                                                                 need_qw ? 1 : 0);
         QG_LAUNCHED();
-        if (int rc0 = pend()) return rc0;
+        if (int rc0 = pend(bs)) return rc0;
         if (overlap && last) {
           // B^{n+1} of every level is written: fork the A solves
-          QG_CK(cudaEventRecord(ev_fork, st));
+          QG_CK(cudaEventRecord(ev_fork, bs));
           QG_CK(cudaStreamWaitEvent(st2, ev_fork, 0));
           if (int rc0 = solve_generic(nullptr, F[F_BR], F[F_BI], nullptr, F[F_AR], F[F_AI], 0, 1, st2)) return rc0;
           QG_CK(cudaEventRecord(ev_join, st2));
         }
         if (need_qw) {
-          if (int rc0 = pbeg(QG_K_ROW_QW)) return rc0;
+          if (int rc0 = pbeg(QG_K_ROW_QW, bs)) return rc0;
           if constexpr (Tiles<T, NN>::QPRE) {
             const int items = zc * (NN / Tiles<T, NN>::RRT);
             const int per_sm = (split && last) ? std::max(1, occ_rq - kQwReserve) : occ_rq;
-            k_row_qw<T, NN><<<std::min(items, nsm * per_sm), Tiles<T, NN>::QTHREADS, sm_rq<NN>(g.KXP), st>>>(
-                g, S, tw, items, wflag);
+            k_row_qw<T, NN><<<std::min(items, std::max(1, nsm * per_sm / L)), Tiles<T, NN>::QTHREADS, sm_rq<NN>(g.KXP), bs>>>(
+                g, Sb, tw, items, wflag);
           } else {
-            k_row_qw<T, NN><<<gr, Tiles<T, NN>::QTHREADS, sm_rq<NN>(g.KXP), st>>>(g, S, tw, 0, wflag);
+            k_row_qw<T, NN><<<gr, Tiles<T, NN>::QTHREADS, sm_rq<NN>(g.KXP), bs>>>(g, Sb, tw, 0, wflag);
           }
           QG_LAUNCHED();
-          if (int rc0 = pend()) return rc0;
-          if (int rc0 = pbeg(QG_K_COL_QW)) return rc0;
-          k_col_qw<T, NN><<<gc, kThreadsB, sm_ci<NN>(2), st>>>(g, s, z0, F[F_Q], F[F_QSTAR], S, tw, nflag);
+          if (int rc0 = pend(bs)) return rc0;
+          if (int rc0 = pbeg(QG_K_COL_QW, bs)) return rc0;
+          k_col_qw<T, NN><<<gc, kThreadsB, sm_ci<NN>(2), bs>>>(g, s, z0, F[F_Q], F[F_QSTAR], Sb, tw, nflag);
           QG_LAUNCHED();
-          if (int rc0 = pend()) return rc0;
+          if (int rc0 = pend(bs)) return rc0;
         }
       });
+    }
+    for (int i = 1; i < L; ++i) {
+      QG_CK(cudaEventRecord(lev[i], lst[i]));
+      QG_CK(cudaStreamWaitEvent(st, lev[i], 0));
     }
     if (int rc0 = pbeg(QG_K_SOLVE)) return rc0;
     int rc = launch_solve(need_qw ? F[F_QSTAR] : F[F_Q], do_psi, split ? 0 : do_A);

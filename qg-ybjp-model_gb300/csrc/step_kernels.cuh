@@ -48,8 +48,21 @@ constexpr int kRowThreads = 256;   // threads of k_row_main, k_row_qw
 constexpr int kRowRT = 0;          // rows per CTA of k_row_main, k_row_qw (0: Tiles RT)
 constexpr int kRowQwThreads = 128; // k_row_qw: half the threads of k_row_main, twice the CTAs
 constexpr int kRowQwMinB = 5;
-constexpr int kColInvMinB = 2;     // k_col_inv
-constexpr int kColQwMinB = 4;      // k_col_qw
+#ifndef QG_COLINV_NF2
+#define QG_COLINV_NF2 1
+#endif
+// k_col_inv (FP32): the six transforms as three passes of two instead of two
+// of three (80 registers instead of 128: 3 CTAs per SM; 0.536 -> 0.496 ms at
+// 512^2 x 256)
+constexpr bool kColInvNF2 = QG_COLINV_NF2 != 0;
+#ifndef QG_COLINV_MINB
+#define QG_COLINV_MINB 3
+#endif
+constexpr int kColInvMinB = QG_COLINV_MINB;     // k_col_inv
+#ifndef QG_COLQW_MINB
+#define QG_COLQW_MINB 4
+#endif
+constexpr int kColQwMinB = QG_COLQW_MINB;      // k_col_qw
 constexpr bool kRowPass0 = true;   // row kernels: first inverse pass fed from registers
 constexpr bool kRowFuse = true;    // k_row_main: inverse last pass, products, forward first pass in registers
 constexpr int kRowMainMinB = 2;    // k_row_main CTAs per SM when fused
@@ -63,10 +76,16 @@ constexpr bool kRowMainMidSwzInv = false;  // the same for its inverse transform
 #endif
 // fused row kernels (N = 512): last forward pass and spectrum split in registers (warp shuffles)
 constexpr bool kRowShflLast = QG_ROW_SHFL_LAST != 0;
-constexpr bool kUpdTablesSmem = true;   // k_col_update (FP32 lean): IF tables staged in shared memory
+#ifndef QG_UPD_TABLES_SMEM
+#define QG_UPD_TABLES_SMEM 1
+#endif
+constexpr bool kUpdTablesSmem = QG_UPD_TABLES_SMEM != 0;   // k_col_update (FP32 lean): IF tables staged in shared memory
 constexpr bool kUpdLean = true;    // k_col_update (FP32): smaller shared footprint ...
 constexpr bool kUpdStage16 = true; // k_col_update (FP32): state staged by 16-byte copies
-constexpr int kUpdMinB = 2;        // ... for this many CTAs per SM
+#ifndef QG_UPD_MINB
+#define QG_UPD_MINB 2
+#endif
+constexpr int kUpdMinB = QG_UPD_MINB;        // ... for this many CTAs per SM (3, with the tables read from global memory, measured slower)
 __host__ __device__ constexpr int smem_ctas(int bytes) {
   return 233472 / (bytes + 1024) >= 8 ? 8 : (233472 / (bytes + 1024) >= 1 ? 233472 / (bytes + 1024) : 1);
 }
@@ -214,9 +233,54 @@ k_col_inv(Geom g, int zbase, const cplx<T>* __restrict__ psi, const cplx<T>* __r
         for (int r = 0; r < RL; ++r) S[scr_off(zb, f0 + f, j + r * NSL, N, g.KXP) + kx0 + c] = v[f][r];
     };
   };
-  col_fft<T, N, false, 3, CT, NT>(sm, tw, pro_psi, epi(0));
-  __syncthreads();
-  col_fft<T, N, false, 3, CT, NT>(sm, tw, pro_raw, epi(3));
+  if constexpr (kColInvNF2 && sizeof(T) == 4) {
+    // three passes of two transforms: (u, v), (zeta, q), (BR, BI)
+    auto pro2 = [&](int which) {
+      return [&, which](int c, int j, cplx<T> (&v)[2][R0]) {
+        const int kx = kx0 + c;
+#pragma unroll
+        for (int r = 0; r < R0; ++r) {
+          int row; bool cj;
+          col_src(g, kx, j + r * NB0, row, cj);
+          const long long m = zoff + (long long)row * g.KXP + kx;
+          const T ky = row >= 0 ? (T)g.ky_of_row(row) : (T)0;
+          const T fkx = (T)kx;
+          cplx<T> a, b;
+          if (which == 0) {
+            const cplx<T> sv = row >= 0 ? psi[m] : mk<T>(0, 0);
+            a = cscale(cmul_mi(sv), ky);
+            b = cscale(cmul_i(sv), fkx);
+          } else if (which == 1) {
+            const cplx<T> sv = row >= 0 ? psi[m] : mk<T>(0, 0);
+            a = cscale(sv, -(fkx * fkx + ky * ky));
+            b = row >= 0 ? q[m] : mk<T>(0, 0);
+          } else {
+            a = row >= 0 ? BR[m] : mk<T>(0, 0);
+            b = row >= 0 ? BI[m] : mk<T>(0, 0);
+          }
+          if (cj) { a = cconj(a); b = cconj(b); }
+          v[0][r] = a; v[1][r] = b;
+        }
+      };
+    };
+    auto epi2 = [&](int f0) {
+      return [&, f0](int c, int j, cplx<T> (&v)[2][RL]) {
+#pragma unroll
+        for (int f = 0; f < 2; ++f)
+#pragma unroll
+          for (int r = 0; r < RL; ++r) S[scr_off(zb, f0 + f, j + r * NSL, N, g.KXP) + kx0 + c] = v[f][r];
+      };
+    };
+    col_fft<T, N, false, 2, CT, NT>(sm, tw, pro2(0), epi2(0));
+    __syncthreads();
+    col_fft<T, N, false, 2, CT, NT>(sm, tw, pro2(1), epi2(2));
+    __syncthreads();
+    col_fft<T, N, false, 2, CT, NT>(sm, tw, pro2(2), epi2(4));
+  } else {
+    col_fft<T, N, false, 3, CT, NT>(sm, tw, pro_psi, epi(0));
+    __syncthreads();
+    col_fft<T, N, false, 3, CT, NT>(sm, tw, pro_raw, epi(3));
+  }
 }
 
 // Hermitian-extended packed spectrum X + iY of two real rows from their
@@ -1179,6 +1243,14 @@ constexpr int kSolveStBlocks = 128;  // k_solve_st: register target of 128/TC CT
 #define QG_QW_RESERVE 1
 #endif
 constexpr bool kSolveOverlap = QG_SOLVE_OVERLAP != 0;
+// Phase-A batches are independent (z-local): with several batches per step,
+// up to kBatchLanes of them run at once on their own streams and scratch
+// slots, so that different kernels of different batches share the GPU and
+// each batch's (kx,y) planes can stay in L2 between its kernels.
+#ifndef QG_BATCH_LANES
+#define QG_BATCH_LANES 1
+#endif
+constexpr int kBatchLanes = QG_BATCH_LANES;
 constexpr int kQwReserve = QG_QW_RESERVE;
 // Per-column copies of the mixed path's elimination factors, expanded from
 // the per-kh^2 tables so that the consecutive columns of a warp read
