@@ -504,7 +504,7 @@ def run_ensemble(args, world, rank, local):
     # concurrent member chains of the step graph: timed choice among a few
     stream0 = torch.cuda.ExternalStream(ens.stream(), device=dev)
     lane_ms = {}
-    for lanes in (1, 2, 4, 8, 16, 32, 64):
+    for lanes in (1, 2, 3, 4):
         ens.set_lanes(lanes)
         ens.step(2, True)
         ens.synchronize()
@@ -535,9 +535,8 @@ def run_ensemble(args, world, rank, local):
     clk = clocks.stop()
     barrier(dist)
     ms = reduce_max(dist, e0.elapsed_time(e1), device=dev)
-    launches = 0
-    for sim in ens.members:
-        launches += sum(c for _, c in sim.profile_step(False).values())
+    prof = ens.profile_step(False)
+    launches = sum(c for _, c in prof.values())
     ens.close()
     # the same members one after another
     seq_ms = 0.0
@@ -568,6 +567,8 @@ def run_ensemble(args, world, rank, local):
                    "solve_columns": {f"{n}x{n}x{n3}": t["solve_columns"] for (n, n3), t in tuned.items()},
                    "precision": "mixed", "parallelism": f"replicas{world}"},
         "lanes": best_lanes, "lanes_ms_per_step": lane_ms,
+        "kernels_ms_per_step": {k: v[0] for k, v in prof.items() if v[1]},
+        "launches_per_step": {k: v[1] for k, v in prof.items() if v[1]},
         "sequential_value": cells * args.steps / (seq_ms / 1e3),
         "ensemble_over_sequential": seq_ms / (ms / world),
         "gpu_launches": launches * args.steps, "clocks": clk, "e2e": None,

@@ -254,29 +254,46 @@ int qg_adjoint_step(qg_handle* h, int euler_first, const double* const* X, const
 /* ---- ensembles and tuning (no counterpart in the reference) -------------- */
 
 /* An ensemble of independent runs, possibly of different sizes and
- * parameters, advanced together: one CUDA graph per step kind forks every
- * member's step onto the member's own stream and joins them, so one graph
- * launch advances all members, which then run concurrently on the GPU.
- * Members are ordinary handles (set/get/init/diagnostics through
- * qg_ensemble_member); all members must use the same device. */
+ * parameters, advanced together.  Members that share the resolution,
+ * precision, physics switches, Bu, dz, gamma, nuz, the Laplacian powers, the
+ * solve block shape and the vertical profiles (a_ell_ut, rho, N^2) - and so
+ * differ only in delt, Ro, W2F and the hyperdiffusion coefficients - are
+ * stacked in z into one run of members*n3 levels: each kernel of the step
+ * then runs once for the whole stack, every member a vertical segment with
+ * its own top and bottom, its own time step, Rossby number, W2F and
+ * integrating factors (YBJ+ only; regular-YBJ members run unstacked).  One
+ * CUDA graph per step kind forks every run (stack or unstacked member) onto
+ * its own stream and joins them, so one graph launch advances all members.
+ * Results are bitwise those of the members run alone.
+ * qg_ensemble_member returns a handle per member: for a stacked member a
+ * view of its levels of the stack, valid for qg_set_state, qg_get_state,
+ * qg_init_state, qg_diagnostics_fp64, qg_dump_psi / qg_dump_la and the
+ * transform drop-ins; calls that act on a whole run (steps, solves, omega,
+ * adjoint, profiling) return QG_ERR_UNSUPPORTED on a view.  Member handles
+ * belong to the ensemble.  All members must use the same device. */
 typedef struct qg_ensemble qg_ensemble;
 int qg_ensemble_create(const qg_config* cfgs, int nmembers, qg_ensemble** out);
 int qg_ensemble_member(qg_ensemble* e, int member, qg_handle** h);
 /* nsteps steps of every member (the first forward Euler when euler_first=1);
  * asynchronous, like qg_steps_async. */
 int qg_ensemble_step(qg_ensemble* e, int nsteps, int euler_first);
-/* Number of member chains the step graph runs concurrently (default 8; 1
- * runs the members one after another).  Members are dealt to the chains
- * largest first, each to the chain with the fewest cells so far.  Drops the
- * captured graphs; results do not depend on it. */
+/* Number of chains of runs the step graph runs concurrently (default 8; 1
+ * runs them one after another).  Runs (stacks and unstacked members) are
+ * dealt to the chains largest first, each to the chain with the fewest cells
+ * so far.  Drops the captured graphs; results do not depend on it. */
 int qg_ensemble_set_lanes(qg_ensemble* e, int lanes);
 /* Waits for the ensemble's stream; QG_ERR_TIMEOUT / QG_ERR_NONFINITE as
- * qg_synchronize for the first member that raised one (named in the error
- * text); every member's status is cleared. */
+ * qg_synchronize for the first run that raised one (named in the error
+ * text; a stack reports for all its members); every status is cleared. */
 int qg_ensemble_synchronize(qg_ensemble* e);
 int qg_ensemble_get_stream(qg_ensemble* e, void** stream);
 int qg_ensemble_destroy(qg_ensemble* e);
 const char* qg_ensemble_last_error(const qg_ensemble* e);
+/* One step of every run of the ensemble (stacks and unstacked members), one
+ * run after another, with CUDA events around each launch, as
+ * qg_profile_step: per kernel class the summed device time and the launch
+ * count.  It advances the state like qg_ensemble_step. */
+int qg_ensemble_profile_step(qg_ensemble* e, int euler_first, double* ms, int* launches, int nclasses);
 
 /* Autotuner: times candidate phase-A batch depths (levels per batch: the L2
  * footprint of the (kx,y) scratch planes and the wave count of the column

@@ -14,6 +14,10 @@
 struct qg_handle {
   qg::EngineBase* eng = nullptr;
   std::string err;
+  // a member of an ensemble stack: levels [z0, z0 + nz) of an engine that the
+  // ensemble owns (state I/O, initialisation and diagnostics of that member)
+  bool view = false;
+  int z0 = 0, nz = 0;
 };
 
 namespace {
@@ -227,10 +231,8 @@ int qg_config_defaults(qg_config* c) {
   return QG_OK;
 }
 
-int qg_create(const qg_config* cfg, qg_handle** out) {
-  if (!cfg || !out) return fail(nullptr, QG_ERR_ARG, "null argument");
-  *out = nullptr;
-  const qg_config& c = *cfg;
+// the checks of qg_create; QG_OK or the status with its text in g_create_err
+static int validate_config(const qg_config& c) {
   if (c.n1 != c.n2) return fail(nullptr, QG_ERR_UNSUPPORTED, "n1 must equal n2");
   if (!qg::supported_n(c.n1)) return fail(nullptr, QG_ERR_UNSUPPORTED, "n1 must be a power of two in [16,1024]");
   if (c.n3 < 2) return fail(nullptr, QG_ERR_ARG, "n3 must be >= 2");
@@ -250,13 +252,14 @@ int qg_create(const qg_config* cfg, qg_handle** out) {
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || c.device < 0 || c.device >= ndev)
     return fail(nullptr, QG_ERR_CUDA, "no CUDA device with that ordinal");
-  qg::HostTables t;
-  std::string err;
-  int rc = build_tables(c, t, err);
-  if (rc) return fail(nullptr, rc, err);
+  return QG_OK;
+}
+
+// a handle whose engine is built from c and the tables t
+static int create_from_tables(const qg_config& c, const qg::HostTables& t, qg_handle** out) {
   qg_handle* h = new qg_handle();
   h->eng = c.precision == QG_PREC_FP64 ? qg::make_engine_fp64() : qg::make_engine_fp32();
-  rc = h->eng->init(c, t);
+  const int rc = h->eng->init(c, t);
   if (rc) {
     g_create_err = h->eng->err;
     delete h->eng;
@@ -267,9 +270,21 @@ int qg_create(const qg_config* cfg, qg_handle** out) {
   return QG_OK;
 }
 
+int qg_create(const qg_config* cfg, qg_handle** out) {
+  if (!cfg || !out) return fail(nullptr, QG_ERR_ARG, "null argument");
+  *out = nullptr;
+  int rc = validate_config(*cfg);
+  if (rc) return rc;
+  qg::HostTables t;
+  std::string err;
+  rc = build_tables(*cfg, t, err);
+  if (rc) return fail(nullptr, rc, err);
+  return create_from_tables(*cfg, t, out);
+}
+
 int qg_destroy(qg_handle* h) {
   if (!h) return QG_ERR_ARG;
-  delete h->eng;
+  if (!h->view) delete h->eng;    // a member view leaves its stack to the ensemble
   delete h;
   return QG_OK;
 }
@@ -291,6 +306,18 @@ const char* qg_last_error(const qg_handle* h) {
 #define QG_ENTRY(h)                       \
   if (!(h) || !(h)->eng) return QG_ERR_ARG; \
   (h)->err.clear();
+// calls that act on a whole run: refused on a member of an ensemble stack
+#define QG_WHOLE(h)                                                                                     \
+  if ((h)->view)                                                                                        \
+    return fail(h, QG_ERR_UNSUPPORTED, "this call acts on a whole run; the handle is a member of an "   \
+                                       "ensemble stack (step and solve it through the ensemble)");
+// level range of a member view: [level0, level0 + nlev) of the member, shifted to the stack
+#define QG_LEVELS(h, level0, nlev)                                                                      \
+  if ((h)->view) {                                                                                      \
+    if ((level0) < 0 || (nlev) <= 0 || (level0) + (nlev) > (h)->nz)                                      \
+      return fail(h, QG_ERR_ARG, "bad level range for this member");                                    \
+    (level0) += (h)->z0;                                                                                \
+  }
 
 static int fwd(qg_handle* h, int rc) {
   if (rc && h->err.empty()) h->err = h->eng->err;
@@ -299,22 +326,27 @@ static int fwd(qg_handle* h, int rc) {
 
 int qg_set_state(qg_handle* h, int field, const double* kvar, int level0, int nlev) {
   QG_ENTRY(h);
+  QG_LEVELS(h, level0, nlev);
   return fwd(h, h->eng->set_state(field, kvar, level0, nlev));
 }
 int qg_get_state(qg_handle* h, int field, double* kvar, int level0, int nlev) {
   QG_ENTRY(h);
+  QG_LEVELS(h, level0, nlev);
   return fwd(h, h->eng->get_state(field, kvar, level0, nlev));
 }
 int qg_init_state(qg_handle* h, int apply_sumB, int q_from_psi) {
   QG_ENTRY(h);
+  if (h->view) return fwd(h, h->eng->init_state_range(h->z0, h->nz, apply_sumB, q_from_psi));
   return fwd(h, h->eng->init_state(apply_sumB, q_from_psi));
 }
 int qg_step(qg_handle* h, int euler_first) {
   QG_ENTRY(h);
+  QG_WHOLE(h);
   return fwd(h, h->eng->step(euler_first));
 }
 int qg_steps_async(qg_handle* h, int nsteps, int euler_first) {
   QG_ENTRY(h);
+  QG_WHOLE(h);
   if (nsteps < 0) return fail(h, QG_ERR_ARG, "nsteps must be >= 0");
   return fwd(h, h->eng->steps_async(nsteps, euler_first));
 }
@@ -324,6 +356,7 @@ int qg_synchronize(qg_handle* h) {
 }
 int qg_selftest_wait(qg_handle* h) {
   QG_ENTRY(h);
+  QG_WHOLE(h);
   return fwd(h, h->eng->selftest_wait());
 }
 int qg_get_stream(qg_handle* h, void** stream) {
@@ -335,16 +368,19 @@ int qg_get_stream(qg_handle* h, void** stream) {
 int qg_diagnostics_fp64(qg_handle* h, qg_energy* out) {
   QG_ENTRY(h);
   if (!out) return fail(h, QG_ERR_ARG, "null output");
+  if (h->view) return fwd(h, h->eng->diagnostics_range(h->z0, h->nz, out));
   return fwd(h, h->eng->diagnostics(out));
 }
 int qg_profile_step(qg_handle* h, int euler_first, double* ms, int* launches, int nclasses) {
   QG_ENTRY(h);
+  QG_WHOLE(h);
   if (!ms || !launches || nclasses <= 0) return fail(h, QG_ERR_ARG, "null output or nclasses <= 0");
   return fwd(h, h->eng->profile_step(euler_first, ms, launches, nclasses));
 }
 int qg_adjoint_run(qg_handle* h, const double* q0, const double* BR0, const double* BI0, int nsteps, int ckpt_every,
                    int objective, double* J, double* gq, double* gR, double* gI) {
   QG_ENTRY(h);
+  QG_WHOLE(h);
   if (!q0 || !BR0 || !BI0 || !J || nsteps < 1 || ckpt_every < 1) return fail(h, QG_ERR_ARG, "qg_adjoint_run: bad arguments");
   if (objective != QG_OBJ_LA_SUBVOLUME) return fail(h, QG_ERR_ARG, "qg_adjoint_run: unknown objective");
   if ((gq || gR || gI) && !(gq && gR && gI)) return fail(h, QG_ERR_ARG, "qg_adjoint_run: pass all three gradients or none");
@@ -353,6 +389,7 @@ int qg_adjoint_run(qg_handle* h, const double* q0, const double* BR0, const doub
 int qg_adjoint_step(qg_handle* h, int euler_first, const double* const* X, const double* const* lX, double* const* Xn,
                     double* const* lXo) {
   QG_ENTRY(h);
+  QG_WHOLE(h);
   if (!X) return fail(h, QG_ERR_ARG, "qg_adjoint_step: null state");
   for (int i = 0; i < 6; ++i) if (!X[i]) return fail(h, QG_ERR_ARG, "qg_adjoint_step: null state field");
   if (lXo && !lX) return fail(h, QG_ERR_ARG, "qg_adjoint_step: lX_out needs lX");
@@ -387,51 +424,85 @@ int qg_compute_qw(qg_handle* h, const double* BRk, const double* BIk, double* qw
 }
 int qg_dump_psi(qg_handle* h, float* out, int level0, int nlev, double U_scale, double L_scale) {
   QG_ENTRY(h);
+  QG_LEVELS(h, level0, nlev);
   if (!out) return fail(h, QG_ERR_ARG, "qg_dump_psi: null pointer");
   return fwd(h, h->eng->dump_real(0, out, nullptr, level0, nlev, U_scale, L_scale));
 }
 int qg_dump_la(qg_handle* h, float* outR, float* outI, int level0, int nlev, double Uw_scale, int la) {
   QG_ENTRY(h);
+  QG_LEVELS(h, level0, nlev);
   if (!outR || !outI) return fail(h, QG_ERR_ARG, "qg_dump_la: null pointer");
   return fwd(h, h->eng->dump_real(la ? 2 : 1, outR, outI, level0, nlev, Uw_scale, 1.0));
 }
 int qg_omega_eqn_rhs(qg_handle* h, const double* psik, double* rhs) {
   QG_ENTRY(h);
+  QG_WHOLE(h);
   if (!psik || !rhs) return fail(h, QG_ERR_ARG, "qg_omega_eqn_rhs: null pointer");
   return fwd(h, h->eng->omega_eqn_rhs(psik, rhs));
 }
 int qg_omega_equation(qg_handle* h, const double* rhs, double* wk) {
   QG_ENTRY(h);
+  QG_WHOLE(h);
   if (!rhs || !wk) return fail(h, QG_ERR_ARG, "qg_omega_equation: null pointer");
   return fwd(h, h->eng->omega_equation(rhs, wk));
 }
 int qg_omega(qg_handle* h, double* wk) {
   QG_ENTRY(h);
+  QG_WHOLE(h);
   if (!wk) return fail(h, QG_ERR_ARG, "qg_omega: null pointer");
   return fwd(h, h->eng->omega_from_state(wk));
 }
 int qg_psi_solver(qg_handle* h, const double* qstar, double* psik) {
   QG_ENTRY(h);
+  QG_WHOLE(h);
   if (!qstar || !psik) return fail(h, QG_ERR_ARG, "null pointer");
   return fwd(h, h->eng->psi_solver(qstar, psik));
 }
 int qg_A_solver_ybj_plus(qg_handle* h, const double* bk, double* ak, double* ck) {
   QG_ENTRY(h);
+  QG_WHOLE(h);
   if (!bk || !ak) return fail(h, QG_ERR_ARG, "null pointer");
   return fwd(h, h->eng->A_solver(bk, ak, ck));
 }
 
 // ---- ensembles ----------------------------------------------------------------
+// Members of one shape, precision, physics switches and vertical operator
+// are stacked in z into one engine (a "stack": each member a segment of
+// n3 levels, with its own time step, Rossby number, W2F and integrating
+// factors), so that every kernel of the step runs once per stack instead of
+// once per member.  The step graph advances the runs: stacks and the
+// members that share their shape with no other.
 struct qg_ensemble {
-  std::vector<qg_handle*> members;
-  std::vector<long long> cells;       // n1*n2*n3 of each member (lane balancing)
+  std::vector<qg_handle*> members;    // per member: its own handle, or a view of its stack
+  std::vector<qg_handle*> runs;       // stacks and unstacked members (owned)
+  std::vector<long long> cells;       // n1*n2*n3 of each run (lane balancing)
   cudaStream_t master = nullptr;
   cudaEvent_t fork = nullptr;
-  std::vector<cudaEvent_t> join;
-  int lanes = 8;                      // concurrent chains of members in the step graph
+  std::vector<cudaEvent_t> join;      // per run
+  int lanes = 8;                      // concurrent chains of runs in the step graph
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
   std::string err;
 };
+
+namespace {
+bool same_doubles(const double* a, const double* b, int n) {
+  if (!a || !b) return a == b;
+  return std::memcmp(a, b, (size_t)n * sizeof(double)) == 0;
+}
+// members that can share one stack: everything but the time step, Ro, W2F
+// and the hyperdiffusion coefficients equal (YBJ+ only: the regular-YBJ A
+// is a vertical integral over one run's column)
+bool stackable(const qg_config& a, const qg_config& b) {
+  return a.n1 == b.n1 && a.n2 == b.n2 && a.n3 == b.n3 && a.precision == b.precision && a.device == b.device &&
+         a.ybj_plus == 1 && b.ybj_plus == 1 && a.fixed_flow == b.fixed_flow && a.no_feedback == b.no_feedback &&
+         a.passive_scalar == b.passive_scalar && a.linear == b.linear && a.no_dispersion == b.no_dispersion &&
+         a.inviscid == b.inviscid && a.dz == b.dz && a.Bu == b.Bu && a.gamma == b.gamma && a.nuz == b.nuz &&
+         a.ilap1 == b.ilap1 && a.ilap2 == b.ilap2 && a.ilap1w == b.ilap1w && a.ilap2w == b.ilap2w &&
+         a.solve_columns == b.solve_columns && same_doubles(a.a_ell_ut, b.a_ell_ut, a.n3) &&
+         same_doubles(a.rho_ut, b.rho_ut, a.n3) && same_doubles(a.rho_st, b.rho_st, a.n3) &&
+         same_doubles(a.r_2ut, b.r_2ut, a.n3);
+}
+}  // namespace
 
 static int ens_fail(qg_ensemble* e, int code, const std::string& msg) {
   if (e) e->err = msg;
@@ -448,7 +519,8 @@ int qg_ensemble_destroy(qg_ensemble* e) {
   if (!e) return QG_ERR_ARG;
   if (e->master) cudaStreamSynchronize(e->master);
   for (auto& g : e->gexec) if (g) cudaGraphExecDestroy(g);
-  for (auto* h : e->members) qg_destroy(h);
+  for (auto* h : e->members) if (h && h->view) qg_destroy(h);
+  for (auto* h : e->runs) qg_destroy(h);
   for (auto ev : e->join) cudaEventDestroy(ev);
   if (e->fork) cudaEventDestroy(e->fork);
   if (e->master) cudaStreamDestroy(e->master);
@@ -462,25 +534,75 @@ int qg_ensemble_create(const qg_config* cfgs, int nmembers, qg_ensemble** out) {
   for (int m = 1; m < nmembers; ++m)
     if (cfgs[m].device != cfgs[0].device) return fail(nullptr, QG_ERR_ARG, "ensemble members must share one device");
   qg_ensemble* e = new qg_ensemble();
+  e->members.assign(nmembers, nullptr);
+  // group the members into stacks (first member of each group as its key)
+  std::vector<std::vector<int>> groups;
   for (int m = 0; m < nmembers; ++m) {
-    qg_config c = cfgs[m];
-    c.use_graphs = 0;          // members are replayed through the ensemble graph
+    size_t k = 0;
+    while (k < groups.size() && !stackable(cfgs[groups[k][0]], cfgs[m])) ++k;
+    if (k == groups.size()) groups.push_back({});
+    groups[k].push_back(m);
+  }
+  for (const auto& grp : groups) {
+    const int m0 = grp[0], M = (int)grp.size();
+    qg_config c = cfgs[m0];
+    c.use_graphs = 0;          // runs are replayed through the ensemble graph
     qg_handle* h = nullptr;
-    int rc = qg_create(&c, &h);
+    int rc = QG_OK;
+    std::string where = "member " + std::to_string(m0) + ": ";
+    if (M == 1) {
+      rc = qg_create(&c, &h);
+    } else {
+      qg::HostTables t;
+      std::string err;
+      for (int k = 0; k < M && !rc; ++k) {
+        const qg_config& cm = cfgs[grp[k]];
+        where = "member " + std::to_string(grp[k]) + ": ";
+        if ((rc = validate_config(cm))) break;
+        qg::HostTables tk;
+        if ((rc = build_tables(cm, tk, err))) { g_create_err = err; break; }
+        if (k == 0) {
+          t = std::move(tk);
+        } else {
+          t.e1.insert(t.e1.end(), tk.e1.begin(), tk.e1.end());
+          t.e2.insert(t.e2.end(), tk.e2.begin(), tk.e2.end());
+          t.e1w.insert(t.e1w.end(), tk.e1w.begin(), tk.e1w.end());
+          t.e2w.insert(t.e2w.end(), tk.e2w.begin(), tk.e2w.end());
+        }
+        t.mpar.insert(t.mpar.end(), {cm.delt, 0.5 / (cm.Bu * cm.Ro), cm.Ro, cm.W2F});
+      }
+      if (!rc) {
+        t.nseg = c.n3;
+        t.members = M;
+        t.n3 = M * c.n3;
+        c.n3 = t.n3;
+        c.levels_per_batch = 0;    // the stack's own batch depth
+        rc = create_from_tables(c, t, &h);
+      }
+    }
     if (rc) {
-      const std::string msg = "member " + std::to_string(m) + ": " + g_create_err;
+      const std::string msg = where + g_create_err;
       qg_ensemble_destroy(e);
       return fail(nullptr, rc, msg);
     }
-    e->members.push_back(h);
-    e->cells.push_back((long long)cfgs[m].n1 * cfgs[m].n2 * cfgs[m].n3);
+    e->runs.push_back(h);
+    e->cells.push_back((long long)c.n1 * c.n2 * c.n3);
+    for (int k = 0; k < M; ++k) {
+      if (M == 1) { e->members[grp[k]] = h; continue; }
+      qg_handle* v = new qg_handle();
+      v->eng = h->eng;
+      v->view = true;
+      v->z0 = k * cfgs[m0].n3;
+      v->nz = cfgs[m0].n3;
+      e->members[grp[k]] = v;
+    }
   }
   if (cudaSetDevice(cfgs[0].device) != cudaSuccess || cudaStreamCreateWithFlags(&e->master, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming) != cudaSuccess) {
     qg_ensemble_destroy(e);
     return fail(nullptr, QG_ERR_CUDA, "qg_ensemble_create: stream/event creation failed");
   }
-  e->join.resize(nmembers);
+  e->join.resize(e->runs.size());
   for (auto& ev : e->join) cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
   *out = e;
   return QG_OK;
@@ -498,7 +620,7 @@ int qg_ensemble_member(qg_ensemble* e, int member, qg_handle** h) {
 // which bounds how many members' scratch planes compete for L2 at once.
 static int ens_capture(qg_ensemble* e, int euler) {
   cudaGraph_t graph = nullptr;
-  const int nm = (int)e->members.size();
+  const int nm = (int)e->runs.size();
   const int L = std::max(1, std::min(e->lanes, nm));
   std::vector<int> order(nm);
   for (int m = 0; m < nm; ++m) order[m] = m;
@@ -512,11 +634,11 @@ static int ens_capture(qg_ensemble* e, int euler) {
     const int m = order[k];
     int lane = 0;
     for (int l = 1; l < L; ++l) if (load[l] < load[lane]) lane = l;
-    cudaStream_t ms = (cudaStream_t)e->members[m]->eng->stream();
+    cudaStream_t ms = (cudaStream_t)e->runs[m]->eng->stream();
     cudaEvent_t dep = tail[lane] < 0 ? e->fork : e->join[tail[lane]];
     if (cudaStreamWaitEvent(ms, dep, 0) != cudaSuccess) { rc = QG_ERR_CUDA; e->err = "ensemble fork failed"; break; }
-    rc = e->members[m]->eng->enqueue(euler);
-    if (rc) { e->err = "member " + std::to_string(m) + ": " + e->members[m]->eng->err; break; }
+    rc = e->runs[m]->eng->enqueue(euler);
+    if (rc) { e->err = "run " + std::to_string(m) + ": " + e->runs[m]->eng->err; break; }
     if (cudaEventRecord(e->join[m], ms) != cudaSuccess) { rc = QG_ERR_CUDA; e->err = "ensemble join failed"; break; }
     tail[lane] = m;
     load[lane] += e->cells[m];
@@ -538,6 +660,7 @@ static int ens_capture(qg_ensemble* e, int euler) {
 int qg_ensemble_step(qg_ensemble* e, int nsteps, int euler_first) {
   if (!e || nsteps < 0) return ens_fail(e, QG_ERR_ARG, "bad arguments");
   e->err.clear();
+  for (auto* r : e->runs) r->eng->release_init_buffers();   // outside any capture
   for (int i = 0; i < nsteps; ++i) {
     const int k = (euler_first && i == 0) ? 1 : 0;
     if (!e->gexec[k]) {
@@ -563,11 +686,13 @@ int qg_ensemble_synchronize(qg_ensemble* e) {
   ENS_CK(cudaStreamSynchronize(e->master));
   // every member's device-raised status (expired wait, non-finite q*)
   int first = QG_OK;
-  for (size_t m = 0; m < e->members.size(); ++m) {
-    const int rc = e->members[m]->eng->check_waits();
+  for (size_t m = 0; m < e->runs.size(); ++m) {
+    const int rc = e->runs[m]->eng->check_waits();
     if (rc && !first) {
       first = rc;
-      e->err = "member " + std::to_string(m) + ": " + e->members[m]->eng->err;
+      const int nm = e->runs[m]->eng->member_count();
+      e->err = (nm > 1 ? "stack of " + std::to_string(nm) + " members (run " + std::to_string(m) + "): "
+                       : "run " + std::to_string(m) + ": ") + e->runs[m]->eng->err;
     }
   }
   return first;
@@ -580,6 +705,21 @@ int qg_ensemble_get_stream(qg_ensemble* e, void** stream) {
 }
 
 const char* qg_ensemble_last_error(const qg_ensemble* e) { return e ? e->err.c_str() : ""; }
+
+int qg_ensemble_profile_step(qg_ensemble* e, int euler_first, double* ms, int* launches, int nclasses) {
+  if (!e || !ms || !launches || nclasses <= 0) return ens_fail(e, QG_ERR_ARG, "qg_ensemble_profile_step: bad arguments");
+  ENS_CK(cudaStreamSynchronize(e->master));
+  for (int i = 0; i < nclasses; ++i) { ms[i] = 0.0; launches[i] = 0; }
+  std::vector<double> rm(nclasses);
+  std::vector<int> rl(nclasses);
+  for (size_t r = 0; r < e->runs.size(); ++r) {
+    e->runs[r]->eng->release_init_buffers();
+    const int rc = e->runs[r]->eng->profile_step(euler_first, rm.data(), rl.data(), nclasses);
+    if (rc) return ens_fail(e, rc, "run " + std::to_string(r) + ": " + e->runs[r]->eng->err);
+    for (int i = 0; i < nclasses; ++i) { ms[i] += rm[i]; launches[i] += rl[i]; }
+  }
+  return QG_OK;
+}
 
 // ---- autotuner -------------------------------------------------------------
 int qg_autotune(const qg_config* cfg, int nsteps, qg_tuning* out) {

@@ -37,6 +37,10 @@ struct Geom {
   int KXP;     // padded row length
   int kmax2;   // L=1 iff kx^2+ky^2 <= kmax2 and not (kx==0 && ky<0)
   long long plane;  // KY*KXP
+  // levels per vertical segment: n3 for one run; for a stack of ensemble
+  // members of one shape, n3 = members * nseg and each member is a segment
+  // with its own top and bottom (no vertical coupling across segments)
+  int nseg;
   __host__ __device__ __forceinline__ int ky_of_row(int r) const { return r <= K ? r : r - KY; }
   __host__ __device__ __forceinline__ int row_of_ky(int ky) const { return ky >= 0 ? ky : ky + KY; }
   __host__ __device__ __forceinline__ bool mask(int kx, int ky) const {
@@ -58,6 +62,10 @@ struct StepParams {
   int use_dq;         // inviscid == 0 && nuz != 0
   int euler;          // forward Euler first step
   int ybj;            // 1: YBJ+ (A from A_solver_ybj_plus); 0: regular YBJ (A from the vertical integral of B)
+  // a stack of ensemble members (Geom::nseg levels each): per member
+  // {delt, 0.5/(Bu Ro), Ro, W2F} at mpar[4 m .. 4 m + 3], and the integrating
+  // factor tables of member m at + m * plane; nullptr for one run
+  const double* mpar;
 };
 
 }  // namespace qg

@@ -10,6 +10,13 @@ namespace qg {
 // Tables built once on the host from the configuration (init.f90:17-264).
 struct HostTables {
   int n, n3, K, KX, KY, KXP, kmax2;
+  // a stack of `members` ensemble members of nseg levels each (n3 = members
+  // * nseg): the per-level tables below (du, cu, cl, r2, factors) describe
+  // one member's levels, the integrating factors are [members][plane] and
+  // mpar holds {delt, 0.5/(Bu Ro), Ro, W2F} per member.  One run: nseg = n3,
+  // members = 1, mpar empty.
+  int nseg = 0, members = 1;
+  std::vector<double> mpar;
   long long plane;
   std::vector<double> e1, e2, e1w, e2w;     // [plane] integrating factors
   std::vector<double> tw;                   // [2n] cos, sin of -2 pi m / n interleaved
@@ -32,6 +39,13 @@ struct EngineBase {
   virtual int set_state(int field, const double* kvar, int level0, int nlev) = 0;
   virtual int get_state(int field, double* kvar, int level0, int nlev) = 0;
   virtual int init_state(int apply_sumB, int q_from_psi) = 0;
+  // the same on the members of levels [z0, z0 + nz) of a stack, and the
+  // release of what the initialisation kept (see Engine::init_state_range)
+  virtual int init_state_range(int z0, int nz, int apply_sumB, int q_from_psi) = 0;
+  virtual void release_init_buffers() = 0;
+  // levels per member and members of this engine (a stack holds several)
+  virtual int levels_per_member() const = 0;
+  virtual int member_count() const = 0;
   virtual int step(int euler) = 0;
   virtual int steps_async(int nsteps, int euler) = 0;
   virtual int synchronize() = 0;
@@ -42,6 +56,7 @@ struct EngineBase {
   virtual int selftest_wait() = 0;
   virtual void* stream() = 0;
   virtual int diagnostics(qg_energy* out) = 0;
+  virtual int diagnostics_range(int z0, int nz, qg_energy* out) = 0;
   virtual int profile_step(int euler, double* ms, int* launches, int nclasses) = 0;
   // enqueue one step on the engine's stream without synchronising or graph
   // replay (used when an ensemble captures its members into one graph)

@@ -49,6 +49,8 @@ class Engine : public EngineBase {
   int init(const qg_config& c, const HostTables& t) override {
     cfg = c;
     g.n = t.n; g.n3 = t.n3; g.K = t.K; g.KX = t.KX; g.KY = t.KY; g.KXP = t.KXP; g.kmax2 = t.kmax2;
+    g.nseg = t.nseg > 0 ? t.nseg : t.n3;
+    members = g.n3 / g.nseg;
     g.plane = t.plane;
     QG_CK(cudaSetDevice(cfg.device));
     // the step's stream at the highest priority, the overlapped A solves on
@@ -70,13 +72,18 @@ class Engine : public EngineBase {
       for (auto& p : sig) { QG_CK(cudaMalloc(&p, fbytes)); QG_CK(cudaMemsetAsync(p, 0, fbytes, st)); }
     }
     // tables
-    std::vector<T> tmp(g.plane);
+    // integrating factors: [members][plane]
+    std::vector<T> tmp((size_t)members * g.plane);
     auto up = [&](T** d, const std::vector<double>& h) -> int {
-      for (long long i = 0; i < g.plane; ++i) tmp[i] = (T)h[i];
-      QG_CK(cudaMalloc(d, g.plane * sizeof(T)));
-      QG_CK(cudaMemcpy(*d, tmp.data(), g.plane * sizeof(T), cudaMemcpyHostToDevice));
+      for (size_t i = 0; i < tmp.size(); ++i) tmp[i] = (T)h[i];
+      QG_CK(cudaMalloc(d, tmp.size() * sizeof(T)));
+      QG_CK(cudaMemcpy(*d, tmp.data(), tmp.size() * sizeof(T), cudaMemcpyHostToDevice));
       return QG_OK;
     };
+    if (members > 1) {
+      QG_CK(cudaMalloc(&mpar, t.mpar.size() * sizeof(double)));
+      QG_CK(cudaMemcpy(mpar, t.mpar.data(), t.mpar.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
     int rc;
     if ((rc = up(&e1, t.e1)) || (rc = up(&e2, t.e2)) || (rc = up(&e1w, t.e1w)) || (rc = up(&e2w, t.e2w))) return rc;
     {
@@ -93,12 +100,12 @@ class Engine : public EngineBase {
     QG_CK(cudaMemcpy(tw, twh.data(), g.n * sizeof(C), cudaMemcpyHostToDevice));
     QG_CK(cudaMalloc(&tab_idx, g.plane * sizeof(int)));
     QG_CK(cudaMemcpy(tab_idx, t.tab_idx.data(), g.plane * sizeof(int), cudaMemcpyHostToDevice));
-    const size_t fb = std::max<size_t>(1, (size_t)t.ndistinct * g.n3) * sizeof(double4);
+    const size_t fb = std::max<size_t>(1, (size_t)t.ndistinct * g.nseg) * sizeof(double4);
     QG_CK(cudaMalloc(&fac_psi, fb));
     QG_CK(cudaMalloc(&fac_A, fb));
     if (t.ndistinct > 0) {
-      QG_CK(cudaMemcpy(fac_psi, t.fac_psi.data(), (size_t)t.ndistinct * g.n3 * sizeof(double4), cudaMemcpyHostToDevice));
-      QG_CK(cudaMemcpy(fac_A, t.fac_A.data(), (size_t)t.ndistinct * g.n3 * sizeof(double4), cudaMemcpyHostToDevice));
+      QG_CK(cudaMemcpy(fac_psi, t.fac_psi.data(), (size_t)t.ndistinct * g.nseg * sizeof(double4), cudaMemcpyHostToDevice));
+      QG_CK(cudaMemcpy(fac_A, t.fac_A.data(), (size_t)t.ndistinct * g.nseg * sizeof(double4), cudaMemcpyHostToDevice));
     }
     auto upd = [&](double** d, const std::vector<double>& h) -> int {
       QG_CK(cudaMalloc(d, h.size() * sizeof(double)));
@@ -141,6 +148,7 @@ class Engine : public EngineBase {
     sp.use_dq = (cfg.inviscid == 0 && cfg.nuz != 0.0) ? 1 : 0;
     sp.euler = 0;
     sp.ybj = cfg.ybj_plus ? 1 : 0;
+    sp.mpar = mpar;
     need_qw = (!cfg.fixed_flow && !cfg.no_feedback);
     int r0 = set_smem_attrs();
     if (r0) return r0;
@@ -158,11 +166,11 @@ class Engine : public EngineBase {
     // mixed path: per-column copies of the solve factors (coalesced reads);
     // without them the solves read the per-kh^2 tables
     if (kSolvePerColumn && sizeof(T) == 4 && vbuf) {
-      if (cudaMalloc(&pcfac, (size_t)6 * g.n3 * g.plane * sizeof(double)) != cudaSuccess) {
+      if (cudaMalloc(&pcfac, (size_t)6 * g.nseg * g.plane * sizeof(double)) != cudaSuccess) {
         pcfac = nullptr;
         (void)cudaGetLastError();
       } else {
-        k_expand_fac<<<grid_for((long long)g.n3 * g.plane), 256, 0, st>>>(g, tab_idx, fac_psi, fac_A, pcfac);
+        k_expand_fac<<<grid_for((long long)g.nseg * g.plane), 256, 0, st>>>(g, tab_idx, fac_psi, fac_A, pcfac);
         QG_LAUNCHED();
       }
     }
@@ -175,6 +183,8 @@ class Engine : public EngineBase {
   int enqueue(int euler) override { return enqueue_step(euler ? 1 : 0); }
 
   int batch_levels() const override { return Zb; }
+  int levels_per_member() const override { return g.nseg; }
+  int member_count() const override { return members; }
 
   int set_batch_levels(int zb) override {
     QG_CK(cudaStreamSynchronize(st));
@@ -307,32 +317,53 @@ class Engine : public EngineBase {
   }
 
   int init_state(int apply_sumB, int q_from_psi) override {
+    int rc = init_state_range(0, g.n3, apply_sumB, q_from_psi);
+    if (rc) return rc;
+    release_init_buffers();
+    return QG_OK;
+  }
+
+  // The initialisation sequence on levels [z0, z0 + nz) (whole segments):
+  // one run, or one member of a stack (whose FP64 psi copy stays until
+  // release_init_buffers, so that every member's q is built from it)
+  int init_state_range(int z0, int nz, int apply_sumB, int q_from_psi) override {
+    if (z0 < 0 || nz <= 0 || z0 + nz > g.n3 || z0 % g.nseg || nz % g.nseg) {
+      err = "initialisation range must cover whole members";
+      return QG_ERR_ARG;
+    }
     if (apply_sumB) {
-      k_sumB<T><<<(unsigned)((g.plane + 127) / 128), 128, 0, st>>>(g, F[F_BR], F[F_BI]);
+      k_sumB<T><<<(unsigned)((g.plane + 127) / 128), 128, 0, st>>>(g, F[F_BR], F[F_BI], z0, z0 + nz);
       QG_LAUNCHED();
     }
+    const size_t lb = (size_t)g.plane * sizeof(C), off = (size_t)z0 * g.plane;
     if (cfg.fixed_flow) {
       // fixed flow: q = 0 for all times (main_waqg.f90:141-146)
-      QG_CK(cudaMemsetAsync(F[F_Q], 0, (size_t)g.n3 * g.plane * sizeof(C), st));
+      QG_CK(cudaMemsetAsync(F[F_Q] + off, 0, (size_t)nz * lb, st));
     } else if (q_from_psi) {
       if (psi64) {
-        k_init_q<T, double><<<grid_for((long long)g.n3 * g.plane), 256, 0, st>>>(g, cfg.dz, cu, cl, psi64, F[F_Q]);
+        k_init_q<T, double><<<grid_for((long long)nz * g.plane), 256, 0, st>>>(g, cfg.dz, cu, cl, psi64, F[F_Q], z0,
+                                                                               z0 + nz);
       } else {
-        k_init_q<T, T><<<grid_for((long long)g.n3 * g.plane), 256, 0, st>>>(g, cfg.dz, cu, cl, F[F_PSI], F[F_Q]);
+        k_init_q<T, T><<<grid_for((long long)nz * g.plane), 256, 0, st>>>(g, cfg.dz, cu, cl, F[F_PSI], F[F_Q], z0,
+                                                                          z0 + nz);
       }
       QG_LAUNCHED();
     }
-    const size_t fbytes = (size_t)g.n3 * g.plane * sizeof(C);
-    QG_CK(cudaMemcpyAsync(F[F_QO], F[F_Q], fbytes, cudaMemcpyDeviceToDevice, st));
-    QG_CK(cudaMemcpyAsync(F[F_BRO], F[F_BR], fbytes, cudaMemcpyDeviceToDevice, st));
-    QG_CK(cudaMemcpyAsync(F[F_BIO], F[F_BI], fbytes, cudaMemcpyDeviceToDevice, st));
+    QG_CK(cudaMemcpyAsync(F[F_QO] + off, F[F_Q] + off, (size_t)nz * lb, cudaMemcpyDeviceToDevice, st));
+    QG_CK(cudaMemcpyAsync(F[F_BRO] + off, F[F_BR] + off, (size_t)nz * lb, cudaMemcpyDeviceToDevice, st));
+    QG_CK(cudaMemcpyAsync(F[F_BIO] + off, F[F_BI] + off, (size_t)nz * lb, cudaMemcpyDeviceToDevice, st));
     if (!cfg.passive_scalar && cfg.ybj_plus) {   // regular YBJ keeps the A the host set
-      int rc = launch_solve(F[F_QSTAR], 0, 1);
+      int rc = solve_generic(nullptr, F[F_BR], F[F_BI], nullptr, F[F_AR], F[F_AI], 0, 1, st, z0 / g.nseg,
+                             nz / g.nseg);
       if (rc) return rc;
     }
     QG_CK(cudaStreamSynchronize(st));
-    if (psi64) { cudaFree(psi64); psi64 = nullptr; }
     return QG_OK;
+  }
+
+  // the FP64 copy of psi that qg_set_state keeps for init_q (mixed path)
+  void release_init_buffers() override {
+    if (psi64) { cudaStreamSynchronize(st); cudaFree(psi64); psi64 = nullptr; }
   }
 
   // ---- the step -------------------------------------------------------------
@@ -351,10 +382,13 @@ class Engine : public EngineBase {
     return QG_OK;
   }
 
-  int diagnostics(qg_energy* out) override {
+  int diagnostics(qg_energy* out) override { return diagnostics_range(0, g.n3, out); }
+
+  // the integrals over levels [z0, z0 + nz): one run, or one member of a stack
+  int diagnostics_range(int z0, int nz, qg_energy* out) override {
     k_diag_level<T><<<dim3(kDiagChunks, g.n3), 256, 0, st>>>(g, cfg.dz, cfg.Bu, r2, F[F_BR], F[F_BI], F[F_AR], F[F_AI], F[F_PSI], diag_part);
     QG_LAUNCHED();
-    k_diag_sum<<<1, 32 * kNDiag, 0, st>>>(g.n3, diag_part, diag_out);
+    k_diag_sum<<<1, 32 * kNDiag, 0, st>>>(z0, nz, diag_part, diag_out);
     QG_LAUNCHED();
     QG_CK(cudaMemcpyAsync(diag_host, diag_out, kNDiag * sizeof(double), cudaMemcpyDeviceToHost, st));
     QG_CK(cudaStreamSynchronize(st));
@@ -601,6 +635,8 @@ class Engine : public EngineBase {
   int nsm = 1, occ_rm = 1, occ_rq = 1;   // SMs; resident CTAs per SM of the persistent row kernels
   double *om_t1 = nullptr, *om_du = nullptr, *om_dl = nullptr, *om_a = nullptr, *om_scr = nullptr;
   C* sig[2] = {};     // regular YBJ: per-level sigma terms
+  int members = 1;             // ensemble members stacked in z (segments of g.nseg levels)
+  double* mpar = nullptr;      // their step parameters (StepParams::mpar)
   C* S = nullptr;              // [lanes][Zb][kNScr][n][KXP] scratch planes
   int s_levels = 0;            // levels of scratch allocated
   double2* psi64 = nullptr;
@@ -628,7 +664,7 @@ class Engine : public EngineBase {
     for (auto& x : gexec) if (x) { cudaGraphExecDestroy(x); x = nullptr; }
     for (auto& p : F) if (p) { cudaFree(p); p = nullptr; }
     void* ps[] = {e1, e2, e1w, e2w, tw, tab_idx, fac_psi, fac_A, pcfac, vbuf, du, cu, cl, r2, diag_part, diag_out, S, stage,
-                  W, dstage, psi64, om_t1, om_du, om_dl, om_a, om_scr, sig[0], sig[1]};
+                  W, dstage, psi64, om_t1, om_du, om_dl, om_a, om_scr, sig[0], sig[1], mpar};
     for (void* p : ps) if (p) cudaFree(p);
     for (auto& p : D) if (p) cudaFree(p);
     for (auto& p : P) if (p) cudaFree(p);
@@ -881,15 +917,18 @@ class Engine : public EngineBase {
     return solve_generic(qs, F[F_BR], F[F_BI], F[F_PSI], F[F_AR], F[F_AI], do_psi, do_A);
   }
 
+  // the column solves of segments [seg0, seg0 + nsegs) (nsegs < 0: all)
   int solve_generic(const C* qs, const C* br, const C* bi, C* psi, C* ar, C* ai, int do_psi, int do_A,
-                    cudaStream_t on = nullptr) {
+                    cudaStream_t on = nullptr, int seg0 = 0, int nsegs = -1) {
     if (!do_psi && !do_A) return QG_OK;
     if (!on) on = st;
+    if (nsegs < 0) nsegs = members - seg0;
     if (kSolveStore && vbuf) {
       const int nrec = (do_psi ? 2 : 0) + (do_A ? 4 : 0);   // recurrences per column
 #define QG_SOLVE_ST(TCV, PCV)                                                                              \
-  k_solve_st<T, TCV, PCV><<<(unsigned)((g.plane + TCV - 1) / TCV), nrec * TCV, (size_t)g.n3 * 8, on>>>(   \
-      g, cfg.dz, cfg.Bu, tab_idx, fac_psi, fac_A, du, qs, br, bi, psi, ar, ai, do_psi, do_A, vbuf, pcfac)
+  k_solve_st<T, TCV, PCV><<<dim3((unsigned)((g.plane + TCV - 1) / TCV), nsegs), nrec * TCV,             \
+                            (size_t)g.nseg * 8, on>>>(                                                     \
+      g, cfg.dz, cfg.Bu, tab_idx, fac_psi, fac_A, du, qs, br, bi, psi, ar, ai, do_psi, do_A, vbuf, pcfac, seg0)
       if (pcfac) {
         if (solve_tc == 16) QG_SOLVE_ST(16, true);
         else if (solve_tc == 64) QG_SOLVE_ST(64, true);
@@ -903,8 +942,8 @@ class Engine : public EngineBase {
       QG_LAUNCHED();
       return QG_OK;
     }
-    k_solve<T><<<(unsigned)((g.plane + kSolveTC - 1) / kSolveTC), kSolveThreads, solve_smem(g.n3), on>>>(g, cfg.dz, cfg.Bu, tab_idx, fac_psi, fac_A,
-                                                                           du, qs, br, bi, psi, ar, ai, do_psi, do_A);
+    k_solve<T><<<dim3((unsigned)((g.plane + kSolveTC - 1) / kSolveTC), nsegs), kSolveThreads, solve_smem(g.nseg), on>>>(g, cfg.dz, cfg.Bu, tab_idx, fac_psi, fac_A,
+                                                                           du, qs, br, bi, psi, ar, ai, do_psi, do_A, seg0);
     QG_LAUNCHED();
     return QG_OK;
   }

@@ -590,10 +590,15 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
   load_tw<T, N>(tw, twg, NT);
   const T inv_n2 = (T)1 / ((T)N * (T)N);
   const long long zoff = (long long)z * g.plane;
-  const T dt = (T)sp.delt;
+  const int mem = sp.mpar ? z / g.nseg : 0;          // ensemble member of this level (stacks)
+  if (sp.mpar) {
+    const long long to = (long long)mem * g.plane;
+    e1t += to; e2t += to; e1wt += to; e2wt += to;
+  }
+  const T dt = (T)(sp.mpar ? sp.mpar[4 * mem] : sp.delt);
   const T dt2 = (T)2 * dt;
   const T gam = (T)sp.gamma;
-  const T cdisp = sp.disp ? (T)sp.cdisp : (T)0;
+  const T cdisp = sp.disp ? (T)(sp.mpar ? sp.mpar[4 * mem + 1] : sp.cdisp) : (T)0;
   const bool eul = sp.euler != 0;
   // staged entry (c, row) at row*CT + c
   auto stage = [&](int which) {
@@ -975,7 +980,8 @@ k_col_qw(Geom g, StepParams sp, int zbase, const cplx<T>* __restrict__ q, cplx<T
   load_tw<T, N>(tw, twg, NT);
   __syncthreads();
   const T inv_n2 = (T)1 / ((T)N * (T)N);
-  const T s = (T)sp.Ro * (T)sp.W2F;
+  const int mem = sp.mpar ? z / g.nseg : 0;          // ensemble member of this level (stacks)
+  const T s = sp.mpar ? (T)sp.mpar[4 * mem + 2] * (T)sp.mpar[4 * mem + 3] : (T)sp.Ro * (T)sp.W2F;
   const long long zoff = (long long)z * g.plane;
   auto pro = [&](int c, int j, cplx<T> (&v)[2][R0]) {
     const int kx = kx0 + c;
@@ -1028,11 +1034,12 @@ __global__ void k_dissipation(Geom g, double nuz, double dz, const cplx<T>* __re
     const long long m = i - (long long)z * g.plane;
     const int r = (int)(m / g.KXP), kx = (int)(m % g.KXP);
     cplx<T> v = mk<T>(0, 0);
+    const int zl = z % g.nseg;
     if (g.mask(kx, g.ky_of_row(r))) {
       const cplx<T> q0 = qo[i];
-      if (z == 0) {
+      if (zl == 0) {
         v = cscale(csub(qo[i + g.plane], q0), c);
-      } else if (z == g.n3 - 1) {
+      } else if (zl == g.nseg - 1) {
         v = cscale(csub(qo[i - g.plane], q0), c);
       } else {
         v = cscale(cadd(csub(qo[i + g.plane], cscale(q0, (T)2)), qo[i - g.plane]), c);
@@ -1137,11 +1144,11 @@ k_solve(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
         const double4* __restrict__ fac_psi, const double4* __restrict__ fac_A, const double* __restrict__ du,
         const cplx<T>* __restrict__ qs, const cplx<T>* __restrict__ BR, const cplx<T>* __restrict__ BI,
         cplx<T>* __restrict__ psi, cplx<T>* __restrict__ AR, cplx<T>* __restrict__ AI,
-        int do_psi, int do_A) {
+        int do_psi, int do_A, int seg0) {
   constexpr bool EXACT = sizeof(T) == 8;
   constexpr int TC = kSolveTC, NTH = kSolveThreads, S = kSeg;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int n3 = g.n3;
+  const int n3 = g.nseg;                          // levels of one column (blockIdx.y: its segment)
   double* du_s = reinterpret_cast<double*>(smem_raw);
   double* ck = du_s + n3 + threadIdx.x;           // checkpoint of segment j at ck[j*NTH]
   for (int i = threadIdx.x; i < n3; i += NTH) du_s[i] = du[i];
@@ -1154,8 +1161,9 @@ k_solve(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
   const int kx = (int)(m % g.KXP);
   if (kx > g.K) return;
   const long long P = g.plane;
-  const T* rhs = reinterpret_cast<const T*>(rhs_id == 0 ? qs : (rhs_id == 1 ? BR : BI)) + part;
-  T* out = reinterpret_cast<T*>(rhs_id == 0 ? psi : (rhs_id == 1 ? AR : AI)) + part;
+  const long long moff = 2 * (long long)(seg0 + blockIdx.y) * n3 * P;     // this segment's levels
+  const T* rhs = reinterpret_cast<const T*>(rhs_id == 0 ? qs : (rhs_id == 1 ? BR : BI)) + part + moff;
+  T* out = reinterpret_cast<T*>(rhs_id == 0 ? psi : (rhs_id == 1 ? AR : AI)) + part + moff;
   const int idx = tab_idx[m];
   if (idx < 0) {
     for (int i = 0; i < n3; ++i) out[2 * (i * P + m)] = (T)0;
@@ -1260,7 +1268,7 @@ constexpr int kQwReserve = QG_QW_RESERVE;
 // 1: s/d'_i, 2: u_i/d'_i; zeros where the column holds no retained mode.
 static __global__ void k_expand_fac(Geom g, const int* __restrict__ tab_idx, const double4* __restrict__ fac_psi,
                                     const double4* __restrict__ fac_A, double* __restrict__ pc) {
-  const long long P = g.plane, L = (long long)g.n3 * P;
+  const long long P = g.plane, L = (long long)g.nseg * P;     // one segment's levels
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < L; e += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(e / P);
     const long long m = e - (long long)i * P;
@@ -1269,7 +1277,7 @@ static __global__ void k_expand_fac(Geom g, const int* __restrict__ tab_idx, con
     for (int o = 0; o < 2; ++o) {
       double f = 0.0, y = 0.0, z = 0.0;
       if (idx >= 0) {
-        const double4* Fc = (o == 0 ? fac_psi : fac_A) + (long long)idx * g.n3;
+        const double4* Fc = (o == 0 ? fac_psi : fac_A) + (long long)idx * g.nseg;
         f = i > 0 ? Fc[i - 1].x : 0.0;
         y = Fc[i].y;
         z = Fc[i].z;
@@ -1289,12 +1297,12 @@ k_solve_st(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
            const double4* __restrict__ fac_psi, const double4* __restrict__ fac_A, const double* __restrict__ du,
            const cplx<T>* __restrict__ qs, const cplx<T>* __restrict__ BR, const cplx<T>* __restrict__ BI,
            cplx<T>* __restrict__ psi, cplx<T>* __restrict__ AR, cplx<T>* __restrict__ AI,
-           int do_psi, int do_A, double* __restrict__ vbuf, const double* __restrict__ pc) {
+           int do_psi, int do_A, double* __restrict__ vbuf, const double* __restrict__ pc, int seg0) {
   constexpr bool EXACT = sizeof(T) == 8;
   constexpr bool USEPC = PC && !EXACT;
   constexpr int S = kSegSt;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int n3 = g.n3;
+  const int n3 = g.nseg;          // levels of one column (blockIdx.y: its segment)
   double* du_s = reinterpret_cast<double*>(smem_raw);
   for (int i = threadIdx.x; i < n3; i += blockDim.x) du_s[i] = du[i];
   __syncthreads();
@@ -1308,8 +1316,9 @@ k_solve_st(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
   const int kx = (int)(m % g.KXP);
   if (kx > g.K) return;
   const long long P = g.plane;
-  const T* rhs = reinterpret_cast<const T*>(rhs_id == 0 ? qs : (rhs_id == 1 ? BR : BI)) + part;
-  T* out = reinterpret_cast<T*>(rhs_id == 0 ? psi : (rhs_id == 1 ? AR : AI)) + part;
+  const long long moff = (long long)(seg0 + blockIdx.y) * n3 * P;     // this segment's first level
+  const T* rhs = reinterpret_cast<const T*>(rhs_id == 0 ? qs : (rhs_id == 1 ? BR : BI)) + part + 2 * moff;
+  T* out = reinterpret_cast<T*>(rhs_id == 0 ? psi : (rhs_id == 1 ? AR : AI)) + part + 2 * moff;
   const int idx = tab_idx[m];
   if (idx < 0) {
     for (int i = 0; i < n3; ++i) out[2 * (i * P + m)] = (T)0;
@@ -1317,8 +1326,8 @@ k_solve_st(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
   }
   const double4* F = (rhs_id == 0 ? fac_psi : fac_A) + (long long)idx * n3;
   const double s = rhs_id == 0 ? __dmul_rn(dz, dz) : __dmul_rn(__dmul_rn(dz, dz), Bu);
-  double* vb = vbuf + (long long)chain * n3 * P + m;
-  const long long L = (long long)n3 * P;
+  double* vb = vbuf + (long long)chain * g.n3 * P + moff + m;
+  const long long L = (long long)n3 * P;          // per-column factors: one segment's levels
   // (USEPC) f_{i-1}, s/d'_i, u_i/d'_i of this column at + q*L + i*P
   const double* pcf = USEPC ? pc + (rhs_id == 0 ? 0 : 3) * L + m : nullptr;
   auto fwd = [&](double x, double f, T r) -> double {
@@ -1425,7 +1434,7 @@ __global__ void k_compact_to_dense(Geom g, int level0, int nlev, const cplx<T>* 
       if (mode == 0) {
         const cplx<T> a = f[(long long)z * g.plane + c];
         v = make_double2((double)a.x, (double)a.y);
-      } else if (z < g.n3 - 1) {
+      } else if (z % g.nseg < g.nseg - 1) {   // A_z = 0 on each segment's top level
         const cplx<T> a = f[(long long)z * g.plane + c], b = f[(long long)(z + 1) * g.plane + c];
         v = make_double2(((double)b.x - (double)a.x) / dz, ((double)b.y - (double)a.y) / dz);
       }
@@ -1439,23 +1448,25 @@ __global__ void k_compact_to_dense(Geom g, int level0, int nlev, const cplx<T>* 
 // ===========================================================================
 // sumB (derivatives.f90:1073-1118): remove the vertical mean of B where kh>0.
 template <typename T>
-__global__ void k_sumB(Geom g, cplx<T>* __restrict__ BR, cplx<T>* __restrict__ BI) {
+__global__ void k_sumB(Geom g, cplx<T>* __restrict__ BR, cplx<T>* __restrict__ BI, int zbeg, int zend) {
   const long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (m >= g.plane) return;
   const int r = (int)(m / g.KXP), kx = (int)(m % g.KXP);
   const int ky = g.ky_of_row(r);
   if (!g.mask(kx, ky) || kx * kx + ky * ky == 0) return;
-  double sr0 = 0, sr1 = 0, si0 = 0, si1 = 0;
-  for (int z = 0; z < g.n3; ++z) {
-    const cplx<T> a = BR[z * g.plane + m], b = BI[z * g.plane + m];
-    sr0 += a.x; sr1 += a.y; si0 += b.x; si1 += b.y;
-  }
-  sr0 /= g.n3; sr1 /= g.n3; si0 /= g.n3; si1 /= g.n3;
-  for (int z = 0; z < g.n3; ++z) {
-    cplx<T> a = BR[z * g.plane + m], b = BI[z * g.plane + m];
-    a.x = (T)((double)a.x - sr0); a.y = (T)((double)a.y - sr1);
-    b.x = (T)((double)b.x - si0); b.y = (T)((double)b.y - si1);
-    BR[z * g.plane + m] = a; BI[z * g.plane + m] = b;
+  for (int z0 = zbeg; z0 < zend; z0 += g.nseg) {   // each vertical segment of [zbeg, zend) on its own
+    double sr0 = 0, sr1 = 0, si0 = 0, si1 = 0;
+    for (int z = z0; z < z0 + g.nseg; ++z) {
+      const cplx<T> a = BR[z * g.plane + m], b = BI[z * g.plane + m];
+      sr0 += a.x; sr1 += a.y; si0 += b.x; si1 += b.y;
+    }
+    sr0 /= g.nseg; sr1 /= g.nseg; si0 /= g.nseg; si1 /= g.nseg;
+    for (int z = z0; z < z0 + g.nseg; ++z) {
+      cplx<T> a = BR[z * g.plane + m], b = BI[z * g.plane + m];
+      a.x = (T)((double)a.x - sr0); a.y = (T)((double)a.y - sr1);
+      b.x = (T)((double)b.x - si0); b.y = (T)((double)b.y - si1);
+      BR[z * g.plane + m] = a; BI[z * g.plane + m] = b;
+    }
   }
 }
 
@@ -1465,11 +1476,12 @@ __global__ void k_sumB(Geom g, cplx<T>* __restrict__ BR, cplx<T>* __restrict__ B
 // strong stratification) cancel, so the rounding sequence matters.
 template <typename T, typename TI>
 __global__ void k_init_q(Geom g, double dz, const double* __restrict__ cu, const double* __restrict__ cl,
-                         const cplx<TI>* __restrict__ psi, cplx<T>* __restrict__ q) {
-  const long long tot = (long long)g.n3 * g.plane;
+                         const cplx<TI>* __restrict__ psi, cplx<T>* __restrict__ q, int zbeg, int zend) {
+  const long long tot = (long long)zend * g.plane;
   const double dz2 = __dmul_rn(dz, dz);
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
-    const int z = (int)(i / g.plane);
+  for (long long i = (long long)zbeg * g.plane + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int z = (int)(i / g.plane), zl = z % g.nseg;   // zl: level within its segment
     const long long m = i - (long long)z * g.plane;
     const int r = (int)(m / g.KXP), kx = (int)(m % g.KXP);
     const int ky = g.ky_of_row(r);
@@ -1478,23 +1490,23 @@ __global__ void k_init_q(Geom g, double dz, const double* __restrict__ cu, const
       const double kdz = __dmul_rn(__dmul_rn((double)(kx * kx + ky * ky), dz), dz);
       const cplx<TI> p0 = psi[i];
       double vr, vi;
-      if (z == 0) {
+      if (zl == 0) {
         const cplx<TI> pp = psi[i + g.plane];
         const double d = __dadd_rn(cu[0], kdz);
         vr = __dsub_rn(__dmul_rn(cu[0], (double)pp.x), __dmul_rn(d, (double)p0.x));
         vi = __dsub_rn(__dmul_rn(cu[0], (double)pp.y), __dmul_rn(d, (double)p0.y));
-      } else if (z == g.n3 - 1) {
+      } else if (zl == g.nseg - 1) {
         const cplx<TI> pm = psi[i - g.plane];
-        const double d = __dadd_rn(cl[z], kdz);
-        vr = __dadd_rn(-__dmul_rn(d, (double)p0.x), __dmul_rn(cl[z], (double)pm.x));
-        vi = __dadd_rn(-__dmul_rn(d, (double)p0.y), __dmul_rn(cl[z], (double)pm.y));
+        const double d = __dadd_rn(cl[zl], kdz);
+        vr = __dadd_rn(-__dmul_rn(d, (double)p0.x), __dmul_rn(cl[zl], (double)pm.x));
+        vi = __dadd_rn(-__dmul_rn(d, (double)p0.y), __dmul_rn(cl[zl], (double)pm.y));
       } else {
         const cplx<TI> pp = psi[i + g.plane], pm = psi[i - g.plane];
-        const double d = __dadd_rn(__dadd_rn(cu[z], cl[z]), kdz);
-        vr = __dadd_rn(__dsub_rn(__dmul_rn(cu[z], (double)pp.x), __dmul_rn(d, (double)p0.x)),
-                       __dmul_rn(cl[z], (double)pm.x));
-        vi = __dadd_rn(__dsub_rn(__dmul_rn(cu[z], (double)pp.y), __dmul_rn(d, (double)p0.y)),
-                       __dmul_rn(cl[z], (double)pm.y));
+        const double d = __dadd_rn(__dadd_rn(cu[zl], cl[zl]), kdz);
+        vr = __dadd_rn(__dsub_rn(__dmul_rn(cu[zl], (double)pp.x), __dmul_rn(d, (double)p0.x)),
+                       __dmul_rn(cl[zl], (double)pm.x));
+        vi = __dadd_rn(__dsub_rn(__dmul_rn(cu[zl], (double)pp.y), __dmul_rn(d, (double)p0.y)),
+                       __dmul_rn(cl[zl], (double)pm.y));
       }
       out = mk<T>((T)__ddiv_rn(vr, dz2), (T)__ddiv_rn(vi, dz2));
     }
@@ -1587,8 +1599,8 @@ k_diag_level(Geom g, double dz, double Bu, const double* __restrict__ r2, const 
   const long long zo = (long long)z * g.plane;
   const long long per = (g.plane + kDiagChunks - 1) / kDiagChunks;
   const long long m0 = chunk * per, m1 = m0 + per < g.plane ? m0 + per : g.plane;
-  const bool top = (z == g.n3 - 1);
-  const double rz = r2[z];
+  const bool top = (z % g.nseg == g.nseg - 1);     // top level of its segment
+  const double rz = r2[z % g.nseg];
   double acc[kNDiag] = {0, 0, 0, 0, 0, 0, 0};
   for (long long m = m0 + threadIdx.x; m < m1; m += blockDim.x) {
     const int mi = (int)m, r = mi / g.KXP, kx = mi - r * g.KXP;
@@ -1644,9 +1656,10 @@ k_diag_level(Geom g, double dz, double Bu, const double* __restrict__ r2, const 
 
 // one warp per quantity: lane l sums levels l, l+32, ... (each level's
 // chunks in order), then a fixed butterfly over the lanes; mean over levels
-static __global__ void k_diag_sum(int n3, const double* __restrict__ part, double* __restrict__ out) {
+static __global__ void k_diag_sum(int z0, int n3, const double* __restrict__ part, double* __restrict__ out) {
   const int k = threadIdx.x / 32, lane = threadIdx.x % 32;
   if (k >= kNDiag) return;
+  part += (long long)z0 * kDiagChunks * kNDiag;     // levels z0 .. z0 + n3 - 1
   double s = 0.0;
   for (int z = lane; z < n3; z += 32) {
     double lv = 0.0;

@@ -28,7 +28,7 @@ EXPORTS = (
     "qg_ensemble_get_stream", "qg_ensemble_destroy", "qg_ensemble_last_error", "qg_autotune",
     "qg_adjoint_run", "qg_adjoint_step", "qg_dump_psi", "qg_dump_la",
     "qg_omega_eqn_rhs", "qg_omega_equation", "qg_omega", "qg_ensemble_set_lanes",
-    "qg_selftest_conversions", "qg_selftest_wait",
+    "qg_selftest_conversions", "qg_selftest_wait", "qg_ensemble_profile_step",
 )
 KERNEL_CLASSES = ("dissipation", "col_inv", "row_main", "col_update", "row_qw", "col_qw", "solve", "solve_A")
 
@@ -103,6 +103,7 @@ def lib() -> C.CDLL:
         "qg_ensemble_get_stream": (ip, [vp, C.POINTER(vp)]),
         "qg_ensemble_destroy": (ip, [vp]),
         "qg_ensemble_last_error": (C.c_char_p, [vp]),
+        "qg_ensemble_profile_step": (ip, [vp, ip, C.POINTER(C.c_double), C.POINTER(C.c_int), ip]),
         "qg_autotune": (ip, [C.POINTER(QgConfig), ip, C.POINTER(QgTuning)]),
         "qg_adjoint_run": (ip, [vp, vp, vp, vp, ip, ip, ip, dp, vp, vp, vp]),
         "qg_adjoint_step": (ip, [vp, ip, vp, vp, vp, vp]),

@@ -324,8 +324,19 @@ class Ensemble:
     def step(self, nsteps: int = 1, euler_first: bool = False):
         self._ck(lib().qg_ensemble_step(self.e, int(nsteps), int(euler_first)))
 
+    def profile_step(self, euler_first: bool = False) -> dict:
+        """One step of every run with CUDA events around each launch:
+        {class: (ms, launches)} summed over the runs."""
+        from ._lib import KERNEL_CLASSES
+        n = len(KERNEL_CLASSES)
+        ms = (C.c_double * n)()
+        cnt = (C.c_int * n)()
+        self._ck(lib().qg_ensemble_profile_step(self.e, int(euler_first), ms, cnt, n))
+        return {k: (ms[i], cnt[i]) for i, k in enumerate(KERNEL_CLASSES)}
+
     def set_lanes(self, lanes: int):
-        """Member chains the step graph runs concurrently (qg_ensemble_set_lanes)."""
+        """Runs (stacks of same-shape members, or single members) the step
+        graph advances concurrently (qg_ensemble_set_lanes)."""
         self._ck(lib().qg_ensemble_set_lanes(self.e, int(lanes)))
 
     def synchronize(self):
