@@ -721,7 +721,7 @@ class Engine : public EngineBase {
   }
   template <int NN> static constexpr size_t sm_col6() { return (size_t)(NN + 6 * Tiles<T, NN>::CT * Tiles<T, NN>::LD) * sizeof(C); }
   template <int NN> static constexpr size_t sm_row7() { return (size_t)(NN + 7 * Tiles<T, NN>::RT * Tiles<T, NN>::LD) * sizeof(C); }
-  template <int NN> static constexpr size_t sm_rr3() { return (size_t)(NN + 3 * Tiles<T, NN>::RRT * Tiles<T, NN>::LD) * sizeof(C); }
+  template <int NN> static constexpr size_t sm_rr3() { return (size_t)(NN + 3 * Tiles<T, NN>::QRT * Tiles<T, NN>::LD) * sizeof(C); }
   template <int NN> static constexpr size_t sm_rm4() { return (size_t)(NN + 4 * Tiles<T, NN>::RTM * Tiles<T, NN>::LD) * sizeof(C); }
   // the persistent row kernels add a staging copy of an item's scratch rows
   // (nf planes x rows x kxp) and its mbarrier; the attribute is set for the
@@ -731,7 +731,7 @@ class Engine : public EngineBase {
     return sm_rm4<NN>() + (Tiles<T, NN>::RPRE ? (size_t)6 * Tiles<T, NN>::RTM * kxp * sizeof(C) + 16 : 0);
   }
   template <int NN> static constexpr size_t sm_rq(int kxp) {
-    return sm_rr3<NN>() + (Tiles<T, NN>::QPRE ? (size_t)4 * Tiles<T, NN>::RRT * kxp * sizeof(C) + 16 : 0);
+    return sm_rr3<NN>() + (Tiles<T, NN>::QPRE ? (size_t)4 * Tiles<T, NN>::QRT * kxp * sizeof(C) + 16 : 0);
   }
   template <int NN> static constexpr size_t sm_row4() { return (size_t)(NN + 4 * Tiles<T, NN>::RT * Tiles<T, NN>::LD) * sizeof(C); }
   // shared memory of the dense (routine-level) kernels
@@ -843,7 +843,7 @@ class Engine : public EngineBase {
       cudaStream_t bs = lane == 0 ? st : lst[lane];
       C* Sb = S + lane * slot;
       QG_SWITCH_N(g.n, {
-        const dim3 gc(g.KXP / Tiles<T, NN>::CT, zc), gr(g.n / Tiles<T, NN>::RRT, zc),
+        const dim3 gc(g.KXP / Tiles<T, NN>::CT, zc), gr(g.n / Tiles<T, NN>::QRT, zc),
             grm(g.n / Tiles<T, NN>::RTM, zc);
         if (int rc0 = pbeg(QG_K_COL_INV, bs)) return rc0;
         k_col_inv<T, NN><<<gc, kColThreads, sm_ci<NN>(3), bs>>>(g, z0, F[F_PSI], F[F_Q], F[F_BR], F[F_BI], Sb, tw);
@@ -874,7 +874,7 @@ class Engine : public EngineBase {
         if (need_qw) {
           if (int rc0 = pbeg(QG_K_ROW_QW, bs)) return rc0;
           if constexpr (Tiles<T, NN>::QPRE) {
-            const int items = zc * (NN / Tiles<T, NN>::RRT);
+            const int items = zc * (NN / Tiles<T, NN>::QRT);
             const int per_sm = (split && last) ? std::max(1, occ_rq - kQwReserve) : occ_rq;
             k_row_qw<T, NN><<<std::min(items, std::max(1, nsm * per_sm / L)), Tiles<T, NN>::QTHREADS, sm_rq<NN>(g.KXP), bs>>>(
                 g, Sb, tw, items, wflag);

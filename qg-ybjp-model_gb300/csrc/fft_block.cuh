@@ -63,7 +63,20 @@ __device__ __forceinline__ void dftR(cplx<T>* v) {
   else dft2<T, FWD>(v[0], v[1]);
 }
 
-template <int REM> struct PassRadix { static constexpr int value = REM >= 8 ? 8 : (REM >= 4 ? 4 : 2); };
+// Radix of the pass that leaves a remaining length REM = 2^m (the pass with
+// stride NS of a length-N transform has REM = N/NS).  Radix 8 wherever it
+// fits; a leftover factor 4 or 2 goes to a middle pass (N = 256: 8 x 4 x 8,
+// N = 128: 8 x 2 x 8, N = 1024: 8 x 8 x 2 x 8), so that every transform of
+// 64 points or more starts and ends with a radix-8 pass: the row kernels
+// hand the inverse transform's last pass to the forward transform's first
+// pass in registers, which needs the two radices equal.  Below 64 points
+// the leftover factor comes first (32: 4 x 8, 16: 2 x 8).
+__host__ __device__ constexpr int radix_of(int rem) {
+  int m = 0;
+  while ((1 << m) < rem) ++m;
+  return (m % 3 == 0 || m >= 7) ? 8 : (m % 3 == 2 ? 4 : 2);
+}
+template <int REM> struct PassRadix { static constexpr int value = radix_of(REM); };
 
 // One Stockham pass over `batch` transforms of length N stored with leading
 // dimension ld; tw[m] = W_N^m (forward sign).
@@ -191,7 +204,6 @@ static_assert(conflict_free512(), "lay_idx<1> leaves a bank conflict");
 // Twiddles laid out per pass: the pass with stride NS and radix R reads
 // W_N^{k r N/(NS R)} at tw[off(NS) + (r-1)*NS + k], so the threads of a warp
 // (consecutive k) read consecutive words.  Fewer than N entries in total.
-__host__ __device__ constexpr int radix_of(int rem) { return rem >= 8 ? 8 : (rem >= 4 ? 4 : 2); }
 template <int N> __host__ __device__ constexpr int tw_off(int ns) {
   int off = 0;
   for (int s = 1; s < ns; s *= radix_of(N / s)) if (s > 1) off += s * (radix_of(N / s) - 1);

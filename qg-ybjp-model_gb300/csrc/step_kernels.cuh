@@ -114,7 +114,13 @@ template <typename T, int N> struct Tiles {
   static constexpr int FSC = PadLD<N>::value * CT;   // interleaved column tile (colfft.cuh)
   static constexpr int RRT = kRowRT > 0 ? kRowRT : RT;   // rows per CTA of the forward row kernels
   static constexpr int RMINB = imin(CB == 8 ? kRowMinB : 2, smem_ctas((N + 4 * RRT * LD) * CB));
-  static constexpr int QMINB = imin(CB == 8 ? kRowQwMinB : 2, smem_ctas((N + 3 * RRT * LD) * CB));
+  // rows per k_row_qw CTA: one (row, butterfly) task per thread where its
+  // transforms can be fused in registers (below), else RRT
+  static constexpr bool QFUSABLE = kRowFuse && CB == 8 && kRowPass0 && N >= 256 && N <= 512 &&
+                                   LastNS<N>::value == N / radix_of(N) &&
+                                   (CB == 8 ? kRowQwThreads : kRowThreads) % (N / radix_of(N)) == 0;
+  static constexpr int QRT = QFUSABLE ? (CB == 8 ? kRowQwThreads : kRowThreads) / (N / radix_of(N)) : RRT;
+  static constexpr int QMINB = imin(CB == 8 ? kRowQwMinB : 2, smem_ctas((N + 3 * QRT * LD) * CB));
   // FP32: the first inverse row pass fed from registers, k_row_qw on 128
   // threads; FP64 keeps the shared-memory fill and 256 threads (the
   // register-fed pass doubles its registers and halves its occupancy)
@@ -123,13 +129,13 @@ template <typename T, int N> struct Tiles {
   // k_row_main with the inverse last pass, the products and the forward first
   // pass in registers: needs the inverse's last radix to equal the forward's
   // first (N = 512: 8 x 8 x 8) and one (row, butterfly) task per thread
-  static constexpr bool RFUSE = kRowFuse && RPASS0 && N >= 256 && LastNS<N>::value == N / radix_of(N) &&
+  static constexpr bool RFUSE = kRowFuse && RPASS0 && N >= 256 && N <= 512 && LastNS<N>::value == N / radix_of(N) &&
                                 kRowThreads % (N / radix_of(N)) == 0;
   static constexpr int RTM = RFUSE ? kRowThreads / (N / radix_of(N)) : RRT;   // rows per k_row_main CTA
   static constexpr int MMINB = imin(CB == 8 ? (RFUSE ? kRowMainMinB : kRowMinB) : 2, smem_ctas((N + 4 * RTM * LD) * CB));
-  // the same for k_row_qw (rows RRT, QTHREADS threads)
-  static constexpr bool QFUSE = kRowFuse && RPASS0 && N >= 256 && LastNS<N>::value == N / radix_of(N) &&
-                                RRT * (N / radix_of(N)) == QTHREADS;
+  // the same for k_row_qw (rows QRT, QTHREADS threads)
+  static constexpr bool QFUSE = kRowFuse && RPASS0 && N >= 256 && N <= 512 && LastNS<N>::value == N / radix_of(N) &&
+                                QRT * (N / radix_of(N)) == QTHREADS;
   // persistent row kernels that bulk-copy the next item's scratch rows into
   // shared memory during the current item (the fused FP32 row kernels)
   static constexpr bool RPRE = kRowPrefetch && RFUSE;
@@ -142,7 +148,7 @@ template <typename T, int N> struct Tiles {
   // the forward transforms' last pass and the split of the packed spectra in
   // registers (colfft.cuh:row_last_fwd512): one row per 64 threads
   static constexpr bool RSHL = kRowShflLast && RFUSE && N == 512 && RTM * 64 == kRowThreads;
-  static constexpr bool QSHL = kRowShflLast && QFUSE && N == 512 && RRT * 64 == QTHREADS;
+  static constexpr bool QSHL = kRowShflLast && QFUSE && N == 512 && QRT * 64 == QTHREADS;
   static constexpr int CIMINB = imin(CB == 8 ? kColInvMinB : 2, smem_ctas((N + 3 * FSC) * CB));
   static constexpr int CQMINB = imin(CB == 8 ? kColQwMinB : 2, smem_ctas((N + 2 * FSC) * CB));
 };
@@ -792,7 +798,7 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
 template <typename T, int N, class Src, class After>
 __device__ __forceinline__ void row_qw_item(const Geom& g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ tw,
                                             cplx<T>* __restrict__ bA, int zb, int y0, Src src, After after_pass0) {
-  constexpr int RT = Tiles<T, N>::RRT, LD = Tiles<T, N>::LD, NT = Tiles<T, N>::QTHREADS, LAY = Tiles<T, N>::QLAY;
+  constexpr int RT = Tiles<T, N>::QRT, LD = Tiles<T, N>::LD, NT = Tiles<T, N>::QTHREADS, LAY = Tiles<T, N>::QLAY;
   const int tid = threadIdx.x;
   const int K = g.K;
   // packed: (BR, BI), (BRx, BIx), (BRy, BIy)
@@ -918,7 +924,7 @@ __device__ __forceinline__ void row_qw_item(const Geom& g, cplx<T>* __restrict__
 template <typename T, int N>
 __global__ void __launch_bounds__(Tiles<T, N>::QTHREADS, Tiles<T, N>::QMINB)
 k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg, int nitems, int* __restrict__ wflag) {
-  constexpr int RT = Tiles<T, N>::RRT, LD = Tiles<T, N>::LD, NT = Tiles<T, N>::QTHREADS;
+  constexpr int RT = Tiles<T, N>::QRT, LD = Tiles<T, N>::LD, NT = Tiles<T, N>::QTHREADS;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* bA = tw + N;               // [3][RT][LD]; then, in place, (P1, P2) in the first RT

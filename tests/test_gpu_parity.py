@@ -130,6 +130,22 @@ def test_steps_small(precision):
     sim.close()
 
 
+@pytest.mark.parametrize("n", [128, 256, 512])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_steps_each_row_kernel_path(precision, n):
+    """10 steps at n = 128 (row transforms through shared memory), 256
+    (radices 8 x 4 x 8, inverse and forward row transforms fused in
+    registers) and 512 (8 x 8 x 8, fused, spectra split by warp shuffles),
+    exponential stratification, against the oracle."""
+    rc = scaled(CONFIGS["c1"], n, 6)
+    model, st, sim = pair(rc, precision)
+    sim.steps_async(10, True)
+    sim.synchronize()
+    st = model.run(st, 10, first=True)
+    compare(sim, st, 1e-12 if precision == "fp64" else 1e-5)
+    sim.close()
+
+
 def test_c0_fp64_200_steps():
     """64^2 x 64, FP64, 200 leapfrog steps: relative L2 <= 1e-12 per field."""
     rc = CONFIGS["c0"]
