@@ -116,7 +116,7 @@ template <typename T, int N> struct Tiles {
   static constexpr int RMINB = imin(CB == 8 ? kRowMinB : 2, smem_ctas((N + 4 * RRT * LD) * CB));
   // rows per k_row_qw CTA: one (row, butterfly) task per thread where its
   // transforms can be fused in registers (below), else RRT
-  static constexpr bool QFUSABLE = kRowFuse && CB == 8 && kRowPass0 && N >= 256 && N <= 512 &&
+  static constexpr bool QFUSABLE = kRowFuse && CB == 8 && kRowPass0 && N >= 64 && N <= 512 &&
                                    LastNS<N>::value == N / radix_of(N) &&
                                    (CB == 8 ? kRowQwThreads : kRowThreads) % (N / radix_of(N)) == 0;
   static constexpr int QRT = QFUSABLE ? (CB == 8 ? kRowQwThreads : kRowThreads) / (N / radix_of(N)) : RRT;
@@ -129,12 +129,12 @@ template <typename T, int N> struct Tiles {
   // k_row_main with the inverse last pass, the products and the forward first
   // pass in registers: needs the inverse's last radix to equal the forward's
   // first (N = 512: 8 x 8 x 8) and one (row, butterfly) task per thread
-  static constexpr bool RFUSE = kRowFuse && RPASS0 && N >= 256 && N <= 512 && LastNS<N>::value == N / radix_of(N) &&
+  static constexpr bool RFUSE = kRowFuse && RPASS0 && N >= 64 && N <= 512 && LastNS<N>::value == N / radix_of(N) &&
                                 kRowThreads % (N / radix_of(N)) == 0;
   static constexpr int RTM = RFUSE ? kRowThreads / (N / radix_of(N)) : RRT;   // rows per k_row_main CTA
   static constexpr int MMINB = imin(CB == 8 ? (RFUSE ? kRowMainMinB : kRowMinB) : 2, smem_ctas((N + 4 * RTM * LD) * CB));
   // the same for k_row_qw (rows QRT, QTHREADS threads)
-  static constexpr bool QFUSE = kRowFuse && RPASS0 && N >= 256 && N <= 512 && LastNS<N>::value == N / radix_of(N) &&
+  static constexpr bool QFUSE = kRowFuse && RPASS0 && N >= 64 && N <= 512 && LastNS<N>::value == N / radix_of(N) &&
                                 QRT * (N / radix_of(N)) == QTHREADS;
   // persistent row kernels that bulk-copy the next item's scratch rows into
   // shared memory during the current item (the fused FP32 row kernels)
