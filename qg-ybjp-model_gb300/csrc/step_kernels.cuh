@@ -68,8 +68,14 @@ constexpr bool kRowFuse = true;    // k_row_main: inverse last pass, products, f
 constexpr int kRowMainMinB = 2;    // k_row_main CTAs per SM when fused
 constexpr bool kRowPrefetch = true; // fused row kernels: persistent, next item's rows bulk-copied ahead
 constexpr bool kRowSwizzle = true;  // k_row_qw (N = 512): conflict-free XOR placement (lay_idx<1>)
-constexpr bool kRowMainSwizzle = false;  // k_row_main: the same (its index arithmetic spills at 128 registers)
-constexpr bool kRowMainMidSwz = false;   // k_row_main forward transforms: XOR placement between the last two passes (measured slower: spills)
+#ifndef QG_ROWMAIN_SWZ
+#define QG_ROWMAIN_SWZ 0
+#endif
+constexpr bool kRowMainSwizzle = QG_ROWMAIN_SWZ != 0;  // k_row_main: the same (its index arithmetic spills at 128 registers)
+#ifndef QG_ROWMAIN_MIDSWZ
+#define QG_ROWMAIN_MIDSWZ 0
+#endif
+constexpr bool kRowMainMidSwz = QG_ROWMAIN_MIDSWZ != 0;   // k_row_main forward transforms: XOR placement between the last two passes (measured slower: spills)
 constexpr bool kRowMainMidSwzInv = false;  // the same for its inverse transforms (spills: the last pass feeds the products)
 #ifndef QG_ROW_SHFL_LAST
 #define QG_ROW_SHFL_LAST 1

@@ -50,7 +50,7 @@ def compare(sim, st, tol, fields=FIELDS):
 
 # --- transforms ------------------------------------------------------------------
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-@pytest.mark.parametrize("n", [16, 64, 256])
+@pytest.mark.parametrize("n", [16, 64, 128, 256, 512])
 def test_fft_dropins(precision, n):
     rc = scaled(CONFIGS["c0"], n, 4)
     model, st, sim = pair(rc, precision)
