@@ -73,10 +73,13 @@ constexpr bool kRowSwizzle = true;  // k_row_qw (N = 512): conflict-free XOR pla
 #endif
 constexpr bool kRowMainSwizzle = QG_ROWMAIN_SWZ != 0;  // k_row_main: the same (its index arithmetic spills at 128 registers)
 #ifndef QG_ROWMAIN_MIDSWZ
-#define QG_ROWMAIN_MIDSWZ 0
+#define QG_ROWMAIN_MIDSWZ 1
 #endif
-constexpr bool kRowMainMidSwz = QG_ROWMAIN_MIDSWZ != 0;   // k_row_main forward transforms: XOR placement between the last two passes (measured slower: spills)
-constexpr bool kRowMainMidSwzInv = false;  // the same for its inverse transforms (spills: the last pass feeds the products)
+constexpr bool kRowMainMidSwz = QG_ROWMAIN_MIDSWZ != 0;   // k_row_main forward transforms: XOR placement between the last two passes (0.965 -> 0.921 ms at 512^2 x 256 with the last pass in registers)
+#ifndef QG_ROWMAIN_MIDSWZI
+#define QG_ROWMAIN_MIDSWZI 1
+#endif
+constexpr bool kRowMainMidSwzInv = QG_ROWMAIN_MIDSWZI != 0;  // the same for its inverse transforms (0.921 -> 0.907 ms)
 #ifndef QG_ROW_SHFL_LAST
 #define QG_ROW_SHFL_LAST 1
 #endif
