@@ -660,7 +660,11 @@ static int ens_capture(qg_ensemble* e, int euler) {
 int qg_ensemble_step(qg_ensemble* e, int nsteps, int euler_first) {
   if (!e || nsteps < 0) return ens_fail(e, QG_ERR_ARG, "bad arguments");
   e->err.clear();
-  for (auto* r : e->runs) r->eng->release_init_buffers();   // outside any capture
+  for (auto* r : e->runs) {                                  // outside any capture
+    r->eng->release_init_buffers();
+    const int rc = r->eng->prepare();
+    if (rc) return ens_fail(e, rc, r->eng->err);
+  }
   for (int i = 0; i < nsteps; ++i) {
     const int k = (euler_first && i == 0) ? 1 : 0;
     if (!e->gexec[k]) {

@@ -43,6 +43,9 @@ struct EngineBase {
   // release of what the initialisation kept (see Engine::init_state_range)
   virtual int init_state_range(int z0, int nz, int apply_sumB, int q_from_psi) = 0;
   virtual void release_init_buffers() = 0;
+  // work that must precede a step and cannot be captured with it (launched
+  // on the engine's stream); run before capturing enqueue() into a graph
+  virtual int prepare() = 0;
   // levels per member and members of this engine (a stack holds several)
   virtual int levels_per_member() const = 0;
   virtual int member_count() const = 0;

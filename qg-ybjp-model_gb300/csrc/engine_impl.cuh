@@ -150,6 +150,10 @@ class Engine : public EngineBase {
     sp.ybj = cfg.ybj_plus ? 1 : 0;
     sp.mpar = mpar;
     need_qw = (!cfg.fixed_flow && !cfg.no_feedback);
+    // kept y-inverse planes of B (FP32 YBJ+ runs whose update transforms B^{n+1} for q^w)
+    if (kReuseB && sizeof(T) == 4 && need_qw && cfg.ybj_plus && kColInvNF2) {
+      QG_CK(cudaMalloc(&Qp, (size_t)g.n3 * kNQ * g.n * g.KXP * sizeof(C)));
+    }
     int r0 = set_smem_attrs();
     if (r0) return r0;
     if (cfg.solve_columns != 0 && cfg.solve_columns != 16 && cfg.solve_columns != 32 && cfg.solve_columns != 64) {
@@ -267,6 +271,7 @@ class Engine : public EngineBase {
       src = (const double2*)stage;
     }
     *(volatile int*)(wflag_h + 2) = 0;
+    if (f == F_BR || f == F_BI) q_valid = false;
     k_dense_to_compact<T><<<grid_for((long long)nlev * g.plane), 256, 0, st>>>(g, level0, nlev, src, F[f], iflag);
     QG_LAUNCHED();
     if (f == F_PSI && sizeof(T) == 4) {
@@ -331,6 +336,7 @@ class Engine : public EngineBase {
       err = "initialisation range must cover whole members";
       return QG_ERR_ARG;
     }
+    q_valid = false;
     if (apply_sumB) {
       k_sumB<T><<<(unsigned)((g.plane + 127) / 128), 128, 0, st>>>(g, F[F_BR], F[F_BI], z0, z0 + nz);
       QG_LAUNCHED();
@@ -635,6 +641,8 @@ class Engine : public EngineBase {
   int nsm = 1, occ_rm = 1, occ_rq = 1;   // SMs; resident CTAs per SM of the persistent row kernels
   double *om_t1 = nullptr, *om_du = nullptr, *om_dl = nullptr, *om_a = nullptr, *om_scr = nullptr;
   C* sig[2] = {};     // regular YBJ: per-level sigma terms
+  C* Qp = nullptr;             // kept y-inverse planes of B, [n3][2][n][KXP], or null
+  bool q_valid = false;        // Qp holds the transforms of the current B
   int members = 1;             // ensemble members stacked in z (segments of g.nseg levels)
   double* mpar = nullptr;      // their step parameters (StepParams::mpar)
   C* S = nullptr;              // [lanes][Zb][kNScr][n][KXP] scratch planes
@@ -664,7 +672,7 @@ class Engine : public EngineBase {
     for (auto& x : gexec) if (x) { cudaGraphExecDestroy(x); x = nullptr; }
     for (auto& p : F) if (p) { cudaFree(p); p = nullptr; }
     void* ps[] = {e1, e2, e1w, e2w, tw, tab_idx, fac_psi, fac_A, pcfac, vbuf, du, cu, cl, r2, diag_part, diag_out, S, stage,
-                  W, dstage, psi64, om_t1, om_du, om_dl, om_a, om_scr, sig[0], sig[1], mpar};
+                  W, dstage, psi64, om_t1, om_du, om_dl, om_a, om_scr, sig[0], sig[1], mpar, Qp};
     for (void* p : ps) if (p) cudaFree(p);
     for (auto& p : D) if (p) cudaFree(p);
     for (auto& p : P) if (p) cudaFree(p);
@@ -789,6 +797,7 @@ class Engine : public EngineBase {
  public:
   int profile_step(int euler, double* ms, int* launches, int nclasses) override {
     for (int i = 0; i < nclasses; ++i) { ms[i] = 0.0; launches[i] = 0; }
+    if (int rc = prepare()) return rc;
     prof_on = true;
     prof_ev.clear();
     int rc = enqueue_step(euler ? 1 : 0);
@@ -846,22 +855,24 @@ class Engine : public EngineBase {
         const dim3 gc(g.KXP / Tiles<T, NN>::CT, zc), gr(g.n / Tiles<T, NN>::QRT, zc),
             grm(g.n / Tiles<T, NN>::RTM, zc);
         if (int rc0 = pbeg(QG_K_COL_INV, bs)) return rc0;
-        k_col_inv<T, NN><<<gc, kColThreads, sm_ci<NN>(3), bs>>>(g, z0, F[F_PSI], F[F_Q], F[F_BR], F[F_BI], Sb, tw);
+        C* Qb = Qp ? Qp + (size_t)z0 * kNQ * g.n * g.KXP : nullptr;
+        k_col_inv<T, NN><<<gc, kColThreads, sm_ci<NN>(3), bs>>>(g, z0, F[F_PSI], F[F_Q], F[F_BR], F[F_BI], Sb, tw,
+                                                                Qb, Qb ? 1 : 0);
         QG_LAUNCHED();
         if (int rc0 = pend(bs)) return rc0;
         if (int rc0 = pbeg(QG_K_ROW_MAIN, bs)) return rc0;
         if constexpr (Tiles<T, NN>::RPRE) {
           const int items = zc * (NN / Tiles<T, NN>::RTM);
           k_row_main<T, NN><<<std::min(items, std::max(1, nsm * occ_rm / L)), kRowThreads, sm_rm<NN>(g.KXP), bs>>>(g, s, Sb, tw, items,
-                                                                                                 wflag);
+                                                                                                 wflag, Qb);
         } else {
-          k_row_main<T, NN><<<grm, kRowThreads, sm_rm<NN>(g.KXP), bs>>>(g, s, Sb, tw, 0, wflag);
+          k_row_main<T, NN><<<grm, kRowThreads, sm_rm<NN>(g.KXP), bs>>>(g, s, Sb, tw, 0, wflag, Qb);
         }
         QG_LAUNCHED();
         if (int rc0 = pend(bs)) return rc0;
         if (int rc0 = pbeg(QG_K_COL_UPDATE, bs)) return rc0;
         k_col_update<T, NN><<<gc, kColThreads, UpdLay<T, NN>::bytes(), bs>>>(g, s, z0, sptr, e1, e2, e1w, e2w, Sb, tw,
-                                                                need_qw ? 1 : 0);
+                                                                need_qw ? 1 : 0, Qb);
         QG_LAUNCHED();
         if (int rc0 = pend(bs)) return rc0;
         if (overlap && last) {
@@ -877,9 +888,9 @@ class Engine : public EngineBase {
             const int items = zc * (NN / Tiles<T, NN>::QRT);
             const int per_sm = (split && last) ? std::max(1, occ_rq - kQwReserve) : occ_rq;
             k_row_qw<T, NN><<<std::min(items, std::max(1, nsm * per_sm / L)), Tiles<T, NN>::QTHREADS, sm_rq<NN>(g.KXP), bs>>>(
-                g, Sb, tw, items, wflag);
+                g, Sb, tw, items, wflag, Qb);
           } else {
-            k_row_qw<T, NN><<<gr, Tiles<T, NN>::QTHREADS, sm_rq<NN>(g.KXP), bs>>>(g, Sb, tw, 0, wflag);
+            k_row_qw<T, NN><<<gr, Tiles<T, NN>::QTHREADS, sm_rq<NN>(g.KXP), bs>>>(g, Sb, tw, 0, wflag, Qb);
           }
           QG_LAUNCHED();
           if (int rc0 = pend(bs)) return rc0;
@@ -948,7 +959,26 @@ class Engine : public EngineBase {
     return QG_OK;
   }
 
+  // Before a step (outside any stream capture): the kept B planes, when
+  // they do not hold the transforms of the current B (new handle,
+  // qg_set_state of BR or BI, initialisation), are computed from B.
+  int prepare() override {
+    if (!Qp || q_valid) return QG_OK;
+    for (int z0 = 0; z0 < g.n3; z0 += Zb) {
+      const int zc = std::min(Zb, g.n3 - z0);
+      QG_SWITCH_N(g.n, {
+        const dim3 gc(g.KXP / Tiles<T, NN>::CT, zc);
+        k_col_inv<T, NN><<<gc, kColThreads, sm_ci<NN>(3), st>>>(g, z0, F[F_PSI], F[F_Q], F[F_BR], F[F_BI], S, tw,
+                                                                Qp + (size_t)z0 * kNQ * g.n * g.KXP, 2);
+        QG_LAUNCHED();
+      });
+    }
+    q_valid = true;     // every step keeps them current from here on
+    return QG_OK;
+  }
+
   int run_step(int euler) {
+    if (int rc = prepare()) return rc;
     if (!cfg.use_graphs) return enqueue_step(euler);
     if (!gexec[euler]) {
       cudaGraph_t graph = nullptr;

@@ -28,6 +28,14 @@ template <> struct Tile<double> { static constexpr int CT = 4; static constexpr 
 __host__ __device__ __forceinline__ long long scr_off(int zb, int f, int y, int n, int KXP) {
   return (((long long)zb * kNScr + f) * n + y) * KXP;
 }
+// The y-inverse transforms of B^{n+1} that k_col_update computes for q^w are
+// those of the next step's B^n: with kReuseB they are kept for every level in
+// Q[z][2][n][KXP] (BR, BI), read by the next step's k_row_main and by
+// k_row_qw, and k_col_inv transforms only u, v, zeta and q.
+constexpr int kNQ = 2;
+__host__ __device__ __forceinline__ long long q_off(int zb, int f, int y, int n, int KXP) {
+  return (((long long)zb * kNQ + f) * n + y) * KXP;
+}
 
 // ---------------------------------------------------------------------------
 // column helpers
@@ -202,7 +210,9 @@ template <typename T, int N>
 __global__ void __launch_bounds__(kColThreads, Tiles<T, N>::CIMINB)
 k_col_inv(Geom g, int zbase, const cplx<T>* __restrict__ psi, const cplx<T>* __restrict__ q,
           const cplx<T>* __restrict__ BR, const cplx<T>* __restrict__ BI, cplx<T>* __restrict__ S,
-          const cplx<T>* __restrict__ twg) {
+          const cplx<T>* __restrict__ twg, cplx<T>* __restrict__ Qb, int bmode) {
+  // bmode 0: all six transforms into S; 1: u, v, zeta, q into S (BR, BI are
+  // kept in Qb); 2: BR, BI into Qb only (before a step whose Qb is stale)
   constexpr int CT = Tiles<T, N>::CT, NT = kColThreads;
   constexpr int R0 = radix_of(N), NB0 = N / R0, NSL = LastNS<N>::value, RL = N / NSL;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -286,11 +296,23 @@ k_col_inv(Geom g, int zbase, const cplx<T>* __restrict__ psi, const cplx<T>* __r
           for (int r = 0; r < RL; ++r) S[scr_off(zb, f0 + f, j + r * NSL, N, g.KXP) + kx0 + c] = v[f][r];
       };
     };
-    col_fft<T, N, false, 2, CT, NT>(sm, tw, pro2(0), epi2(0));
-    __syncthreads();
-    col_fft<T, N, false, 2, CT, NT>(sm, tw, pro2(1), epi2(2));
-    __syncthreads();
-    col_fft<T, N, false, 2, CT, NT>(sm, tw, pro2(2), epi2(4));
+    auto epiq = [&](int c, int j, cplx<T> (&v)[2][RL]) {
+#pragma unroll
+      for (int f = 0; f < 2; ++f)
+#pragma unroll
+        for (int r = 0; r < RL; ++r) Qb[q_off(zb, f, j + r * NSL, N, g.KXP) + kx0 + c] = v[f][r];
+    };
+    if (bmode != 2) {
+      col_fft<T, N, false, 2, CT, NT>(sm, tw, pro2(0), epi2(0));
+      __syncthreads();
+      col_fft<T, N, false, 2, CT, NT>(sm, tw, pro2(1), epi2(2));
+    }
+    if (bmode == 0) {
+      __syncthreads();
+      col_fft<T, N, false, 2, CT, NT>(sm, tw, pro2(2), epi2(4));
+    } else if (bmode == 2) {
+      col_fft<T, N, false, 2, CT, NT>(sm, tw, pro2(2), epiq);
+    }
   } else {
     col_fft<T, N, false, 3, CT, NT>(sm, tw, pro_psi, epi(0));
     __syncthreads();
@@ -488,7 +510,11 @@ __device__ __forceinline__ void row_main_item(const Geom& g, const StepParams& s
 template <typename T, int N>
 __global__ void __launch_bounds__(kRowThreads, Tiles<T, N>::MMINB)
 k_row_main(Geom g, StepParams sp, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg, int nitems,
-           int* __restrict__ wflag) {
+           int* __restrict__ wflag, const cplx<T>* __restrict__ Qb) {
+  // planes 4, 5 (BR, BI) from the kept-B planes Qb when given
+  auto plane = [&](int zb, int f, int y) -> const cplx<T>* {
+    return (Qb && f >= 4) ? Qb + q_off(zb, f - 4, y, N, g.KXP) : S + scr_off(zb, f, y, N, g.KXP);
+  };
   constexpr int RT = Tiles<T, N>::RTM, LD = Tiles<T, N>::LD, NT = kRowThreads;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
@@ -504,7 +530,7 @@ k_row_main(Geom g, StepParams sp, cplx<T>* __restrict__ S, const cplx<T>* __rest
       const int zb = it / NGY, y0 = (it % NGY) * RT;
       mbar_expect_tx(bar, 6u * fb);
 #pragma unroll
-      for (int f = 0; f < 6; ++f) bulk_g2s(stg + f * RT * g.KXP, S + scr_off(zb, f, y0, N, g.KXP), fb, bar);
+      for (int f = 0; f < 6; ++f) bulk_g2s(stg + f * RT * g.KXP, plane(zb, f, y0), fb, bar);
     };
     if (threadIdx.x == 0) {
       mbar_init(bar, 1);
@@ -529,7 +555,7 @@ k_row_main(Geom g, StepParams sp, cplx<T>* __restrict__ S, const cplx<T>* __rest
   } else {
     const int zb = blockIdx.y, y0 = blockIdx.x * RT;
     row_main_item<T, N>(g, sp, S, tw, bA, zb, y0,
-                        [&](int f, int rr) -> const cplx<T>* { return S + scr_off(zb, f, y0 + rr, N, g.KXP); },
+                        [&](int f, int rr) -> const cplx<T>* { return plane(zb, f, y0 + rr); },
                         []() {});
   }
 }
@@ -587,7 +613,7 @@ template <typename T, int N>
 __global__ void __launch_bounds__(kColThreads, UpdLay<T, N>::MINB)
 k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict__ e1t, const T* __restrict__ e2t,
              const T* __restrict__ e1wt, const T* __restrict__ e2wt, cplx<T>* __restrict__ S,
-             const cplx<T>* __restrict__ twg, int qw_prep) {
+             const cplx<T>* __restrict__ twg, int qw_prep, cplx<T>* __restrict__ Qb) {
   using L = UpdLay<T, N>;
   constexpr int CT = Tiles<T, N>::CT, NT = kColThreads, FE = L::FE;
   constexpr int R0 = radix_of(N), NB0 = N / R0, NSL = LastNS<N>::value, RL = N / NSL;
@@ -779,13 +805,19 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
       }
     };
   };
+  // planes (BR, i ky BR, BI, i ky BI) = 0..3; with Qb, BR and BI go to the
+  // kept-B planes (Q 0 and 1) instead of S 0 and 2
   auto epi_store = [&](int f0, auto nf) {
     constexpr int NFQ = decltype(nf)::value;
     return [&, f0](int c, int j, cplx<T> (&v)[NFQ][RL]) {
 #pragma unroll
       for (int f = 0; f < NFQ; ++f)
 #pragma unroll
-        for (int r = 0; r < RL; ++r) S[scr_off(zb, f0 + f, j + r * NSL, N, g.KXP) + kx0 + c] = v[f][r];
+        for (int r = 0; r < RL; ++r) {
+          const int p = f0 + f, y = j + r * NSL;
+          cplx<T>* dst = (Qb && (p & 1) == 0) ? Qb + q_off(zb, p >> 1, y, N, g.KXP) : S + scr_off(zb, p, y, N, g.KXP);
+          dst[kx0 + c] = v[f][r];
+        }
     };
   };
   if constexpr (sizeof(T) == 4 && !L::LEAN) {
@@ -932,7 +964,12 @@ __device__ __forceinline__ void row_qw_item(const Geom& g, cplx<T>* __restrict__
 // k_row_main.
 template <typename T, int N>
 __global__ void __launch_bounds__(Tiles<T, N>::QTHREADS, Tiles<T, N>::QMINB)
-k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg, int nitems, int* __restrict__ wflag) {
+k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg, int nitems, int* __restrict__ wflag,
+         const cplx<T>* __restrict__ Qb) {
+  // planes 0, 2 (BR, BI) from the kept-B planes Qb when given
+  auto plane = [&](int zb, int f, int y) -> const cplx<T>* {
+    return (Qb && (f & 1) == 0) ? Qb + q_off(zb, f >> 1, y, N, g.KXP) : S + scr_off(zb, f, y, N, g.KXP);
+  };
   constexpr int RT = Tiles<T, N>::QRT, LD = Tiles<T, N>::LD, NT = Tiles<T, N>::QTHREADS;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
@@ -947,7 +984,7 @@ k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg, int n
       const int zb = it / NGY, y0 = (it % NGY) * RT;
       mbar_expect_tx(bar, 4u * fb);
 #pragma unroll
-      for (int f = 0; f < 4; ++f) bulk_g2s(stg + f * RT * g.KXP, S + scr_off(zb, f, y0, N, g.KXP), fb, bar);
+      for (int f = 0; f < 4; ++f) bulk_g2s(stg + f * RT * g.KXP, plane(zb, f, y0), fb, bar);
     };
     if (threadIdx.x == 0) {
       mbar_init(bar, 1);
@@ -971,7 +1008,7 @@ k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg, int n
   } else {
     const int zb = blockIdx.y, y0 = blockIdx.x * RT;
     row_qw_item<T, N>(g, S, tw, bA, zb, y0,
-                      [&](int f, int rr) -> const cplx<T>* { return S + scr_off(zb, f, y0 + rr, N, g.KXP); },
+                      [&](int f, int rr) -> const cplx<T>* { return plane(zb, f, y0 + rr); },
                       []() {});
   }
 }
@@ -1266,6 +1303,10 @@ constexpr int kSolveStBlocks = 128;  // k_solve_st: register target of 128/TC CT
 #define QG_QW_RESERVE 1
 #endif
 constexpr bool kSolveOverlap = QG_SOLVE_OVERLAP != 0;
+#ifndef QG_REUSE_B
+#define QG_REUSE_B 1
+#endif
+constexpr bool kReuseB = QG_REUSE_B != 0;   // kept y-inverse planes of B (q_off)
 // Phase-A batches are independent (z-local): with several batches per step,
 // up to kBatchLanes of them run at once on their own streams and scratch
 // slots, so that different kernels of different batches share the GPU and
