@@ -100,6 +100,22 @@ class Engine : public EngineBase {
     QG_CK(cudaMemcpy(tw, twh.data(), g.n * sizeof(C), cudaMemcpyHostToDevice));
     QG_CK(cudaMalloc(&tab_idx, g.plane * sizeof(int)));
     QG_CK(cudaMemcpy(tab_idx, t.tab_idx.data(), g.plane * sizeof(int), cudaMemcpyHostToDevice));
+    // columns of the solves: every column of the rectangle (any output
+    // array), and the retained ones only (the resident fields, whose other
+    // entries are zeros the solves need not rewrite)
+    {
+      std::vector<int> all(g.plane), ret;
+      for (long long m = 0; m < g.plane; ++m) {
+        all[m] = (int)m;
+        const int r = (int)(m / g.KXP), kx = (int)(m % g.KXP);
+        if (g.mask(kx, g.ky_of_row(r))) ret.push_back((int)m);
+      }
+      nret = (int)ret.size();
+      QG_CK(cudaMalloc(&cols_all, all.size() * sizeof(int)));
+      QG_CK(cudaMemcpy(cols_all, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice));
+      QG_CK(cudaMalloc(&cols_ret, ret.size() * sizeof(int)));
+      QG_CK(cudaMemcpy(cols_ret, ret.data(), ret.size() * sizeof(int), cudaMemcpyHostToDevice));
+    }
     const size_t fb = std::max<size_t>(1, (size_t)t.ndistinct * g.nseg) * sizeof(double4);
     QG_CK(cudaMalloc(&fac_psi, fb));
     QG_CK(cudaMalloc(&fac_A, fb));
@@ -170,11 +186,12 @@ class Engine : public EngineBase {
     // mixed path: per-column copies of the solve factors (coalesced reads);
     // without them the solves read the per-kh^2 tables
     if (kSolvePerColumn && sizeof(T) == 4 && vbuf) {
-      if (cudaMalloc(&pcfac, (size_t)6 * g.nseg * g.plane * sizeof(double)) != cudaSuccess) {
+      if (cudaMalloc(&pcfac, (size_t)6 * g.nseg * nret * sizeof(double)) != cudaSuccess) {
         pcfac = nullptr;
         (void)cudaGetLastError();
       } else {
-        k_expand_fac<<<grid_for((long long)g.nseg * g.plane), 256, 0, st>>>(g, tab_idx, fac_psi, fac_A, pcfac);
+        k_expand_fac<<<grid_for((long long)g.nseg * nret), 256, 0, st>>>(g, tab_idx, fac_psi, fac_A, pcfac,
+                                                                         cols_ret, nret);
         QG_LAUNCHED();
       }
     }
@@ -360,7 +377,7 @@ class Engine : public EngineBase {
     QG_CK(cudaMemcpyAsync(F[F_BIO] + off, F[F_BI] + off, (size_t)nz * lb, cudaMemcpyDeviceToDevice, st));
     if (!cfg.passive_scalar && cfg.ybj_plus) {   // regular YBJ keeps the A the host set
       int rc = solve_generic(nullptr, F[F_BR], F[F_BI], nullptr, F[F_AR], F[F_AI], 0, 1, st, z0 / g.nseg,
-                             nz / g.nseg);
+                             nz / g.nseg, true);
       if (rc) return rc;
     }
     QG_CK(cudaStreamSynchronize(st));
@@ -624,6 +641,9 @@ class Engine : public EngineBase {
   T *e1 = nullptr, *e2 = nullptr, *e1w = nullptr, *e2w = nullptr;
   C* tw = nullptr;
   int* tab_idx = nullptr;
+  int* cols_all = nullptr;   // 0 .. plane-1
+  int* cols_ret = nullptr;   // the retained columns (L = 1), ascending
+  int nret = 0;
   double4 *fac_psi = nullptr, *fac_A = nullptr;
   double* pcfac = nullptr;   // per-column solve factors of the mixed path (k_expand_fac), or null
   double* vbuf = nullptr;    // forward values of the column solves (k_solve_st)
@@ -671,7 +691,7 @@ class Engine : public EngineBase {
     if (st) cudaStreamSynchronize(st);
     for (auto& x : gexec) if (x) { cudaGraphExecDestroy(x); x = nullptr; }
     for (auto& p : F) if (p) { cudaFree(p); p = nullptr; }
-    void* ps[] = {e1, e2, e1w, e2w, tw, tab_idx, fac_psi, fac_A, pcfac, vbuf, du, cu, cl, r2, diag_part, diag_out, S, stage,
+    void* ps[] = {e1, e2, e1w, e2w, tw, tab_idx, cols_all, cols_ret, fac_psi, fac_A, pcfac, vbuf, du, cu, cl, r2, diag_part, diag_out, S, stage,
                   W, dstage, psi64, om_t1, om_du, om_dl, om_a, om_scr, sig[0], sig[1], mpar, Qp};
     for (void* p : ps) if (p) cudaFree(p);
     for (auto& p : D) if (p) cudaFree(p);
@@ -879,7 +899,8 @@ class Engine : public EngineBase {
           // B^{n+1} of every level is written: fork the A solves
           QG_CK(cudaEventRecord(ev_fork, bs));
           QG_CK(cudaStreamWaitEvent(st2, ev_fork, 0));
-          if (int rc0 = solve_generic(nullptr, F[F_BR], F[F_BI], nullptr, F[F_AR], F[F_AI], 0, 1, st2)) return rc0;
+          if (int rc0 = solve_generic(nullptr, F[F_BR], F[F_BI], nullptr, F[F_AR], F[F_AI], 0, 1, st2, 0, -1, true))
+            return rc0;
           QG_CK(cudaEventRecord(ev_join, st2));
         }
         if (need_qw) {
@@ -925,22 +946,27 @@ class Engine : public EngineBase {
   }
 
   int launch_solve(C* qs, int do_psi, int do_A) {
-    return solve_generic(qs, F[F_BR], F[F_BI], F[F_PSI], F[F_AR], F[F_AI], do_psi, do_A);
+    return solve_generic(qs, F[F_BR], F[F_BI], F[F_PSI], F[F_AR], F[F_AI], do_psi, do_A, nullptr, 0, -1, true);
   }
 
   // the column solves of segments [seg0, seg0 + nsegs) (nsegs < 0: all)
+  // retained: the outputs are resident fields (zeros off the retained
+  // modes already), so only the retained columns are solved
   int solve_generic(const C* qs, const C* br, const C* bi, C* psi, C* ar, C* ai, int do_psi, int do_A,
-                    cudaStream_t on = nullptr, int seg0 = 0, int nsegs = -1) {
+                    cudaStream_t on = nullptr, int seg0 = 0, int nsegs = -1, bool retained = false) {
     if (!do_psi && !do_A) return QG_OK;
     if (!on) on = st;
     if (nsegs < 0) nsegs = members - seg0;
+    const int* cl = retained ? cols_ret : cols_all;
+    const int ncl = retained ? nret : (int)g.plane;
+    double* const pcf = retained ? pcfac : nullptr;     // the per-column factors follow the retained list
     if (kSolveStore && vbuf) {
       const int nrec = (do_psi ? 2 : 0) + (do_A ? 4 : 0);   // recurrences per column
 #define QG_SOLVE_ST(TCV, PCV)                                                                              \
-  k_solve_st<T, TCV, PCV><<<dim3((unsigned)((g.plane + TCV - 1) / TCV), nsegs), nrec * TCV,             \
+  k_solve_st<T, TCV, PCV><<<dim3((unsigned)((ncl + TCV - 1) / TCV), nsegs), nrec * TCV,                 \
                             (size_t)g.nseg * 8, on>>>(                                                     \
-      g, cfg.dz, cfg.Bu, tab_idx, fac_psi, fac_A, du, qs, br, bi, psi, ar, ai, do_psi, do_A, vbuf, pcfac, seg0)
-      if (pcfac) {
+      g, cfg.dz, cfg.Bu, tab_idx, fac_psi, fac_A, du, qs, br, bi, psi, ar, ai, do_psi, do_A, vbuf, pcf, seg0, cl, ncl)
+      if (pcf) {
         if (solve_tc == 16) QG_SOLVE_ST(16, true);
         else if (solve_tc == 64) QG_SOLVE_ST(64, true);
         else QG_SOLVE_ST(32, true);

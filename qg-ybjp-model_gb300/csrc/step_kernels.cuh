@@ -1323,12 +1323,13 @@ constexpr int kQwReserve = QG_QW_RESERVE;
 // L = n3*P, operator o (0 psi, 1 A), q = 0: f_{i-1} (0 at i = 0),
 // 1: s/d'_i, 2: u_i/d'_i; zeros where the column holds no retained mode.
 static __global__ void k_expand_fac(Geom g, const int* __restrict__ tab_idx, const double4* __restrict__ fac_psi,
-                                    const double4* __restrict__ fac_A, double* __restrict__ pc) {
-  const long long P = g.plane, L = (long long)g.nseg * P;     // one segment's levels
+                                    const double4* __restrict__ fac_A, double* __restrict__ pc,
+                                    const int* __restrict__ cols, int ncols) {
+  const long long P = ncols, L = (long long)g.nseg * P;     // one segment's levels, listed columns
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < L; e += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(e / P);
     const long long m = e - (long long)i * P;
-    const int idx = tab_idx[m];
+    const int idx = tab_idx[cols[m]];
 #pragma unroll
     for (int o = 0; o < 2; ++o) {
       double f = 0.0, y = 0.0, z = 0.0;
@@ -1353,7 +1354,8 @@ k_solve_st(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
            const double4* __restrict__ fac_psi, const double4* __restrict__ fac_A, const double* __restrict__ du,
            const cplx<T>* __restrict__ qs, const cplx<T>* __restrict__ BR, const cplx<T>* __restrict__ BI,
            cplx<T>* __restrict__ psi, cplx<T>* __restrict__ AR, cplx<T>* __restrict__ AI,
-           int do_psi, int do_A, double* __restrict__ vbuf, const double* __restrict__ pc, int seg0) {
+           int do_psi, int do_A, double* __restrict__ vbuf, const double* __restrict__ pc, int seg0,
+           const int* __restrict__ cols, int ncols) {
   constexpr bool EXACT = sizeof(T) == 8;
   constexpr bool USEPC = PC && !EXACT;
   constexpr int S = kSegSt;
@@ -1367,10 +1369,12 @@ k_solve_st(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
   const int chain = (do_psi ? 0 : 2) + threadIdx.x / TC, c = threadIdx.x % TC;
   const int rhs_id = chain >> 1, part = chain & 1;
   if (rhs_id == 0 ? !do_psi : !do_A) return;
-  const long long m = (long long)blockIdx.x * TC + c;
-  if (m >= g.plane) return;
-  const int kx = (int)(m % g.KXP);
-  if (kx > g.K) return;
+  // thread column: entry li of the list of retained columns (cols), whose
+  // forward values and per-column factors are stored at li with a stride of
+  // ncols per level; the state fields at m with a stride of the plane
+  const long long li = (long long)blockIdx.x * TC + c;
+  if (li >= ncols) return;
+  const long long m = cols[li];
   const long long P = g.plane;
   const long long moff = (long long)(seg0 + blockIdx.y) * n3 * P;     // this segment's first level
   const T* rhs = reinterpret_cast<const T*>(rhs_id == 0 ? qs : (rhs_id == 1 ? BR : BI)) + part + 2 * moff;
@@ -1382,10 +1386,11 @@ k_solve_st(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
   }
   const double4* F = (rhs_id == 0 ? fac_psi : fac_A) + (long long)idx * n3;
   const double s = rhs_id == 0 ? __dmul_rn(dz, dz) : __dmul_rn(__dmul_rn(dz, dz), Bu);
-  double* vb = vbuf + (long long)chain * g.n3 * P + moff + m;
-  const long long L = (long long)n3 * P;          // per-column factors: one segment's levels
-  // (USEPC) f_{i-1}, s/d'_i, u_i/d'_i of this column at + q*L + i*P
-  const double* pcf = USEPC ? pc + (rhs_id == 0 ? 0 : 3) * L + m : nullptr;
+  const long long NL = ncols;
+  double* vb = vbuf + (long long)chain * g.n3 * NL + (long long)(seg0 + blockIdx.y) * n3 * NL + li;
+  const long long L = (long long)n3 * NL;         // per-column factors: one segment's levels
+  // (USEPC) f_{i-1}, s/d'_i, u_i/d'_i of this column at + q*L + i*NL
+  const double* pcf = USEPC ? pc + (rhs_id == 0 ? 0 : 3) * L + li : nullptr;
   auto fwd = [&](double x, double f, T r) -> double {
     return EXACT ? __dsub_rn(__dmul_rn(s, to64<T>(r)), __dmul_rn(f, x)) : fma(-f, x, to64<T>(r));
   };
@@ -1396,7 +1401,7 @@ k_solve_st(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
     for (int k = 0; k < S; ++k) {
       const int i = j * S + k;
       r[k] = i < n3 ? rhs[2 * (i * P + m)] : (T)0;
-      if constexpr (USEPC) f[k] = i < n3 ? pcf[(long long)i * P] : 0.0;
+      if constexpr (USEPC) f[k] = i < n3 ? pcf[(long long)i * NL] : 0.0;
       else f[k] = (i > 0 && i < n3) ? F[i - 1].x : 0.0;
     }
   };
@@ -1404,7 +1409,7 @@ k_solve_st(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
 #pragma unroll
     for (int k = 0; k < S; ++k) {
       const int i = j * S + k;
-      if (i < n3) { x = fwd(x, f[k], r[k]); vb[(long long)i * P] = x; }
+      if (i < n3) { x = fwd(x, f[k], r[k]); vb[(long long)i * NL] = x; }
     }
   };
   for (int j = 0; j < nseg; ++j) {
@@ -1419,10 +1424,10 @@ k_solve_st(Geom g, double dz, double Bu, const int* __restrict__ tab_idx,
 #pragma unroll
     for (int k = 0; k < S; ++k) {
       const int i = j * S + k;
-      v[k] = i < n3 ? vb[(long long)i * P] : 0.0;
+      v[k] = i < n3 ? vb[(long long)i * NL] : 0.0;
       if constexpr (USEPC) {
-        yk[k] = i < n3 ? pcf[L + (long long)i * P] : 1.0;
-        zk[k] = i < n3 ? pcf[2 * L + (long long)i * P] : 0.0;
+        yk[k] = i < n3 ? pcf[L + (long long)i * NL] : 1.0;
+        zk[k] = i < n3 ? pcf[2 * L + (long long)i * NL] : 0.0;
       } else {
         const double4 fl = i < n3 ? F[i] : make_double4(0, 1, 0, 0);
         yk[k] = fl.y;
