@@ -468,6 +468,8 @@ def workload(args):
         rc = scaled(rc, args.n or rc.n, args.n3 or rc.n3)
     if getattr(args, "levels_per_batch", 0):
         rc = dataclasses.replace(rc, levels_per_batch=args.levels_per_batch)
+    if getattr(args, "solve_columns", 0):
+        rc = dataclasses.replace(rc, solve_columns=args.solve_columns)
     return rc
 
 
@@ -772,6 +774,7 @@ def main(argv=None):
     ap.add_argument("--members", type=int, default=0, help="c3: first M ensemble members only")
     ap.add_argument("--ckpt", type=int, default=10, help="c4: checkpoint spacing of the adjoint")
     ap.add_argument("--levels-per-batch", type=int, default=0, help="override the phase-A batch depth")
+    ap.add_argument("--solve-columns", type=int, default=0, help="override the columns per CTA of the solves")
     args = ap.parse_args(argv)
     if args.steps is None:
         args.steps = 50 if args.config == "c4" else 300

@@ -872,7 +872,8 @@ class Engine : public EngineBase {
       cudaStream_t bs = lane == 0 ? st : lst[lane];
       C* Sb = S + lane * slot;
       QG_SWITCH_N(g.n, {
-        const dim3 gc(g.KXP / Tiles<T, NN>::CT, zc), gr(g.n / Tiles<T, NN>::QRT, zc),
+        // column tiles up to kx = K (the padding columns beyond K are never read)
+        const dim3 gc((g.K + Tiles<T, NN>::CT) / Tiles<T, NN>::CT, zc), gr(g.n / Tiles<T, NN>::QRT, zc),
             grm(g.n / Tiles<T, NN>::RTM, zc);
         if (int rc0 = pbeg(QG_K_COL_INV, bs)) return rc0;
         C* Qb = Qp ? Qp + (size_t)z0 * kNQ * g.n * g.KXP : nullptr;
@@ -993,7 +994,7 @@ class Engine : public EngineBase {
     for (int z0 = 0; z0 < g.n3; z0 += Zb) {
       const int zc = std::min(Zb, g.n3 - z0);
       QG_SWITCH_N(g.n, {
-        const dim3 gc(g.KXP / Tiles<T, NN>::CT, zc);
+        const dim3 gc((g.K + Tiles<T, NN>::CT) / Tiles<T, NN>::CT, zc);
         k_col_inv<T, NN><<<gc, kColThreads, sm_ci<NN>(3), st>>>(g, z0, F[F_PSI], F[F_Q], F[F_BR], F[F_BI], S, tw,
                                                                 Qp + (size_t)z0 * kNQ * g.n * g.KXP, 2);
         QG_LAUNCHED();
