@@ -715,6 +715,19 @@ def cpu_baseline_leg(rc, snapshots: dict):
     return base, vs
 
 
+def ensemble_cost(args, local) -> dict:
+    """The C3 ensemble (64 uneven members in one graph launch per step)
+    against the same members run one after another, as --config c3
+    measures it, with 10 timed steps."""
+    a = argparse.Namespace(**vars(args))
+    a.config, a.steps, a.warmup, a.members = "c3", 10, 3, 0
+    r = run_ensemble(a, 1, 0, local)
+    return {"value": r["value"], "unit": r["unit"], "ms_per_step": r["ms_per_step"],
+            "sequential_value": r["sequential_value"], "ensemble_over_sequential": r["ensemble_over_sequential"],
+            "workload": r["config"]["workload"], "sizes": r["config"]["sizes"], "steps": r["steps"],
+            "launches_per_step": sum(r["launches_per_step"].values()), "clocks": r["clocks"]}
+
+
 def adjoint_cost(args, local) -> dict:
     """The adjoint-to-forward cost on the C4 workload (128^2 x 64 FP64, J
     after 50 steps, checkpoints every 10), as --config c4 measures it."""
@@ -770,6 +783,7 @@ def main(argv=None):
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="c2: skip the adjoint/forward cost measurement")
+    ap.add_argument("--no-ensemble", action="store_true", help="c2: skip the ensemble-over-sequential measurement")
     ap.add_argument("--reference-budget-s", type=float, default=120.0)
     ap.add_argument("--members", type=int, default=0, help="c3: first M ensemble members only")
     ap.add_argument("--ckpt", type=int, default=10, help="c4: checkpoint spacing of the adjoint")
@@ -791,6 +805,8 @@ def main(argv=None):
         out, snapshots = run_ours(args, world, rank, local)
         if out is not None and world == 1 and not args.no_adjoint and args.config == "c2":
             out["adjoint"] = adjoint_cost(args, local)
+        if out is not None and world == 1 and not args.no_ensemble and args.config == "c2":
+            out["ensemble"] = ensemble_cost(args, local)
         if out is not None and world == 1 and not args.no_cpu_baseline:
             out["cpu_baseline"], vs_oracle = cpu_baseline_leg(workload(args), snapshots)
             if vs_oracle and out.get("parity") is not None:
