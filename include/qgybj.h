@@ -157,6 +157,15 @@ int qg_get_stream(qg_handle* h, void** stream);
 
 /* FP64 energy / enstrophy integrals of the resident state. */
 int qg_diagnostics_fp64(qg_handle* h, qg_energy* out);
+/* The same in two halves, for a host that reads them every step without
+ * stalling the run: _async queues the integrals of the state as it stands
+ * after the work queued so far (a step may follow at once: its first
+ * kernels, which only read the state, run beside the integrals, and its
+ * update waits for them); _wait blocks until they are done and returns them.
+ * One _async at a time per handle (QG_ERR_ARG while one is uncollected).
+ * Not for members of an ensemble stack. */
+int qg_diagnostics_fp64_async(qg_handle* h);
+int qg_diagnostics_fp64_wait(qg_handle* h, qg_energy* out);
 
 /* Kernel classes of one step, for qg_profile_step. */
 enum qg_kernel_class {

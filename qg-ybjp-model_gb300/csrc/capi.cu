@@ -371,6 +371,17 @@ int qg_diagnostics_fp64(qg_handle* h, qg_energy* out) {
   if (h->view) return fwd(h, h->eng->diagnostics_range(h->z0, h->nz, out));
   return fwd(h, h->eng->diagnostics(out));
 }
+int qg_diagnostics_fp64_async(qg_handle* h) {
+  QG_ENTRY(h);
+  QG_WHOLE(h);
+  return fwd(h, h->eng->diagnostics_async());
+}
+int qg_diagnostics_fp64_wait(qg_handle* h, qg_energy* out) {
+  QG_ENTRY(h);
+  QG_WHOLE(h);
+  if (!out) return fail(h, QG_ERR_ARG, "null output");
+  return fwd(h, h->eng->diagnostics_wait(out));
+}
 int qg_profile_step(qg_handle* h, int euler_first, double* ms, int* launches, int nclasses) {
   QG_ENTRY(h);
   QG_WHOLE(h);

@@ -60,6 +60,8 @@ struct EngineBase {
   virtual void* stream() = 0;
   virtual int diagnostics(qg_energy* out) = 0;
   virtual int diagnostics_range(int z0, int nz, qg_energy* out) = 0;
+  virtual int diagnostics_async() = 0;
+  virtual int diagnostics_wait(qg_energy* out) = 0;
   virtual int profile_step(int euler, double* ms, int* launches, int nclasses) = 0;
   // enqueue one step on the engine's stream without synchronising or graph
   // replay (used when an ensemble captures its members into one graph)

@@ -62,6 +62,7 @@ class Engine : public EngineBase {
     QG_CK(cudaStreamCreateWithPriority(&st2, cudaStreamNonBlocking, prio_low));
     QG_CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
     QG_CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+    QG_CK(cudaEventCreateWithFlags(&ev_diag, cudaEventDisableTiming));
     const size_t fbytes = (size_t)g.n3 * g.plane * sizeof(C);
     for (int f = 0; f < F_NINT; ++f) {
       if (f == F_DQ && !(cfg.inviscid == 0 && cfg.nuz != 0.0)) continue;
@@ -407,6 +408,44 @@ class Engine : public EngineBase {
 
   int diagnostics(qg_energy* out) override { return diagnostics_range(0, g.n3, out); }
 
+  // The integrals of the state as it stands after the work queued so far, on
+  // a stream of their own: the next step's first kernels (which only read
+  // the state) run beside them, and its update kernels wait for them in the
+  // graph (external event wait before each k_col_update).  diagnostics_wait
+  // returns the values.
+  int diagnostics_async() override {
+    if (!std_) {
+      int prio_low = 0, prio_high = 0;
+      QG_CK(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
+      QG_CK(cudaStreamCreateWithPriority(&std_, cudaStreamNonBlocking, prio_low));
+      QG_CK(cudaEventCreateWithFlags(&ev_state, cudaEventDisableTiming));
+      QG_CK(cudaMalloc(&diag_part_a, (size_t)g.n3 * kDiagChunks * kNDiag * sizeof(double)));
+      QG_CK(cudaMalloc(&diag_out_a, kNDiag * sizeof(double)));
+      QG_CK(cudaMallocHost(&diag_host_a, kNDiag * sizeof(double)));
+    }
+    if (diag_pending) { err = "the previous asynchronous diagnostics were not collected"; return QG_ERR_ARG; }
+    QG_CK(cudaEventRecord(ev_state, st));
+    QG_CK(cudaStreamWaitEvent(std_, ev_state, 0));
+    k_diag_level<T><<<dim3(kDiagChunks, g.n3), 256, 0, std_>>>(g, cfg.dz, cfg.Bu, r2, F[F_BR], F[F_BI], F[F_AR],
+                                                                F[F_AI], F[F_PSI], diag_part_a);
+    QG_LAUNCHED();
+    k_diag_sum<<<1, 32 * kNDiag, 0, std_>>>(0, g.n3, diag_part_a, diag_out_a);
+    QG_LAUNCHED();
+    QG_CK(cudaMemcpyAsync(diag_host_a, diag_out_a, kNDiag * sizeof(double), cudaMemcpyDeviceToHost, std_));
+    QG_CK(cudaEventRecord(ev_diag, std_));
+    diag_pending = true;
+    return QG_OK;
+  }
+
+  int diagnostics_wait(qg_energy* out) override {
+    if (!diag_pending) { err = "no asynchronous diagnostics pending"; return QG_ERR_ARG; }
+    QG_CK(cudaEventSynchronize(ev_diag));
+    diag_pending = false;
+    out->wke = diag_host_a[0]; out->wpe = diag_host_a[1]; out->wce = diag_host_a[2];
+    out->ke = diag_host_a[3]; out->pe = diag_host_a[4]; out->zeta2 = diag_host_a[5]; out->omegah2 = diag_host_a[6];
+    return QG_OK;
+  }
+
   // the integrals over levels [z0, z0 + nz): one run, or one member of a stack
   int diagnostics_range(int z0, int nz, qg_energy* out) override {
     k_diag_level<T><<<dim3(kDiagChunks, g.n3), 256, 0, st>>>(g, cfg.dz, cfg.Bu, r2, F[F_BR], F[F_BI], F[F_AR], F[F_AI], F[F_PSI], diag_part);
@@ -637,6 +676,12 @@ class Engine : public EngineBase {
   cudaStream_t st = nullptr;
   cudaStream_t st2 = nullptr;                          // the overlapped A solves
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;   // B^{n+1} ready / A solves done
+  // asynchronous diagnostics: their stream, state-ready and done events,
+  // their own buffers
+  cudaStream_t std_ = nullptr;
+  cudaEvent_t ev_state = nullptr, ev_diag = nullptr;
+  double *diag_part_a = nullptr, *diag_out_a = nullptr, *diag_host_a = nullptr;
+  bool diag_pending = false;
   C* F[F_NINT] = {};
   T *e1 = nullptr, *e2 = nullptr, *e1w = nullptr, *e2w = nullptr;
   C* tw = nullptr;
@@ -708,6 +753,12 @@ class Engine : public EngineBase {
       if (lev[i]) { cudaEventDestroy(lev[i]); lev[i] = nullptr; }
     }
     if (ev_start) { cudaEventDestroy(ev_start); ev_start = nullptr; }
+    if (std_) { cudaStreamSynchronize(std_); cudaStreamDestroy(std_); std_ = nullptr; }
+    if (ev_state) { cudaEventDestroy(ev_state); ev_state = nullptr; }
+    if (ev_diag) { cudaEventDestroy(ev_diag); ev_diag = nullptr; }
+    if (diag_part_a) { cudaFree(diag_part_a); diag_part_a = nullptr; }
+    if (diag_out_a) { cudaFree(diag_out_a); diag_out_a = nullptr; }
+    if (diag_host_a) { cudaFreeHost(diag_host_a); diag_host_a = nullptr; }
     if (st2) cudaStreamSynchronize(st2);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
@@ -891,6 +942,13 @@ class Engine : public EngineBase {
         }
         QG_LAUNCHED();
         if (int rc0 = pend(bs)) return rc0;
+        {
+          // asynchronous diagnostics of the previous state read B, A and psi:
+          // the update waits for them (an external event node when captured)
+          cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+          QG_CK(cudaStreamIsCapturing(bs, &cs));
+          QG_CK(cudaStreamWaitEvent(bs, ev_diag, cs == cudaStreamCaptureStatusActive ? cudaEventWaitExternal : 0));
+        }
         if (int rc0 = pbeg(QG_K_COL_UPDATE, bs)) return rc0;
         k_col_update<T, NN><<<gc, kColThreads, UpdLay<T, NN>::bytes(), bs>>>(g, s, z0, sptr, e1, e2, e1w, e2w, Sb, tw,
                                                                 need_qw ? 1 : 0, Qb);

@@ -29,6 +29,7 @@ EXPORTS = (
     "qg_adjoint_run", "qg_adjoint_step", "qg_dump_psi", "qg_dump_la",
     "qg_omega_eqn_rhs", "qg_omega_equation", "qg_omega", "qg_ensemble_set_lanes",
     "qg_selftest_conversions", "qg_selftest_wait", "qg_ensemble_profile_step",
+    "qg_diagnostics_fp64_async", "qg_diagnostics_fp64_wait",
 )
 KERNEL_CLASSES = ("dissipation", "col_inv", "row_main", "col_update", "row_qw", "col_qw", "solve", "solve_A")
 
@@ -104,6 +105,8 @@ def lib() -> C.CDLL:
         "qg_ensemble_destroy": (ip, [vp]),
         "qg_ensemble_last_error": (C.c_char_p, [vp]),
         "qg_ensemble_profile_step": (ip, [vp, ip, C.POINTER(C.c_double), C.POINTER(C.c_int), ip]),
+        "qg_diagnostics_fp64_async": (ip, [vp]),
+        "qg_diagnostics_fp64_wait": (ip, [vp, C.POINTER(QgEnergy)]),
         "qg_autotune": (ip, [C.POINTER(QgConfig), ip, C.POINTER(QgTuning)]),
         "qg_adjoint_run": (ip, [vp, vp, vp, vp, ip, ip, ip, dp, vp, vp, vp]),
         "qg_adjoint_step": (ip, [vp, ip, vp, vp, vp, vp]),

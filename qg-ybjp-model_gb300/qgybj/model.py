@@ -139,6 +139,16 @@ class Simulation:
         self._ck(lib().qg_diagnostics_fp64(self.h, C.byref(e)))
         return {k: getattr(e, k) for k, _ in QgEnergy._fields_}
 
+    def diagnostics_fp64_async(self):
+        """Queue the FP64 integrals of the current state (collect them with
+        diagnostics_fp64_wait; a step may be queued in between)."""
+        self._ck(lib().qg_diagnostics_fp64_async(self.h))
+
+    def diagnostics_fp64_wait(self) -> dict:
+        e = QgEnergy()
+        self._ck(lib().qg_diagnostics_fp64_wait(self.h, C.byref(e)))
+        return {k: getattr(e, k) for k, _ in QgEnergy._fields_}
+
     def profile_step(self, euler_first: bool = False) -> dict:
         """One step with CUDA events around each launch: {class: (ms, launches)}."""
         from ._lib import KERNEL_CLASSES

@@ -90,3 +90,34 @@ def test_blow_up_reports_nonfinite(precision):
     sim.steps_async(20, True)
     sim.synchronize()
     sim.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_async_diagnostics_pipelined_with_steps(precision):
+    """qg_diagnostics_fp64_async followed at once by a step: the integrals
+    are those of the state before the step, and the step is not disturbed
+    (bitwise against synchronous diagnostics and an undisturbed run)."""
+    a, ic = _sim(precision)
+    b, _ = _sim(precision)
+    _init(a, ic)
+    _init(b, ic)
+    a.steps_async(3, True)
+    b.steps_async(3, True)
+    ref = [b.diagnostics_fp64()]
+    a.diagnostics_fp64_async()
+    a.step(False)
+    got = [a.diagnostics_fp64_wait()]
+    for _ in range(3):
+        a.diagnostics_fp64_async()
+        a.step(False)
+        got.append(a.diagnostics_fp64_wait())
+    for _ in range(4):
+        b.step(False)
+        ref.append(b.diagnostics_fp64())
+    assert got == ref[:4]
+    for f in ("q", "psi", "BR", "BI", "AR", "AI"):
+        assert np.array_equal(a.get_state(f), b.get_state(f)), f
+    with pytest.raises(QgError):
+        a.diagnostics_fp64_wait()          # nothing pending
+    a.close()
+    b.close()
