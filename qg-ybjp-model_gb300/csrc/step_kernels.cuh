@@ -1650,20 +1650,17 @@ __global__ void k_ybj_A(Geom g, double dz, double Bu, double Ro, const double* _
 // ===========================================================================
 constexpr int kNDiag = 7;
 constexpr int kDiagChunks = 32;    // CTAs per level: the level's modes in 32 contiguous ranges
+
+// The seven sums of one thread's modes m0 + tid, m0 + tid + stride, ... < m1
+// of level z, in FP64 arithmetic (before the per-level constant factors).
 template <typename T>
-__global__ void __launch_bounds__(256)
-k_diag_level(Geom g, double dz, double Bu, const double* __restrict__ r2, const cplx<T>* __restrict__ BR,
-             const cplx<T>* __restrict__ BI, const cplx<T>* __restrict__ AR, const cplx<T>* __restrict__ AI,
-             const cplx<T>* __restrict__ psi, double* __restrict__ part) {
-  __shared__ double red[kNDiag][256];
-  const int z = blockIdx.y, chunk = blockIdx.x;
-  const long long zo = (long long)z * g.plane;
-  const long long per = (g.plane + kDiagChunks - 1) / kDiagChunks;
-  const long long m0 = chunk * per, m1 = m0 + per < g.plane ? m0 + per : g.plane;
-  const bool top = (z % g.nseg == g.nseg - 1);     // top level of its segment
-  const double rz = r2[z % g.nseg];
-  double acc[kNDiag] = {0, 0, 0, 0, 0, 0, 0};
-  for (long long m = m0 + threadIdx.x; m < m1; m += blockDim.x) {
+__device__ __forceinline__ void diag_modes_fp64(const Geom& g, long long zo, bool top, long long m0, long long m1,
+                                                int stride, const cplx<T>* __restrict__ BR,
+                                                const cplx<T>* __restrict__ BI, const cplx<T>* __restrict__ AR,
+                                                const cplx<T>* __restrict__ AI, const cplx<T>* __restrict__ psi,
+                                                double acc[kNDiag]) {
+  for (int k = 0; k < kNDiag; ++k) acc[k] = 0.0;
+  for (long long m = m0; m < m1; m += stride) {
     const int mi = (int)m, r = mi / g.KXP, kx = mi - r * g.KXP;
     const int ky = g.ky_of_row(r);
     if (!g.mask(kx, ky)) continue;
@@ -1679,7 +1676,7 @@ k_diag_level(Geom g, double dz, double Bu, const double* __restrict__ r2, const 
     acc[0] += w00 * b2;
     double c2 = 0.0, pz2 = 0.0;
     if (!top) {
-      // C = A_z and b ~ psi_z: differences (f(z+1) - f(z)), scaled by 1/dz^2 below
+      // C = A_z and b ~ psi_z: differences (f(z+1) - f(z)), scaled by 1/dz^2 later
       const cplx<T> ar1 = AR[zo + g.plane + m], ai1 = AI[zo + g.plane + m], p1 = psi[zo + g.plane + m];
       const double crx = to64<T>(ar1.x) - arx, cry = to64<T>(ar1.y) - ary;
       const double cix = to64<T>(ai1.x) - aix, ciy = to64<T>(ai1.y) - aiy;
@@ -1695,6 +1692,137 @@ k_diag_level(Geom g, double dz, double Bu, const double* __restrict__ r2, const 
     acc[4] += w00 * pz2;
     acc[5] += kh2 * t;
     acc[6] += kh2 * pz2;
+  }
+}
+
+// --- FP32-pair ("double-float") arithmetic for the FP32 state --------------
+// A pair (h, l) stands for the real number h + l.  GB300 issues FP32 at many
+// times its FP64 rate, and every FP32 product x*y is exactly p + e with
+// p = fl(x*y), e = fma(x, y, -p); two FP32 numbers add exactly into s + t
+// (Knuth's TwoSum, 6 additions).  With these error-free transformations the
+// sums of squares of FP32 values below are FP64-grade (about 2^-44 relative
+// per sum) on the FP32 pipes.
+struct f2 { float h, l; };
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& t) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  t = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// x0^2 + x1^2 (+ x2^2 + x3^2): every square exact as p + e, the p's added
+// with TwoSum, the e's and the TwoSum remainders in the low word
+__device__ __forceinline__ f2 f2_sq2(float a, float b) {
+  const float pa = __fmul_rn(a, a), ea = __fmaf_rn(a, a, -pa);
+  const float pb = __fmul_rn(b, b), eb = __fmaf_rn(b, b, -pb);
+  f2 r;
+  float t;
+  two_sum(pa, pb, r.h, t);
+  r.l = __fadd_rn(__fadd_rn(ea, eb), t);
+  return r;
+}
+__device__ __forceinline__ f2 f2_add(f2 a, f2 b) {
+  f2 r;
+  float t;
+  two_sum(a.h, b.h, r.h, t);
+  r.l = __fadd_rn(__fadd_rn(a.l, b.l), t);
+  return r;
+}
+// (a1 - a0)^2 + (b1 - b0)^2 for FP32 pairs of values: each difference exact
+// as d + err (TwoSum), its square as p + e + 2 d err (err^2 <= 2^-48 d^2 is
+// dropped)
+__device__ __forceinline__ f2 f2_dsq2(float a1, float a0, float b1, float b0) {
+  float da, ra, db, rb;
+  two_sum(a1, -a0, da, ra);
+  two_sum(b1, -b0, db, rb);
+  const float pa = __fmul_rn(da, da), ea = __fmaf_rn(__fmul_rn(2.0f, da), ra, __fmaf_rn(da, da, -pa));
+  const float pb = __fmul_rn(db, db), eb = __fmaf_rn(__fmul_rn(2.0f, db), rb, __fmaf_rn(db, db, -pb));
+  f2 r;
+  float t;
+  two_sum(pa, pb, r.h, t);
+  r.l = __fadd_rn(__fadd_rn(ea, eb), t);
+  return r;
+}
+// w * (h + l) for an FP32 weight w: w*h exact as q + r, w*l rounded
+__device__ __forceinline__ f2 f2_scale(float w, f2 a) {
+  f2 r;
+  r.h = __fmul_rn(w, a.h);
+  r.l = __fmaf_rn(w, a.l, __fmaf_rn(w, a.h, -r.h));
+  return r;
+}
+// accumulator += a, then renormalised so that |l| <= ulp(h)/2 (Fast2Sum)
+__device__ __forceinline__ void f2_acc(f2& s, f2 a) {
+  float h, t;
+  two_sum(s.h, a.h, h, t);
+  const float l = __fadd_rn(__fadd_rn(s.l, a.l), t);
+  s.h = __fadd_rn(h, l);
+  s.l = __fsub_rn(l, __fsub_rn(s.h, h));
+}
+
+// The seven sums of the FP32 state in FP32-pair arithmetic.  kh2 = kx^2 +
+// ky^2 < 2^24 is exact in FP32 and kh2^2 is applied as two exact scalings.
+// Error per sum: about 2^-44 of the sum (TwoSum accumulation, the rounded
+// w*l terms and the dropped err^2), plus at most 2^-100 absolute per mode
+// for values below 2^-50, whose square's low word underflows.  Returns false
+// when a pair is not finite (values beyond ~2^60 overflow FP32 squares); the
+// caller then recomputes the thread's sums in FP64.
+__device__ __forceinline__ bool diag_modes_f2(const Geom& g, long long zo, bool top, long long m0, long long m1,
+                                              int stride, const cplx<float>* __restrict__ BR,
+                                              const cplx<float>* __restrict__ BI,
+                                              const cplx<float>* __restrict__ AR,
+                                              const cplx<float>* __restrict__ AI,
+                                              const cplx<float>* __restrict__ psi, double acc[kNDiag]) {
+  f2 s[kNDiag];
+  for (int k = 0; k < kNDiag; ++k) s[k] = f2{0.0f, 0.0f};
+  for (long long m = m0; m < m1; m += stride) {
+    const int mi = (int)m, r = mi / g.KXP, kx = mi - r * g.KXP;
+    const int ky = g.ky_of_row(r);
+    if (!g.mask(kx, ky)) continue;
+    const float kh2 = (float)(kx * kx + ky * ky);      // exact: < 2^24
+    const float w00 = (kx == 0 && ky == 0) ? 0.5f : 1.0f;
+    const cplx<float> brc = BR[zo + m], bic = BI[zo + m], arc = AR[zo + m], aic = AI[zo + m], pc = psi[zo + m];
+    const f2 b2 = f2_add(f2_sq2(brc.x, brc.y), f2_sq2(bic.x, bic.y));
+    const f2 a2 = f2_add(f2_sq2(arc.x, arc.y), f2_sq2(aic.x, aic.y));
+    const f2 p2 = f2_sq2(pc.x, pc.y);
+    f2 c2{0.0f, 0.0f}, pz2{0.0f, 0.0f};
+    if (!top) {
+      const cplx<float> ar1 = AR[zo + g.plane + m], ai1 = AI[zo + g.plane + m], p1 = psi[zo + g.plane + m];
+      c2 = f2_add(f2_dsq2(ar1.x, arc.x, ar1.y, arc.y), f2_dsq2(ai1.x, aic.x, ai1.y, aic.y));
+      pz2 = f2_dsq2(p1.x, pc.x, p1.y, pc.y);
+    }
+    const f2 t = f2_scale(kh2, p2);
+    f2_acc(s[0], f2_scale(w00, b2));
+    f2_acc(s[1], f2_scale(kh2, c2));
+    f2_acc(s[2], f2_scale(kh2, f2_scale(kh2, a2)));
+    f2_acc(s[3], t);
+    f2_acc(s[4], f2_scale(w00, pz2));
+    f2_acc(s[5], f2_scale(kh2, t));
+    f2_acc(s[6], f2_scale(kh2, pz2));
+  }
+  bool ok = true;
+  for (int k = 0; k < kNDiag; ++k) {
+    ok = ok && fabsf(s[k].h) <= 3.0e38f && fabsf(s[k].l) <= 3.0e38f;     // false for inf and NaN
+    acc[k] = f32_to_f64(s[k].h) + f32_to_f64(s[k].l);
+  }
+  return ok;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_diag_level(Geom g, double dz, double Bu, const double* __restrict__ r2, const cplx<T>* __restrict__ BR,
+             const cplx<T>* __restrict__ BI, const cplx<T>* __restrict__ AR, const cplx<T>* __restrict__ AI,
+             const cplx<T>* __restrict__ psi, double* __restrict__ part) {
+  __shared__ double red[kNDiag][256];
+  const int z = blockIdx.y, chunk = blockIdx.x;
+  const long long zo = (long long)z * g.plane;
+  const long long per = (g.plane + kDiagChunks - 1) / kDiagChunks;
+  const long long m0 = chunk * per, m1 = m0 + per < g.plane ? m0 + per : g.plane;
+  const bool top = (z % g.nseg == g.nseg - 1);     // top level of its segment
+  const double rz = r2[z % g.nseg];
+  double acc[kNDiag];
+  if constexpr (std::is_same<T, float>::value) {
+    if (!diag_modes_f2(g, zo, top, m0 + threadIdx.x, m1, blockDim.x, BR, BI, AR, AI, psi, acc))
+      diag_modes_fp64<T>(g, zo, top, m0 + threadIdx.x, m1, blockDim.x, BR, BI, AR, AI, psi, acc);
+  } else {
+    diag_modes_fp64<T>(g, zo, top, m0 + threadIdx.x, m1, blockDim.x, BR, BI, AR, AI, psi, acc);
   }
   // constant factors of each sum (per level)
   {

@@ -130,6 +130,41 @@ def test_steps_small(precision):
     sim.close()
 
 
+@pytest.mark.parametrize("scale", [1.0, 1e25, 1e-30])
+def test_mixed_diagnostics_are_fp64_sums_of_the_fp32_state(scale):
+    """The mixed engine forms the seven diagnostic sums of its FP32 state in
+    FP32-pair arithmetic (exact products, TwoSum accumulation) and
+    recomputes a thread's sums in FP64 where a pair overflows.  They equal
+    the FP64 sums of that same FP32 state within 1e-12 relative, plus an
+    absolute 2^-100 per mode for values whose squares underflow FP32.
+    Scale 1e25: squares overflow FP32 and the FP64 recomputation runs;
+    1e-30: squares underflow and only the absolute bound holds."""
+    rc = scaled(CONFIGS["c1"], 64, 16)
+    model, st, sim = pair(rc, "mixed")
+    sim.step(True)
+    sim.step()
+    sim.step()
+    s = st.copy()
+    for f in ("psi", "BR", "BI", "AR", "AI"):
+        v = sim.get_state(f)
+        if scale != 1.0:
+            sim.set_state(f, v * scale)
+            v = sim.get_state(f)                  # the FP32-rounded values
+        setattr(s, f, v)
+    for c, a in (("CR", "AR"), ("CI", "AI")):
+        A = getattr(s, a)
+        C = np.zeros_like(A)
+        C[:-1] = (A[1:] - A[:-1]) / model.p.dz
+        setattr(s, c, C)
+    exp = model.diagnostics(s)
+    got = sim.diagnostics_fp64()
+    nmodes = s.psi.size
+    for k, v in exp.items():
+        assert np.isfinite(got[k]), k
+        assert abs(got[k] - v) <= 1e-12 * abs(v) + nmodes * 2.0 ** -100, (k, got[k], v)
+    sim.close()
+
+
 @pytest.mark.parametrize("n", [128, 256, 512])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_steps_each_row_kernel_path(precision, n):
