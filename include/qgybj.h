@@ -155,7 +155,11 @@ int qg_selftest_wait(qg_handle* h);
 /* The handle's cudaStream_t (as void*) for event timing by the host. */
 int qg_get_stream(qg_handle* h, void** stream);
 
-/* FP64 energy / enstrophy integrals of the resident state. */
+/* FP64 energy / enstrophy integrals of the resident state.  FP64 handles sum
+ * in FP64.  Mixed handles (FP32 state) form the sums of squares in FP32-pair
+ * arithmetic (exact products, TwoSum accumulation; a thread whose FP32 pairs
+ * overflow recomputes in FP64): within ~2^-40 of the FP64 sums of the same
+ * FP32 values, plus 2^-100 absolute per mode where squares underflow FP32. */
 int qg_diagnostics_fp64(qg_handle* h, qg_energy* out);
 /* The same in two halves, for a host that reads them every step without
  * stalling the run: _async queues the integrals of the state as it stands

@@ -130,7 +130,26 @@ class Engine : public EngineBase {
       return QG_OK;
     };
     if ((rc = upd(&du, t.du)) || (rc = upd(&cu, t.cu)) || (rc = upd(&cl, t.cl)) || (rc = upd(&r2, t.r2))) return rc;
-    QG_CK(cudaMalloc(&diag_part, (size_t)g.n3 * kDiagChunks * kNDiag * sizeof(double)));
+    {
+      // per-level weights of the diagnostics' vertical-difference sums:
+      // w1 = 0.5/(r2 Bu dz^2) (wpe), w4 = Bu/(r2 dz^2) (pe), in FP64 and as
+      // FP32 pairs (h, l) with h + l = w to ~2^-48
+      std::vector<double> wv(2 * (size_t)g.nseg);
+      std::vector<float2> wf(2 * (size_t)g.nseg);
+      const double inv_dz2 = 1.0 / (cfg.dz * cfg.dz);
+      for (int i = 0; i < g.nseg; ++i) {
+        wv[i] = (0.5 / (t.r2[i] * cfg.Bu)) * inv_dz2;
+        wv[g.nseg + i] = (cfg.Bu / t.r2[i]) * inv_dz2;
+      }
+      for (size_t i = 0; i < wv.size(); ++i) {
+        const float h = (float)wv[i];
+        wf[i] = make_float2(h, (float)(wv[i] - (double)h));
+      }
+      if ((rc = upd(&dwz, wv))) return rc;
+      QG_CK(cudaMalloc(&fwz, wf.size() * sizeof(float2)));
+      QG_CK(cudaMemcpy(fwz, wf.data(), wf.size() * sizeof(float2), cudaMemcpyHostToDevice));
+    }
+    QG_CK(cudaMalloc(&diag_part, diag_parts(g.n3 / g.nseg) * kNDiag * sizeof(double)));
     QG_CK(cudaMalloc(&diag_out, kNDiag * sizeof(double)));
     QG_CK(cudaMallocHost(&diag_host, kNDiag * sizeof(double)));
     QG_CK(cudaHostAlloc(&wflag_h, 3 * sizeof(int), cudaHostAllocMapped));
@@ -408,6 +427,22 @@ class Engine : public EngineBase {
 
   int diagnostics(qg_energy* out) override { return diagnostics_range(0, g.n3, out); }
 
+  // partials of k_diag_cols over nsegs whole segments
+  size_t diag_parts(int nsegs) const {
+    return (size_t)((nret + kDiagThreads - 1) / kDiagThreads) * ((g.nseg + kDiagZC - 1) / kDiagZC) * nsegs;
+  }
+  // the seven integrals of segments [seg0, seg0 + nsegs) into out (device)
+  int launch_diag(int seg0, int nsegs, double* part, double* out, cudaStream_t s) {
+    const dim3 grid((nret + kDiagThreads - 1) / kDiagThreads, (g.nseg + kDiagZC - 1) / kDiagZC, nsegs);
+    const double c2 = (1.0 / 8.0) * (1.0 / (cfg.Bu * cfg.Bu)), c6 = 2.0 * (1.0 / (cfg.dz * cfg.dz));
+    k_diag_cols<T><<<grid, kDiagThreads, 0, s>>>(g, seg0, dwz, fwz, c2, c6, F[F_BR], F[F_BI], F[F_AR], F[F_AI],
+                                                 F[F_PSI], cols_ret, nret, part);
+    QG_LAUNCHED();
+    k_diag_sum<<<1, 32 * kNDiag, 0, s>>>((long long)diag_parts(nsegs), nsegs * g.nseg, part, out);
+    QG_LAUNCHED();
+    return QG_OK;
+  }
+
   // The integrals of the state as it stands after the work queued so far, on
   // a stream of their own: the next step's first kernels (which only read
   // the state) run beside them, and its update kernels wait for them in the
@@ -419,18 +454,14 @@ class Engine : public EngineBase {
       QG_CK(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
       QG_CK(cudaStreamCreateWithPriority(&std_, cudaStreamNonBlocking, prio_low));
       QG_CK(cudaEventCreateWithFlags(&ev_state, cudaEventDisableTiming));
-      QG_CK(cudaMalloc(&diag_part_a, (size_t)g.n3 * kDiagChunks * kNDiag * sizeof(double)));
+      QG_CK(cudaMalloc(&diag_part_a, diag_parts(g.n3 / g.nseg) * kNDiag * sizeof(double)));
       QG_CK(cudaMalloc(&diag_out_a, kNDiag * sizeof(double)));
       QG_CK(cudaMallocHost(&diag_host_a, kNDiag * sizeof(double)));
     }
     if (diag_pending) { err = "the previous asynchronous diagnostics were not collected"; return QG_ERR_ARG; }
     QG_CK(cudaEventRecord(ev_state, st));
     QG_CK(cudaStreamWaitEvent(std_, ev_state, 0));
-    k_diag_level<T><<<dim3(kDiagChunks, g.n3), 256, 0, std_>>>(g, cfg.dz, cfg.Bu, r2, F[F_BR], F[F_BI], F[F_AR],
-                                                                F[F_AI], F[F_PSI], diag_part_a);
-    QG_LAUNCHED();
-    k_diag_sum<<<1, 32 * kNDiag, 0, std_>>>(0, g.n3, diag_part_a, diag_out_a);
-    QG_LAUNCHED();
+    if (int rc = launch_diag(0, g.n3 / g.nseg, diag_part_a, diag_out_a, std_)) return rc;
     QG_CK(cudaMemcpyAsync(diag_host_a, diag_out_a, kNDiag * sizeof(double), cudaMemcpyDeviceToHost, std_));
     QG_CK(cudaEventRecord(ev_diag, std_));
     diag_pending = true;
@@ -448,10 +479,8 @@ class Engine : public EngineBase {
 
   // the integrals over levels [z0, z0 + nz): one run, or one member of a stack
   int diagnostics_range(int z0, int nz, qg_energy* out) override {
-    k_diag_level<T><<<dim3(kDiagChunks, g.n3), 256, 0, st>>>(g, cfg.dz, cfg.Bu, r2, F[F_BR], F[F_BI], F[F_AR], F[F_AI], F[F_PSI], diag_part);
-    QG_LAUNCHED();
-    k_diag_sum<<<1, 32 * kNDiag, 0, st>>>(z0, nz, diag_part, diag_out);
-    QG_LAUNCHED();
+    if (z0 % g.nseg || nz % g.nseg || nz <= 0) { err = "diagnostics range is not a set of whole segments"; return QG_ERR_ARG; }
+    if (int rc = launch_diag(z0 / g.nseg, nz / g.nseg, diag_part, diag_out, st)) return rc;
     QG_CK(cudaMemcpyAsync(diag_host, diag_out, kNDiag * sizeof(double), cudaMemcpyDeviceToHost, st));
     QG_CK(cudaStreamSynchronize(st));
     out->wke = diag_host[0]; out->wpe = diag_host[1]; out->wce = diag_host[2];
@@ -695,6 +724,8 @@ class Engine : public EngineBase {
   int solve_tc = 32;         // columns per CTA of k_solve_st
   double *du = nullptr, *cu = nullptr, *cl = nullptr, *r2 = nullptr;
   double *diag_part = nullptr, *diag_out = nullptr, *diag_host = nullptr;
+  double* dwz = nullptr;     // diagnostics' per-level weights (w1, w4), FP64
+  float2* fwz = nullptr;     // the same as FP32 pairs
   // set by a kernel whose bounded wait expired (mapped page-locked word)
   // mapped page-locked words raised on the device: [0] a bounded wait
   // expired, [1] a step produced a non-finite q*, [2] qg_set_state's input
@@ -736,7 +767,7 @@ class Engine : public EngineBase {
     if (st) cudaStreamSynchronize(st);
     for (auto& x : gexec) if (x) { cudaGraphExecDestroy(x); x = nullptr; }
     for (auto& p : F) if (p) { cudaFree(p); p = nullptr; }
-    void* ps[] = {e1, e2, e1w, e2w, tw, tab_idx, cols_all, cols_ret, fac_psi, fac_A, pcfac, vbuf, du, cu, cl, r2, diag_part, diag_out, S, stage,
+    void* ps[] = {e1, e2, e1w, e2w, tw, tab_idx, cols_all, cols_ret, fac_psi, fac_A, pcfac, vbuf, du, cu, cl, r2, diag_part, diag_out, dwz, fwz, S, stage,
                   W, dstage, psi64, om_t1, om_du, om_dl, om_a, om_scr, sig[0], sig[1], mpar, Qp};
     for (void* p : ps) if (p) cudaFree(p);
     for (auto& p : D) if (p) cudaFree(p);

@@ -1646,54 +1646,25 @@ __global__ void k_ybj_A(Geom g, double dz, double Bu, double Ro, const double* _
 }
 
 // ===========================================================================
-// FP64 diagnostics: per-level partial sums, then a fixed-order vertical sum
+// FP64 diagnostics (diagnostics.f90: wave_energy 647-743, the rotational part
+// of diag_zentrum 16-211, enstrophy 1262-1363): column partial sums, then a
+// fixed-order sum of the partials
 // ===========================================================================
+// A thread owns one retained column (kx, ky) and walks a chunk of up to
+// kDiagZC levels of one vertical segment, loading each level's B, A and psi
+// once (the level above is the next iteration's level) and accumulating six
+// column sums: |B|^2, w1_z |A(z+1)-A(z)|^2, |A|^2, |psi|^2,
+// w4_z |psi(z+1)-psi(z)|^2 and |psi(z+1)-psi(z)|^2, with the per-level
+// weights w1_z = 0.5/(r2_z Bu dz^2), w4_z = Bu/(r2_z dz^2) (the difference
+// terms vanish on a segment's top level).  The column's factors (kh^2,
+// kh^4, the half weight of the (0,0) mode) multiply the sums once, in FP64,
+// giving the seven integrals:
+//   wke = w00 S_b, wpe = kh^2 S_w1c, wce = kh^4 S_a / (8 Bu^2), ke = kh^2 S_p,
+//   pe = w00 S_w4b, zeta2 = 2 kh^4 S_p, omegah2 = 2 kh^2 S_b' / dz^2.
 constexpr int kNDiag = 7;
-constexpr int kDiagChunks = 32;    // CTAs per level: the level's modes in 32 contiguous ranges
-
-// The seven sums of one thread's modes m0 + tid, m0 + tid + stride, ... < m1
-// of level z, in FP64 arithmetic (before the per-level constant factors).
-template <typename T>
-__device__ __forceinline__ void diag_modes_fp64(const Geom& g, long long zo, bool top, long long m0, long long m1,
-                                                int stride, const cplx<T>* __restrict__ BR,
-                                                const cplx<T>* __restrict__ BI, const cplx<T>* __restrict__ AR,
-                                                const cplx<T>* __restrict__ AI, const cplx<T>* __restrict__ psi,
-                                                double acc[kNDiag]) {
-  for (int k = 0; k < kNDiag; ++k) acc[k] = 0.0;
-  for (long long m = m0; m < m1; m += stride) {
-    const int mi = (int)m, r = mi / g.KXP, kx = mi - r * g.KXP;
-    const int ky = g.ky_of_row(r);
-    if (!g.mask(kx, ky)) continue;
-    // exact int -> double without a conversion instruction: (2^52 + k) - 2^52
-    const double kh2 = __hiloint2double(0x43300000, kx * kx + ky * ky) - 4503599627370496.0;
-    const double w00 = (kx == 0 && ky == 0) ? 0.5 : 1.0;
-    // widen once per value (exact; FP32 inputs convert with integer operations)
-    const cplx<T> brc = BR[zo + m], bic = BI[zo + m], arc = AR[zo + m], aic = AI[zo + m], pc = psi[zo + m];
-    const double brx = to64<T>(brc.x), bry = to64<T>(brc.y), bix = to64<T>(bic.x), biy = to64<T>(bic.y);
-    const double arx = to64<T>(arc.x), ary = to64<T>(arc.y), aix = to64<T>(aic.x), aiy = to64<T>(aic.y);
-    const double px = to64<T>(pc.x), py = to64<T>(pc.y);
-    const double b2 = brx * brx + bry * bry + bix * bix + biy * biy;
-    acc[0] += w00 * b2;
-    double c2 = 0.0, pz2 = 0.0;
-    if (!top) {
-      // C = A_z and b ~ psi_z: differences (f(z+1) - f(z)), scaled by 1/dz^2 later
-      const cplx<T> ar1 = AR[zo + g.plane + m], ai1 = AI[zo + g.plane + m], p1 = psi[zo + g.plane + m];
-      const double crx = to64<T>(ar1.x) - arx, cry = to64<T>(ar1.y) - ary;
-      const double cix = to64<T>(ai1.x) - aix, ciy = to64<T>(ai1.y) - aiy;
-      c2 = crx * crx + cry * cry + cix * cix + ciy * ciy;
-      const double bx = to64<T>(p1.x) - px, by = to64<T>(p1.y) - py;
-      pz2 = bx * bx + by * by;
-    }
-    acc[1] += kh2 * c2;
-    const double a2 = arx * arx + ary * ary + aix * aix + aiy * aiy;
-    acc[2] += (kh2 * kh2) * a2;
-    const double t = kh2 * (px * px + py * py);
-    acc[3] += t;
-    acc[4] += w00 * pz2;
-    acc[5] += kh2 * t;
-    acc[6] += kh2 * pz2;
-  }
-}
+constexpr int kDiagSums = 6;
+constexpr int kDiagZC = 64;        // levels per chunk
+constexpr int kDiagThreads = 128;  // columns per CTA
 
 // --- FP32-pair ("double-float") arithmetic for the FP32 state --------------
 // A pair (h, l) stands for the real number h + l.  GB300 issues FP32 at many
@@ -1708,8 +1679,8 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& t) {
   const float bb = __fsub_rn(s, a);
   t = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
-// x0^2 + x1^2 (+ x2^2 + x3^2): every square exact as p + e, the p's added
-// with TwoSum, the e's and the TwoSum remainders in the low word
+// x0^2 + x1^2: every square exact as p + e, the p's added with TwoSum, the
+// e's and the TwoSum remainder in the low word
 __device__ __forceinline__ f2 f2_sq2(float a, float b) {
   const float pa = __fmul_rn(a, a), ea = __fmaf_rn(a, a, -pa);
   const float pb = __fmul_rn(b, b), eb = __fmaf_rn(b, b, -pb);
@@ -1726,9 +1697,8 @@ __device__ __forceinline__ f2 f2_add(f2 a, f2 b) {
   r.l = __fadd_rn(__fadd_rn(a.l, b.l), t);
   return r;
 }
-// (a1 - a0)^2 + (b1 - b0)^2 for FP32 pairs of values: each difference exact
-// as d + err (TwoSum), its square as p + e + 2 d err (err^2 <= 2^-48 d^2 is
-// dropped)
+// (a1 - a0)^2 + (b1 - b0)^2: each difference exact as d + err (TwoSum), its
+// square as p + e + 2 d err (err^2 <= 2^-48 d^2 is dropped)
 __device__ __forceinline__ f2 f2_dsq2(float a1, float a0, float b1, float b0) {
   float da, ra, db, rb;
   two_sum(a1, -a0, da, ra);
@@ -1741,14 +1711,14 @@ __device__ __forceinline__ f2 f2_dsq2(float a1, float a0, float b1, float b0) {
   r.l = __fadd_rn(__fadd_rn(ea, eb), t);
   return r;
 }
-// w * (h + l) for an FP32 weight w: w*h exact as q + r, w*l rounded
-__device__ __forceinline__ f2 f2_scale(float w, f2 a) {
+// (wh + wl) * (h + l): wh*h exact as q + r, the cross terms rounded
+__device__ __forceinline__ f2 f2_mul(float wh, float wl, f2 a) {
   f2 r;
-  r.h = __fmul_rn(w, a.h);
-  r.l = __fmaf_rn(w, a.l, __fmaf_rn(w, a.h, -r.h));
+  r.h = __fmul_rn(wh, a.h);
+  r.l = __fmaf_rn(wl, a.h, __fmaf_rn(wh, a.l, __fmaf_rn(wh, a.h, -r.h)));
   return r;
 }
-// accumulator += a, then renormalised so that |l| <= ulp(h)/2 (Fast2Sum)
+// accumulator += a, renormalised so that |l| <= ulp(h)/2 (Fast2Sum)
 __device__ __forceinline__ void f2_acc(f2& s, f2 a) {
   float h, t;
   two_sum(s.h, a.h, h, t);
@@ -1756,107 +1726,146 @@ __device__ __forceinline__ void f2_acc(f2& s, f2 a) {
   s.h = __fadd_rn(h, l);
   s.l = __fsub_rn(l, __fsub_rn(s.h, h));
 }
+__device__ __forceinline__ bool f2_finite(f2 a) { return fabsf(a.h) <= 3.0e38f && fabsf(a.l) <= 3.0e38f; }
 
-// The seven sums of the FP32 state in FP32-pair arithmetic.  kh2 = kx^2 +
-// ky^2 < 2^24 is exact in FP32 and kh2^2 is applied as two exact scalings.
-// Error per sum: about 2^-44 of the sum (TwoSum accumulation, the rounded
-// w*l terms and the dropped err^2), plus at most 2^-100 absolute per mode
-// for values below 2^-50, whose square's low word underflows.  Returns false
-// when a pair is not finite (values beyond ~2^60 overflow FP32 squares); the
-// caller then recomputes the thread's sums in FP64.
-__device__ __forceinline__ bool diag_modes_f2(const Geom& g, long long zo, bool top, long long m0, long long m1,
-                                              int stride, const cplx<float>* __restrict__ BR,
-                                              const cplx<float>* __restrict__ BI,
-                                              const cplx<float>* __restrict__ AR,
-                                              const cplx<float>* __restrict__ AI,
-                                              const cplx<float>* __restrict__ psi, double acc[kNDiag]) {
-  f2 s[kNDiag];
-  for (int k = 0; k < kNDiag; ++k) s[k] = f2{0.0f, 0.0f};
-  for (long long m = m0; m < m1; m += stride) {
-    const int mi = (int)m, r = mi / g.KXP, kx = mi - r * g.KXP;
-    const int ky = g.ky_of_row(r);
-    if (!g.mask(kx, ky)) continue;
-    const float kh2 = (float)(kx * kx + ky * ky);      // exact: < 2^24
-    const float w00 = (kx == 0 && ky == 0) ? 0.5f : 1.0f;
-    const cplx<float> brc = BR[zo + m], bic = BI[zo + m], arc = AR[zo + m], aic = AI[zo + m], pc = psi[zo + m];
-    const f2 b2 = f2_add(f2_sq2(brc.x, brc.y), f2_sq2(bic.x, bic.y));
-    const f2 a2 = f2_add(f2_sq2(arc.x, arc.y), f2_sq2(aic.x, aic.y));
-    const f2 p2 = f2_sq2(pc.x, pc.y);
-    f2 c2{0.0f, 0.0f}, pz2{0.0f, 0.0f};
-    if (!top) {
-      const cplx<float> ar1 = AR[zo + g.plane + m], ai1 = AI[zo + g.plane + m], p1 = psi[zo + g.plane + m];
-      c2 = f2_add(f2_dsq2(ar1.x, arc.x, ar1.y, arc.y), f2_dsq2(ai1.x, aic.x, ai1.y, aic.y));
-      pz2 = f2_dsq2(p1.x, pc.x, p1.y, pc.y);
+// The six column sums of levels [zlo, zhi) of the segment whose top level is
+// ztop, in FP64 arithmetic; wz: w1 at [0, nseg), w4 at [nseg, 2 nseg).
+template <typename T>
+__device__ __forceinline__ void diag_column_fp64(const Geom& g, long long m, int zlo, int zhi, int ztop,
+                                                 const double* __restrict__ wz, const cplx<T>* __restrict__ BR,
+                                                 const cplx<T>* __restrict__ BI, const cplx<T>* __restrict__ AR,
+                                                 const cplx<T>* __restrict__ AI, const cplx<T>* __restrict__ psi,
+                                                 double S[kDiagSums]) {
+  for (int k = 0; k < kDiagSums; ++k) S[k] = 0.0;
+  const long long P = g.plane;
+  cplx<T> ar = AR[zlo * P + m], ai = AI[zlo * P + m], ps = psi[zlo * P + m];
+  for (int z = zlo; z < zhi; ++z) {
+    const cplx<T> br = BR[z * P + m], bi = BI[z * P + m];
+    const double brx = to64<T>(br.x), bry = to64<T>(br.y), bix = to64<T>(bi.x), biy = to64<T>(bi.y);
+    const double arx = to64<T>(ar.x), ary = to64<T>(ar.y), aix = to64<T>(ai.x), aiy = to64<T>(ai.y);
+    const double px = to64<T>(ps.x), py = to64<T>(ps.y);
+    S[0] += brx * brx + bry * bry + bix * bix + biy * biy;
+    S[2] += arx * arx + ary * ary + aix * aix + aiy * aiy;
+    S[3] += px * px + py * py;
+    if (z < ztop) {
+      const cplx<T> ar1 = AR[(z + 1) * P + m], ai1 = AI[(z + 1) * P + m], p1 = psi[(z + 1) * P + m];
+      const double crx = to64<T>(ar1.x) - arx, cry = to64<T>(ar1.y) - ary;
+      const double cix = to64<T>(ai1.x) - aix, ciy = to64<T>(ai1.y) - aiy;
+      const double bx = to64<T>(p1.x) - px, by = to64<T>(p1.y) - py;
+      const double pz2 = bx * bx + by * by;
+      const int zl = z % g.nseg;
+      S[1] += wz[zl] * (crx * crx + cry * cry + cix * cix + ciy * ciy);
+      S[4] += wz[g.nseg + zl] * pz2;
+      S[5] += pz2;
+      ar = ar1; ai = ai1; ps = p1;
     }
-    const f2 t = f2_scale(kh2, p2);
-    f2_acc(s[0], f2_scale(w00, b2));
-    f2_acc(s[1], f2_scale(kh2, c2));
-    f2_acc(s[2], f2_scale(kh2, f2_scale(kh2, a2)));
-    f2_acc(s[3], t);
-    f2_acc(s[4], f2_scale(w00, pz2));
-    f2_acc(s[5], f2_scale(kh2, t));
-    f2_acc(s[6], f2_scale(kh2, pz2));
+  }
+}
+
+// The same sums of the FP32 state in FP32-pair arithmetic; wzf holds the
+// weights as pairs.  Error per sum: about 2^-44 of the sum (the TwoSum
+// accumulation, the rounded cross terms, the dropped err^2), plus at most
+// 2^-100 absolute per mode for values below 2^-50, whose square's low word
+// underflows.  Returns false when a pair is not finite (values beyond ~2^60
+// overflow FP32 squares); the caller then recomputes the column in FP64.
+__device__ __forceinline__ bool diag_column_f2(const Geom& g, long long m, int zlo, int zhi, int ztop,
+                                               const float2* __restrict__ wzf, const cplx<float>* __restrict__ BR,
+                                               const cplx<float>* __restrict__ BI,
+                                               const cplx<float>* __restrict__ AR,
+                                               const cplx<float>* __restrict__ AI,
+                                               const cplx<float>* __restrict__ psi, double S[kDiagSums]) {
+  f2 s[kDiagSums];
+  for (int k = 0; k < kDiagSums; ++k) s[k] = f2{0.0f, 0.0f};
+  const long long P = g.plane;
+  cplx<float> ar = AR[zlo * P + m], ai = AI[zlo * P + m], ps = psi[zlo * P + m];
+#pragma unroll 2
+  for (int z = zlo; z < zhi; ++z) {
+    const cplx<float> br = BR[z * P + m], bi = BI[z * P + m];
+    f2_acc(s[0], f2_add(f2_sq2(br.x, br.y), f2_sq2(bi.x, bi.y)));
+    f2_acc(s[2], f2_add(f2_sq2(ar.x, ar.y), f2_sq2(ai.x, ai.y)));
+    f2_acc(s[3], f2_sq2(ps.x, ps.y));
+    if (z < ztop) {
+      const cplx<float> ar1 = AR[(z + 1) * P + m], ai1 = AI[(z + 1) * P + m], p1 = psi[(z + 1) * P + m];
+      const int zl = z % g.nseg;
+      const float2 w1 = wzf[zl], w4 = wzf[g.nseg + zl];
+      const f2 c2 = f2_add(f2_dsq2(ar1.x, ar.x, ar1.y, ar.y), f2_dsq2(ai1.x, ai.x, ai1.y, ai.y));
+      const f2 pz2 = f2_dsq2(p1.x, ps.x, p1.y, ps.y);
+      f2_acc(s[1], f2_mul(w1.x, w1.y, c2));
+      f2_acc(s[4], f2_mul(w4.x, w4.y, pz2));
+      f2_acc(s[5], pz2);
+      ar = ar1; ai = ai1; ps = p1;
+    }
   }
   bool ok = true;
-  for (int k = 0; k < kNDiag; ++k) {
-    ok = ok && fabsf(s[k].h) <= 3.0e38f && fabsf(s[k].l) <= 3.0e38f;     // false for inf and NaN
-    acc[k] = f32_to_f64(s[k].h) + f32_to_f64(s[k].l);
+  for (int k = 0; k < kDiagSums; ++k) {
+    ok = ok && f2_finite(s[k]);
+    S[k] = f32_to_f64(s[k].h) + f32_to_f64(s[k].l);
   }
   return ok;
 }
 
+// grid: (columns / kDiagThreads, chunks per segment, segments seg0 ...);
+// part: kNDiag partials per CTA, at ((blockIdx.z * gridDim.y + blockIdx.y)
+// * gridDim.x + blockIdx.x) * kNDiag.  c2 = 1/(8 Bu^2), c6 = 2/dz^2.
 template <typename T>
-__global__ void __launch_bounds__(256)
-k_diag_level(Geom g, double dz, double Bu, const double* __restrict__ r2, const cplx<T>* __restrict__ BR,
-             const cplx<T>* __restrict__ BI, const cplx<T>* __restrict__ AR, const cplx<T>* __restrict__ AI,
-             const cplx<T>* __restrict__ psi, double* __restrict__ part) {
-  __shared__ double red[kNDiag][256];
-  const int z = blockIdx.y, chunk = blockIdx.x;
-  const long long zo = (long long)z * g.plane;
-  const long long per = (g.plane + kDiagChunks - 1) / kDiagChunks;
-  const long long m0 = chunk * per, m1 = m0 + per < g.plane ? m0 + per : g.plane;
-  const bool top = (z % g.nseg == g.nseg - 1);     // top level of its segment
-  const double rz = r2[z % g.nseg];
-  double acc[kNDiag];
-  if constexpr (std::is_same<T, float>::value) {
-    if (!diag_modes_f2(g, zo, top, m0 + threadIdx.x, m1, blockDim.x, BR, BI, AR, AI, psi, acc))
-      diag_modes_fp64<T>(g, zo, top, m0 + threadIdx.x, m1, blockDim.x, BR, BI, AR, AI, psi, acc);
-  } else {
-    diag_modes_fp64<T>(g, zo, top, m0 + threadIdx.x, m1, blockDim.x, BR, BI, AR, AI, psi, acc);
+__global__ void __launch_bounds__(kDiagThreads)
+k_diag_cols(Geom g, int seg0, const double* __restrict__ wz, const float2* __restrict__ wzf, double c2, double c6,
+            const cplx<T>* __restrict__ BR, const cplx<T>* __restrict__ BI, const cplx<T>* __restrict__ AR,
+            const cplx<T>* __restrict__ AI, const cplx<T>* __restrict__ psi, const int* __restrict__ cols,
+            int ncols, double* __restrict__ part) {
+  __shared__ double red[kNDiag][kDiagThreads / 32];
+  const int li = blockIdx.x * kDiagThreads + threadIdx.x;
+  double acc[kNDiag] = {0, 0, 0, 0, 0, 0, 0};
+  if (li < ncols) {
+    const long long m = cols[li];
+    const int r = (int)(m / g.KXP), kx = (int)(m - (long long)r * g.KXP);
+    const int ky = g.ky_of_row(r);
+    const int zs = (seg0 + blockIdx.z) * g.nseg, ztop = zs + g.nseg - 1;
+    const int zlo = zs + blockIdx.y * kDiagZC, zhi = zlo + kDiagZC < zs + g.nseg ? zlo + kDiagZC : zs + g.nseg;
+    double S[kDiagSums];
+    if constexpr (std::is_same<T, float>::value) {
+      if (!diag_column_f2(g, m, zlo, zhi, ztop, wzf, BR, BI, AR, AI, psi, S))
+        diag_column_fp64<T>(g, m, zlo, zhi, ztop, wz, BR, BI, AR, AI, psi, S);
+    } else {
+      diag_column_fp64<T>(g, m, zlo, zhi, ztop, wz, BR, BI, AR, AI, psi, S);
+    }
+    // exact int -> double without a conversion instruction: (2^52 + k) - 2^52
+    const double kh2 = __hiloint2double(0x43300000, kx * kx + ky * ky) - 4503599627370496.0;
+    const double kh4 = kh2 * kh2;                      // exact: < 2^53
+    const double w00 = (kx == 0 && ky == 0) ? 0.5 : 1.0;
+    acc[0] = w00 * S[0];
+    acc[1] = kh2 * S[1];
+    acc[2] = (kh4 * S[2]) * c2;
+    acc[3] = kh2 * S[3];
+    acc[4] = w00 * S[4];
+    acc[5] = 2.0 * (kh4 * S[3]);
+    acc[6] = (kh2 * S[5]) * c6;
   }
-  // constant factors of each sum (per level)
-  {
-    const double inv_dz2 = 1.0 / (dz * dz);
-    acc[1] *= (0.5 / (rz * Bu)) * inv_dz2;
-    acc[2] *= (1.0 / 8.0) * (1.0 / (Bu * Bu));
-    acc[4] *= (Bu / rz) * inv_dz2;
-    acc[5] *= 2.0;
-    acc[6] *= 2.0 * inv_dz2;
+  // fixed-order reduction: a butterfly in each warp, then the warps in order
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < kNDiag; ++k) {
+    double v = acc[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[k][w] = v;
   }
-  for (int k = 0; k < kNDiag; ++k) red[k][threadIdx.x] = acc[k];
   __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s)
-      for (int k = 0; k < kNDiag; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + s];
-    __syncthreads();
+  if (threadIdx.x < kNDiag) {
+    double v = 0.0;
+    for (int i = 0; i < kDiagThreads / 32; ++i) v += red[threadIdx.x][i];
+    part[(((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x) * kNDiag + threadIdx.x] = v;
   }
-  if (threadIdx.x < kNDiag) part[((long long)z * kDiagChunks + chunk) * kNDiag + threadIdx.x] = red[threadIdx.x][0];
 }
 
-// one warp per quantity: lane l sums levels l, l+32, ... (each level's
-// chunks in order), then a fixed butterfly over the lanes; mean over levels
-static __global__ void k_diag_sum(int z0, int n3, const double* __restrict__ part, double* __restrict__ out) {
+// one warp per quantity: lane l sums partials l, l+32, ... in order, then a
+// fixed butterfly over the lanes; the mean over the nlev levels
+static __global__ void k_diag_sum(long long nparts, int nlev, const double* __restrict__ part, double* __restrict__ out) {
   const int k = threadIdx.x / 32, lane = threadIdx.x % 32;
   if (k >= kNDiag) return;
-  part += (long long)z0 * kDiagChunks * kNDiag;     // levels z0 .. z0 + n3 - 1
   double s = 0.0;
-  for (int z = lane; z < n3; z += 32) {
-    double lv = 0.0;
-    for (int c = 0; c < kDiagChunks; ++c) lv += part[((long long)z * kDiagChunks + c) * kNDiag + k];
-    s += lv;
-  }
+  for (long long p = lane; p < nparts; p += 32) s += part[p * kNDiag + k];
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if (lane == 0) out[k] = s / n3;
+  if (lane == 0) out[k] = s / nlev;
 }
 
 }  // namespace qg
