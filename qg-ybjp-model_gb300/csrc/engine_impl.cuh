@@ -149,7 +149,17 @@ class Engine : public EngineBase {
       QG_CK(cudaMalloc(&fwz, wf.size() * sizeof(float2)));
       QG_CK(cudaMemcpy(fwz, wf.data(), wf.size() * sizeof(float2), cudaMemcpyHostToDevice));
     }
-    QG_CK(cudaMalloc(&diag_part, diag_parts(g.n3 / g.nseg) * kNDiag * sizeof(double)));
+    {
+      int occ = 0;
+      QG_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, cfg.device));
+      QG_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_diag_cols<T>, kDiagThreads, 0));
+      diag_slots = std::max(1, occ) * nsm;
+      // partials of the largest launch (any number of whole segments)
+      size_t mx = 0;
+      for (int ns = 1; ns <= g.n3 / g.nseg; ++ns) mx = std::max(mx, diag_parts(ns));
+      diag_part_n = mx;
+    }
+    QG_CK(cudaMalloc(&diag_part, diag_part_n * kNDiag * sizeof(double)));
     QG_CK(cudaMalloc(&diag_out, kNDiag * sizeof(double)));
     QG_CK(cudaMallocHost(&diag_host, kNDiag * sizeof(double)));
     QG_CK(cudaHostAlloc(&wflag_h, 3 * sizeof(int), cudaHostAllocMapped));
@@ -427,18 +437,31 @@ class Engine : public EngineBase {
 
   int diagnostics(qg_energy* out) override { return diagnostics_range(0, g.n3, out); }
 
-  // partials of k_diag_cols over nsegs whole segments
+  // k_diag_cols over nsegs whole segments: the levels of each segment in
+  // chunks of zc, as many chunks as keep the grid within one wave of
+  // resident CTAs (a second, partial wave would run at a fraction of the
+  // GPU); returns the grid
+  dim3 diag_grid(int nsegs, int* zc) const {
+    const int cb = (nret + kDiagThreads - 1) / kDiagThreads;
+    const long long per = (long long)cb * nsegs;
+    const int nch0 = (int)std::max<long long>(1, std::min<long long>(g.nseg, (long long)diag_slots / per));
+    *zc = (g.nseg + nch0 - 1) / nch0;
+    return dim3(cb, (g.nseg + *zc - 1) / *zc, nsegs);
+  }
   size_t diag_parts(int nsegs) const {
-    return (size_t)((nret + kDiagThreads - 1) / kDiagThreads) * ((g.nseg + kDiagZC - 1) / kDiagZC) * nsegs;
+    int zc;
+    const dim3 gr = diag_grid(nsegs, &zc);
+    return (size_t)gr.x * gr.y * gr.z;
   }
   // the seven integrals of segments [seg0, seg0 + nsegs) into out (device)
   int launch_diag(int seg0, int nsegs, double* part, double* out, cudaStream_t s) {
-    const dim3 grid((nret + kDiagThreads - 1) / kDiagThreads, (g.nseg + kDiagZC - 1) / kDiagZC, nsegs);
+    int zc;
+    const dim3 grid = diag_grid(nsegs, &zc);
     const double c2 = (1.0 / 8.0) * (1.0 / (cfg.Bu * cfg.Bu)), c6 = 2.0 * (1.0 / (cfg.dz * cfg.dz));
-    k_diag_cols<T><<<grid, kDiagThreads, 0, s>>>(g, seg0, dwz, fwz, c2, c6, F[F_BR], F[F_BI], F[F_AR], F[F_AI],
-                                                 F[F_PSI], cols_ret, nret, part);
+    k_diag_cols<T><<<grid, kDiagThreads, 0, s>>>(g, seg0, zc, dwz, fwz, c2, c6, F[F_BR], F[F_BI], F[F_AR],
+                                                 F[F_AI], F[F_PSI], cols_ret, nret, part);
     QG_LAUNCHED();
-    k_diag_sum<<<1, 32 * kNDiag, 0, s>>>((long long)diag_parts(nsegs), nsegs * g.nseg, part, out);
+    k_diag_sum<<<1, 32 * kNDiag, 0, s>>>((long long)grid.x * grid.y * grid.z, nsegs * g.nseg, part, out);
     QG_LAUNCHED();
     return QG_OK;
   }
@@ -454,7 +477,7 @@ class Engine : public EngineBase {
       QG_CK(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
       QG_CK(cudaStreamCreateWithPriority(&std_, cudaStreamNonBlocking, prio_low));
       QG_CK(cudaEventCreateWithFlags(&ev_state, cudaEventDisableTiming));
-      QG_CK(cudaMalloc(&diag_part_a, diag_parts(g.n3 / g.nseg) * kNDiag * sizeof(double)));
+      QG_CK(cudaMalloc(&diag_part_a, diag_part_n * kNDiag * sizeof(double)));
       QG_CK(cudaMalloc(&diag_out_a, kNDiag * sizeof(double)));
       QG_CK(cudaMallocHost(&diag_host_a, kNDiag * sizeof(double)));
     }
@@ -726,6 +749,8 @@ class Engine : public EngineBase {
   double *diag_part = nullptr, *diag_out = nullptr, *diag_host = nullptr;
   double* dwz = nullptr;     // diagnostics' per-level weights (w1, w4), FP64
   float2* fwz = nullptr;     // the same as FP32 pairs
+  int diag_slots = 1;        // resident k_diag_cols CTAs on the GPU
+  size_t diag_part_n = 0;    // partials the diagnostics buffers hold
   // set by a kernel whose bounded wait expired (mapped page-locked word)
   // mapped page-locked words raised on the device: [0] a bounded wait
   // expired, [1] a step produced a non-finite q*, [2] qg_set_state's input

@@ -1650,8 +1650,8 @@ __global__ void k_ybj_A(Geom g, double dz, double Bu, double Ro, const double* _
 // of diag_zentrum 16-211, enstrophy 1262-1363): column partial sums, then a
 // fixed-order sum of the partials
 // ===========================================================================
-// A thread owns one retained column (kx, ky) and walks a chunk of up to
-// kDiagZC levels of one vertical segment, loading each level's B, A and psi
+// A thread owns one retained column (kx, ky) and walks a chunk of levels of
+// one vertical segment, loading each level's B, A and psi
 // once (the level above is the next iteration's level) and accumulating six
 // column sums: |B|^2, w1_z |A(z+1)-A(z)|^2, |A|^2, |psi|^2,
 // w4_z |psi(z+1)-psi(z)|^2 and |psi(z+1)-psi(z)|^2, with the per-level
@@ -1663,7 +1663,14 @@ __global__ void k_ybj_A(Geom g, double dz, double Bu, double Ro, const double* _
 //   pe = w00 S_w4b, zeta2 = 2 kh^4 S_p, omegah2 = 2 kh^2 S_b' / dz^2.
 constexpr int kNDiag = 7;
 constexpr int kDiagSums = 6;
-constexpr int kDiagZC = 64;        // levels per chunk
+#ifndef QG_DIAG_MINB
+#define QG_DIAG_MINB 10
+#endif
+constexpr int kDiagMinB = QG_DIAG_MINB;   // register target: CTAs per SM
+#ifndef QG_DIAG_UNROLL
+#define QG_DIAG_UNROLL 2
+#endif
+constexpr int kDiagUnroll = QG_DIAG_UNROLL;   // levels per iteration of the FP32-pair loop
 constexpr int kDiagThreads = 128;  // columns per CTA
 
 // --- FP32-pair ("double-float") arithmetic for the FP32 state --------------
@@ -1753,7 +1760,7 @@ __device__ __forceinline__ void diag_column_fp64(const Geom& g, long long m, int
       const double cix = to64<T>(ai1.x) - aix, ciy = to64<T>(ai1.y) - aiy;
       const double bx = to64<T>(p1.x) - px, by = to64<T>(p1.y) - py;
       const double pz2 = bx * bx + by * by;
-      const int zl = z % g.nseg;
+      const int zl = z - (ztop + 1 - g.nseg);      // level within the segment
       S[1] += wz[zl] * (crx * crx + cry * cry + cix * cix + ciy * ciy);
       S[4] += wz[g.nseg + zl] * pz2;
       S[5] += pz2;
@@ -1778,7 +1785,7 @@ __device__ __forceinline__ bool diag_column_f2(const Geom& g, long long m, int z
   for (int k = 0; k < kDiagSums; ++k) s[k] = f2{0.0f, 0.0f};
   const long long P = g.plane;
   cplx<float> ar = AR[zlo * P + m], ai = AI[zlo * P + m], ps = psi[zlo * P + m];
-#pragma unroll 2
+#pragma unroll kDiagUnroll
   for (int z = zlo; z < zhi; ++z) {
     const cplx<float> br = BR[z * P + m], bi = BI[z * P + m];
     f2_acc(s[0], f2_add(f2_sq2(br.x, br.y), f2_sq2(bi.x, bi.y)));
@@ -1786,7 +1793,7 @@ __device__ __forceinline__ bool diag_column_f2(const Geom& g, long long m, int z
     f2_acc(s[3], f2_sq2(ps.x, ps.y));
     if (z < ztop) {
       const cplx<float> ar1 = AR[(z + 1) * P + m], ai1 = AI[(z + 1) * P + m], p1 = psi[(z + 1) * P + m];
-      const int zl = z % g.nseg;
+      const int zl = z - (ztop + 1 - g.nseg);      // level within the segment
       const float2 w1 = wzf[zl], w4 = wzf[g.nseg + zl];
       const f2 c2 = f2_add(f2_dsq2(ar1.x, ar.x, ar1.y, ar.y), f2_dsq2(ai1.x, ai.x, ai1.y, ai.y));
       const f2 pz2 = f2_dsq2(p1.x, ps.x, p1.y, ps.y);
@@ -1804,12 +1811,13 @@ __device__ __forceinline__ bool diag_column_f2(const Geom& g, long long m, int z
   return ok;
 }
 
-// grid: (columns / kDiagThreads, chunks per segment, segments seg0 ...);
-// part: kNDiag partials per CTA, at ((blockIdx.z * gridDim.y + blockIdx.y)
-// * gridDim.x + blockIdx.x) * kNDiag.  c2 = 1/(8 Bu^2), c6 = 2/dz^2.
+// grid: (columns / kDiagThreads, chunks of zc levels per segment, segments
+// seg0 ...), sized by the host to one wave of resident CTAs; part: kNDiag
+// partials per CTA, at ((blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x +
+// blockIdx.x) * kNDiag.  c2 = 1/(8 Bu^2), c6 = 2/dz^2.
 template <typename T>
-__global__ void __launch_bounds__(kDiagThreads)
-k_diag_cols(Geom g, int seg0, const double* __restrict__ wz, const float2* __restrict__ wzf, double c2, double c6,
+__global__ void __launch_bounds__(kDiagThreads, kDiagMinB)
+k_diag_cols(Geom g, int seg0, int zc, const double* __restrict__ wz, const float2* __restrict__ wzf, double c2, double c6,
             const cplx<T>* __restrict__ BR, const cplx<T>* __restrict__ BI, const cplx<T>* __restrict__ AR,
             const cplx<T>* __restrict__ AI, const cplx<T>* __restrict__ psi, const int* __restrict__ cols,
             int ncols, double* __restrict__ part) {
@@ -1821,7 +1829,7 @@ k_diag_cols(Geom g, int seg0, const double* __restrict__ wz, const float2* __res
     const int r = (int)(m / g.KXP), kx = (int)(m - (long long)r * g.KXP);
     const int ky = g.ky_of_row(r);
     const int zs = (seg0 + blockIdx.z) * g.nseg, ztop = zs + g.nseg - 1;
-    const int zlo = zs + blockIdx.y * kDiagZC, zhi = zlo + kDiagZC < zs + g.nseg ? zlo + kDiagZC : zs + g.nseg;
+    const int zlo = zs + blockIdx.y * zc, zhi = zlo + zc < zs + g.nseg ? zlo + zc : zs + g.nseg;
     double S[kDiagSums];
     if constexpr (std::is_same<T, float>::value) {
       if (!diag_column_f2(g, m, zlo, zhi, ztop, wzf, BR, BI, AR, AI, psi, S))
