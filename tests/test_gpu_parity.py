@@ -130,6 +130,24 @@ def test_steps_small(precision):
     sim.close()
 
 
+@pytest.mark.parametrize("strat", ["c0", "c1"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_step_solves_equal_dropin_solvers(strat, precision):
+    """The step's column solves (over the retained columns only; on the
+    mixed path with per-column copies of the elimination factors) equal the
+    drop-in solvers (every column, the per-kh^2 factor tables) bitwise on
+    the same right-hand sides: A from B after the update, psi from q*
+    (exponential N^2, c1: the ill-conditioned small-kh columns included)."""
+    rc = scaled(CONFIGS[strat], 64, 32)
+    model, st, sim = pair(rc, precision)
+    sim.step(True)
+    BR = sim.get_state("BR")
+    assert np.array_equal(sim.get_state("AR"), sim.A_solver_ybj_plus(BR)[0])
+    qs = sim.get_state("qstar")
+    assert np.array_equal(sim.get_state("psi"), sim.psi_solver(qs))
+    sim.close()
+
+
 @pytest.mark.parametrize("scale", [1.0, 1e25, 1e-30])
 def test_mixed_diagnostics_are_fp64_sums_of_the_fp32_state(scale):
     """The mixed engine forms the seven diagnostic sums of its FP32 state in
