@@ -319,13 +319,21 @@ class Engine : public EngineBase {
     }
     *(volatile int*)(wflag_h + 2) = 0;
     if (f == F_BR || f == F_BI) q_valid = false;
-    k_dense_to_compact<T><<<grid_for((long long)nlev * g.plane), 256, 0, st>>>(g, level0, nlev, src, F[f], iflag);
-    QG_LAUNCHED();
     if (f == F_PSI && sizeof(T) == 4) {
       // mixed path: keep psi in FP64 until qg_init_state has built q from it
-      // (init_q's vertical second difference would amplify FP32 rounding)
+      // (init_q's vertical second difference would amplify FP32 rounding);
+      // the FP32 field is rounded from that copy on the device, so the input
+      // crosses the host link once
       if (!psi64) QG_CK(cudaMalloc(&psi64, (size_t)g.n3 * g.plane * sizeof(double2)));
-      k_dense_to_compact<double><<<grid_for((long long)nlev * g.plane), 256, 0, st>>>(g, level0, nlev, src, psi64);
+      k_dense_to_compact<double><<<grid_for((long long)nlev * g.plane), 256, 0, st>>>(g, level0, nlev, src, psi64,
+                                                                                        iflag);
+      QG_LAUNCHED();
+      k_round_compact<T><<<grid_for((long long)nlev * g.plane), 256, 0, st>>>(
+          (long long)nlev * g.plane, reinterpret_cast<const cplx<double>*>(psi64) + (size_t)level0 * g.plane,
+          F[f] + (size_t)level0 * g.plane);
+      QG_LAUNCHED();
+    } else {
+      k_dense_to_compact<T><<<grid_for((long long)nlev * g.plane), 256, 0, st>>>(g, level0, nlev, src, F[f], iflag);
       QG_LAUNCHED();
     }
     QG_CK(cudaStreamSynchronize(st));

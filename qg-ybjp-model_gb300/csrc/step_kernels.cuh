@@ -1476,6 +1476,15 @@ static __global__ void k_dense_to_compact(Geom g, int level0, int nlev, const do
   if (nflag && __syncthreads_or(bad) && threadIdx.x == 0) raise_wait_flag(nflag);
 }
 
+// compact FP64 values rounded to T (the same rounding as k_dense_to_compact)
+template <typename T>
+__global__ void k_round_compact(long long n, const cplx<double>* __restrict__ src, cplx<T>* __restrict__ dst) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const cplx<double> v = src[i];
+    dst[i] = mk<T>((T)v.x, (T)v.y);
+  }
+}
+
 // mode: 0 plain copy, 1 vertical difference (A_z, elliptic.f90:437-450)
 template <typename T>
 __global__ void k_compact_to_dense(Geom g, int level0, int nlev, const cplx<T>* __restrict__ f, double2* __restrict__ dense,
