@@ -992,7 +992,7 @@ class Engine : public EngineBase {
             grm(g.n / Tiles<T, NN>::RTM, zc);
         if (int rc0 = pbeg(QG_K_COL_INV, bs)) return rc0;
         C* Qb = Qp ? Qp + (size_t)z0 * kNQ * g.n * g.KXP : nullptr;
-        k_col_inv<T, NN><<<gc, kColThreads, sm_ci<NN>(3), bs>>>(g, z0, F[F_PSI], F[F_Q], F[F_BR], F[F_BI], Sb, tw,
+        k_col_inv<T, NN><<<gc, Tiles<T, NN>::CNT, sm_ci<NN>(3), bs>>>(g, z0, F[F_PSI], F[F_Q], F[F_BR], F[F_BI], Sb, tw,
                                                                 Qb, Qb ? 1 : 0);
         QG_LAUNCHED();
         if (int rc0 = pend(bs)) return rc0;
@@ -1014,7 +1014,7 @@ class Engine : public EngineBase {
           QG_CK(cudaStreamWaitEvent(bs, ev_diag, cs == cudaStreamCaptureStatusActive ? cudaEventWaitExternal : 0));
         }
         if (int rc0 = pbeg(QG_K_COL_UPDATE, bs)) return rc0;
-        k_col_update<T, NN><<<gc, kColThreads, UpdLay<T, NN>::bytes(), bs>>>(g, s, z0, sptr, e1, e2, e1w, e2w, Sb, tw,
+        k_col_update<T, NN><<<gc, Tiles<T, NN>::CNT, UpdLay<T, NN>::bytes(), bs>>>(g, s, z0, sptr, e1, e2, e1w, e2w, Sb, tw,
                                                                 need_qw ? 1 : 0, Qb);
         QG_LAUNCHED();
         if (int rc0 = pend(bs)) return rc0;
@@ -1039,7 +1039,7 @@ class Engine : public EngineBase {
           QG_LAUNCHED();
           if (int rc0 = pend(bs)) return rc0;
           if (int rc0 = pbeg(QG_K_COL_QW, bs)) return rc0;
-          k_col_qw<T, NN><<<gc, kThreadsB, sm_ci<NN>(2), bs>>>(g, s, z0, F[F_Q], F[F_QSTAR], Sb, tw, nflag);
+          k_col_qw<T, NN><<<gc, Tiles<T, NN>::CNT, sm_ci<NN>(2), bs>>>(g, s, z0, F[F_Q], F[F_QSTAR], Sb, tw, nflag);
           QG_LAUNCHED();
           if (int rc0 = pend(bs)) return rc0;
         }
@@ -1117,7 +1117,7 @@ class Engine : public EngineBase {
       const int zc = std::min(Zb, g.n3 - z0);
       QG_SWITCH_N(g.n, {
         const dim3 gc((g.K + Tiles<T, NN>::CT) / Tiles<T, NN>::CT, zc);
-        k_col_inv<T, NN><<<gc, kColThreads, sm_ci<NN>(3), st>>>(g, z0, F[F_PSI], F[F_Q], F[F_BR], F[F_BI], S, tw,
+        k_col_inv<T, NN><<<gc, Tiles<T, NN>::CNT, sm_ci<NN>(3), st>>>(g, z0, F[F_PSI], F[F_Q], F[F_BR], F[F_BI], S, tw,
                                                                 Qp + (size_t)z0 * kNQ * g.n * g.KXP, 2);
         QG_LAUNCHED();
       });

@@ -107,6 +107,11 @@ __host__ __device__ constexpr int smem_ctas(int bytes) {
   return 233472 / (bytes + 1024) >= 8 ? 8 : (233472 / (bytes + 1024) >= 1 ? 233472 / (bytes + 1024) : 1);
 }
 __host__ __device__ constexpr int imin(int a, int b) { return a < b ? a : b; }
+__host__ __device__ constexpr int imax(int a, int b) { return a > b ? a : b; }
+// CTAs of `bytes` shared memory that fit on an SM, at most cap (<= 32)
+__host__ __device__ constexpr int smem_ctas_cap(int bytes, int cap) {
+  return 233472 / (bytes + 1024) >= cap ? cap : (233472 / (bytes + 1024) >= 1 ? 233472 / (bytes + 1024) : 1);
+}
 
 template <typename T, int N> struct Tiles {
   static constexpr int CB = (int)sizeof(cplx<T>);
@@ -166,11 +171,17 @@ template <typename T, int N> struct Tiles {
   // registers (colfft.cuh:row_last_fwd512): one row per 64 threads
   static constexpr bool RSHL = kRowShflLast && RFUSE && N == 512 && RTM * 64 == kRowThreads;
   static constexpr bool QSHL = kRowShflLast && QFUSE && N == 512 && QRT * 64 == QTHREADS;
-  static constexpr int CIMINB = imin(CB == 8 ? kColInvMinB : 2, smem_ctas((N + 3 * FSC) * CB));
-  static constexpr int CQMINB = imin(CB == 8 ? kColQwMinB : 2, smem_ctas((N + 2 * FSC) * CB));
+  // threads of the column kernels: one per (column, butterfly) task of the
+  // first pass (256 at N >= 256 in FP32; fewer for small N and in FP64,
+  // where a 256-thread CTA left threads idle in every pass), with the CTAs
+  // per SM scaled up by CSCALE so that the threads per SM stay the same
+  static constexpr int CNT = imin(256, imax(32, CT * (N / radix_of(N))));
+  static constexpr int CSCALE = 256 / CNT;
+  static constexpr int CIMINB = imin((CB == 8 ? kColInvMinB : 2) * CSCALE, smem_ctas_cap((N + 3 * FSC) * CB, 32));
+  static constexpr int CQMINB = imin((CB == 8 ? kColQwMinB : 2) * CSCALE, smem_ctas_cap((N + 2 * FSC) * CB, 32));
 };
-constexpr int kColThreads = 256;   // k_col_inv, k_col_update
-constexpr int kThreadsB = 256;     // row kernels, k_col_qw
+constexpr int kColThreads = 256;   // the adjoint's column kernels
+constexpr int kThreadsB = 256;     // row kernels
 
 // per-pass twiddle table of fft_ip (at most N entries)
 template <typename T, int N>
@@ -207,13 +218,13 @@ __device__ __forceinline__ void col_src(const Geom& g, int kx, int idx, int& row
 }
 
 template <typename T, int N>
-__global__ void __launch_bounds__(kColThreads, Tiles<T, N>::CIMINB)
+__global__ void __launch_bounds__(Tiles<T, N>::CNT, Tiles<T, N>::CIMINB)
 k_col_inv(Geom g, int zbase, const cplx<T>* __restrict__ psi, const cplx<T>* __restrict__ q,
           const cplx<T>* __restrict__ BR, const cplx<T>* __restrict__ BI, cplx<T>* __restrict__ S,
           const cplx<T>* __restrict__ twg, cplx<T>* __restrict__ Qb, int bmode) {
   // bmode 0: all six transforms into S; 1: u, v, zeta, q into S (BR, BI are
   // kept in Qb); 2: BR, BI into Qb only (before a step whose Qb is stale)
-  constexpr int CT = Tiles<T, N>::CT, NT = kColThreads;
+  constexpr int CT = Tiles<T, N>::CT, NT = Tiles<T, N>::CNT;
   constexpr int R0 = radix_of(N), NB0 = N / R0, NSL = LastNS<N>::value, RL = N / NSL;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
@@ -583,7 +594,7 @@ template <typename T, int N> struct UpdLay {
   // lean (FP32): B^{n+1} re-read from global memory for the q^w transforms
   // (two passes of two) instead of kept in shared memory
   static constexpr bool LEAN = kUpdLean && sizeof(T) == 4;
-  static constexpr int MINB = LEAN ? kUpdMinB : Tiles<T, N>::MINB;
+  static constexpr int MINB0 = LEAN ? kUpdMinB : Tiles<T, N>::MINB;
   // lean with the IF tables of the variable staged after the state
   // (kUpdTablesSmem) or read from global memory in the epilogue
   static constexpr bool GTAB = LEAN && !kUpdTablesSmem;
@@ -591,6 +602,8 @@ template <typename T, int N> struct UpdLay {
     return LEAN ? (size_t)(N + 2 * ColLay<N, CT>::FS + 3 * FE) * sizeof(cplx<T>) + (GTAB ? 0 : (size_t)2 * FE * sizeof(T))
                 : (size_t)(N + 2 * ColLay<N, CT>::FS + 5 * FE + PAD) * sizeof(cplx<T>) + (size_t)2 * FE * sizeof(T);
   }
+  // CTAs per SM: scaled with the column CTAs' size (Tiles::CSCALE)
+  static constexpr int MINB = imin(MINB0 * Tiles<T, N>::CSCALE, smem_ctas_cap((int)bytes(), 32));
 };
 
 // 16-byte asynchronous copy of nbytes (0, 8 or 16) and zeros for the rest
@@ -610,12 +623,12 @@ __device__ __forceinline__ void cp_async_s(T* dst, const T* src, bool valid) {
 }
 
 template <typename T, int N>
-__global__ void __launch_bounds__(kColThreads, UpdLay<T, N>::MINB)
+__global__ void __launch_bounds__(Tiles<T, N>::CNT, UpdLay<T, N>::MINB)
 k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict__ e1t, const T* __restrict__ e2t,
              const T* __restrict__ e1wt, const T* __restrict__ e2wt, cplx<T>* __restrict__ S,
              const cplx<T>* __restrict__ twg, int qw_prep, cplx<T>* __restrict__ Qb) {
   using L = UpdLay<T, N>;
-  constexpr int CT = Tiles<T, N>::CT, NT = kColThreads, FE = L::FE;
+  constexpr int CT = Tiles<T, N>::CT, NT = Tiles<T, N>::CNT, FE = L::FE;
   constexpr int R0 = radix_of(N), NB0 = N / R0, NSL = LastNS<N>::value, RL = N / NSL;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
@@ -1017,10 +1030,10 @@ k_row_qw(Geom g, cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg, int n
 // Phase A, kernel 5: y-forward FFTs of the q^w planes, q* = q - q^w
 // ===========================================================================
 template <typename T, int N>
-__global__ void __launch_bounds__(kThreadsB, Tiles<T, N>::CQMINB)
+__global__ void __launch_bounds__(Tiles<T, N>::CNT, Tiles<T, N>::CQMINB)
 k_col_qw(Geom g, StepParams sp, int zbase, const cplx<T>* __restrict__ q, cplx<T>* __restrict__ qstar,
          const cplx<T>* __restrict__ S, const cplx<T>* __restrict__ twg, int* __restrict__ nflag) {
-  constexpr int CT = Tiles<T, N>::CT, NT = kThreadsB;
+  constexpr int CT = Tiles<T, N>::CT, NT = Tiles<T, N>::CNT;
   constexpr int R0 = radix_of(N), NB0 = N / R0, NSL = LastNS<N>::value, RL = N / NSL;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
