@@ -191,13 +191,13 @@ __device__ __forceinline__ void row_pass0(cplx<T>* __restrict__ sm, Pro pro) {
 }
 
 // In-place Stockham passes (ip_pass) from stride NS up to, not including,
-// the last pass; MID: the second-to-last pass writes layout 1 (for a last
-// pass that reads layout 1).
+// the last pass; MID (a layout number, 0 for none): the second-to-last pass
+// writes layout MID (for a last pass that reads layout MID).
 template <typename T, int N, bool FWD, int BATCH, int NT, int LD, int NS, int LAY = 0, int MID = 0>
 __device__ __forceinline__ void ip_passes_but_last(cplx<T>* buf, const cplx<T>* tw) {
   if constexpr (NS < LastNS<N>::value) {
     constexpr int R = radix_of(N / NS);
-    ip_pass<T, N, R, NS, FWD, BATCH, NT, LD, LAY, (MID && NS * R == LastNS<N>::value) ? 1 : LAY>(buf, tw);
+    ip_pass<T, N, R, NS, FWD, BATCH, NT, LD, LAY, (MID && NS * R == LastNS<N>::value) ? MID : LAY>(buf, tw);
     ip_passes_but_last<T, N, FWD, BATCH, NT, LD, NS * R, LAY, MID>(buf, tw);
   }
 }

@@ -158,12 +158,27 @@ template <int N> struct PadLD { static constexpr int value = N + (N >> 4); };
 // 64(j/8) + j%8 + 8r) and all reads (index j + 64r) of 16 consecutive tasks
 // then fall on 16 distinct 8-byte bank pairs, where pad_idx leaves the middle
 // pass's writes two-way conflicted.  No padding: N entries per transform.
+//
+// LAY 2 (N = 256 with the radix plan 8 x 4 x 8, used only for the hand-off
+// between the middle radix-4 pass and the last radix-8 pass): i ^ 8*bit5(i).
+// The middle pass writes index 32(j/8) + j%8 + 8r; a half-warp's 16 tasks
+// span two runs of 8 whose low four bits coincide under pad_idx (a two-way
+// conflict) and differ in bit 3 here; the last pass reads j + 32r, whose
+// bit 5 is the same for the 16 tasks.
+//
+// LAY 3 (N = 128, plan 8 x 2 x 8, the same hand-off): i ^ 8*bit4(i).  The
+// middle radix-2 pass writes 16(j/8) + j%8 + 8r: the two runs of 8 of a
+// half-warp differ in bit 4, and under pad_idx overlap in seven bank pairs.
 template <int LAY> __host__ __device__ __forceinline__ constexpr int lay_idx(int i) {
   if constexpr (LAY == 0) {
     return pad_idx(i);
-  } else {
+  } else if constexpr (LAY == 1) {
     const int m = i >> 4;
     return i ^ ((m & 7) | ((m & 4) << 1));
+  } else if constexpr (LAY == 2) {
+    return i ^ (((i >> 5) & 1) << 3);
+  } else {
+    return i ^ (((i >> 4) & 1) << 3);
   }
 }
 
@@ -197,8 +212,64 @@ constexpr bool conflict_free512() {
       }
   return true;
 }
+// lay_idx<2> on N = 256: a permutation of [0, 256), conflict free for the
+// middle radix-4 pass's writes and the last pass's reads
+constexpr bool permutes256() {
+  bool seen[256] = {};
+  for (int i = 0; i < 256; ++i) {
+    const int p = lay_idx<2>(i);
+    if (p < 0 || p >= 256 || seen[p]) return false;
+    seen[p] = true;
+  }
+  return true;
+}
+constexpr bool conflict_free256() {
+  for (int pat = 0; pat < 2; ++pat)
+    for (int r = 0; r < (pat == 0 ? 4 : 8); ++r)
+      for (int j0 = 0; j0 < (pat == 0 ? 64 : 32); j0 += 16) {
+        bool hit[16] = {};
+        for (int j = j0; j < j0 + 16; ++j) {
+          const int i = pat == 0 ? 32 * (j >> 3) + (j & 7) + 8 * r    // middle (radix-4) pass writes
+                                 : j + 32 * r;                        // last pass reads
+          const int slot = lay_idx<2>(i) & 15;
+          if (hit[slot]) return false;
+          hit[slot] = true;
+        }
+      }
+  return true;
+}
+// lay_idx<3> on N = 128: the middle radix-2 pass's writes and the last
+// pass's reads
+constexpr bool permutes128() {
+  bool seen[128] = {};
+  for (int i = 0; i < 128; ++i) {
+    const int p = lay_idx<3>(i);
+    if (p < 0 || p >= 128 || seen[p]) return false;
+    seen[p] = true;
+  }
+  return true;
+}
+constexpr bool conflict_free128() {
+  for (int pat = 0; pat < 2; ++pat)
+    for (int r = 0; r < (pat == 0 ? 2 : 8); ++r)
+      for (int j0 = 0; j0 < (pat == 0 ? 64 : 16); j0 += 16) {
+        bool hit[16] = {};
+        for (int j = j0; j < j0 + 16; ++j) {
+          const int i = pat == 0 ? 16 * (j >> 3) + (j & 7) + 8 * r    // middle (radix-2) pass writes
+                                 : j + 16 * r;                        // last pass reads
+          const int slot = lay_idx<3>(i) & 15;
+          if (hit[slot]) return false;
+          hit[slot] = true;
+        }
+      }
+  return true;
+}
 static_assert(permutes512(), "lay_idx<1> is not a permutation of [0, 512)");
 static_assert(conflict_free512(), "lay_idx<1> leaves a bank conflict");
+static_assert(permutes256(), "lay_idx<2> is not a permutation of [0, 256)");
+static_assert(conflict_free256(), "lay_idx<2> leaves a bank conflict");
+static_assert(permutes128(), "lay_idx<3> is not a permutation of [0, 128)");
+static_assert(conflict_free128(), "lay_idx<3> leaves a bank conflict");
 }  // namespace lay_check
 
 // Twiddles laid out per pass: the pass with stride NS and radix R reads
@@ -269,15 +340,15 @@ __device__ __forceinline__ void ip_pass(cplx<T>* __restrict__ buf, const cplx<T>
   __syncthreads();
 }
 
-// MID: the second-to-last pass writes, and the last pass reads, layout 1
-// (the other hand-offs stay in LAY)
+// MID (a layout number, 0 for none): the second-to-last pass writes, and
+// the last pass reads, layout MID (the other hand-offs stay in LAY)
 template <typename T, int N, bool FWD, int BATCH, int NT, int LD, int NS, int LAY = 0, int MID = 0>
 __device__ __forceinline__ void ip_passes(cplx<T>* buf, const cplx<T>* tw) {
   if constexpr (NS < N) {
     constexpr int R = PassRadix<N / NS>::value;
     constexpr bool last = NS * R == N;
     constexpr bool pen = !last && NS * R * PassRadix<(last ? 1 : N / (NS * R))>::value == N;
-    ip_pass<T, N, R, NS, FWD, BATCH, NT, LD, (MID && last) ? 1 : LAY, (MID && pen) ? 1 : LAY>(buf, tw);
+    ip_pass<T, N, R, NS, FWD, BATCH, NT, LD, (MID && last) ? MID : LAY, (MID && pen) ? MID : LAY>(buf, tw);
     ip_passes<T, N, FWD, BATCH, NT, LD, NS * R, LAY, MID>(buf, tw);
   }
 }

@@ -87,7 +87,11 @@ constexpr bool kRowMainMidSwz = QG_ROWMAIN_MIDSWZ != 0;   // k_row_main forward 
 #ifndef QG_ROWMAIN_MIDSWZI
 #define QG_ROWMAIN_MIDSWZI 1
 #endif
-constexpr bool kRowMainMidSwzInv = QG_ROWMAIN_MIDSWZI != 0;  // the same for its inverse transforms (0.921 -> 0.907 ms)
+constexpr bool kRowMainMidSwzInv = QG_ROWMAIN_MIDSWZI != 0;
+#ifndef QG_ROWQW_MIDSWZ
+#define QG_ROWQW_MIDSWZ 1
+#endif
+constexpr bool kRowQwMidSwz = QG_ROWQW_MIDSWZ != 0;   // k_row_qw (N = 256, 128): the mid-pass hand-off in layout 2, 3  // the same for its inverse transforms (0.921 -> 0.907 ms)
 #ifndef QG_ROW_SHFL_LAST
 #define QG_ROW_SHFL_LAST 1
 #endif
@@ -164,9 +168,14 @@ template <typename T, int N> struct Tiles {
   static constexpr bool QPRE = kRowPrefetch && QFUSE;
   // element placement of the fused row kernels' transforms (lay_idx)
   static constexpr int RLAY = kRowMainSwizzle && RFUSE && N == 512 ? 1 : 0;
-  static constexpr int RMID = !kRowMainSwizzle && kRowMainMidSwz && RFUSE && N == 512 ? 1 : 0;
-  static constexpr int RMIDI = !kRowMainSwizzle && kRowMainMidSwzInv && RFUSE && N == 512 ? 1 : 0;
+  // (the mid-pass hand-off layouts: 1 at N = 512, 2 at N = 256, 3 at N = 128)
+  static constexpr int MIDL = N == 512 ? 1
+                            : (N == 256 && LastNS<N>::value == 32 && radix_of(N) == 8) ? 2
+                            : (N == 128 && LastNS<N>::value == 16 && radix_of(N) == 8) ? 3 : 0;
+  static constexpr int RMID = !kRowMainSwizzle && kRowMainMidSwz && RFUSE ? MIDL : 0;
+  static constexpr int RMIDI = !kRowMainSwizzle && kRowMainMidSwzInv && RFUSE ? MIDL : 0;
   static constexpr int QLAY = kRowSwizzle && QFUSE && N == 512 ? 1 : 0;
+  static constexpr int QMID = kRowQwMidSwz && QFUSE && N < 512 ? MIDL : 0;   // k_row_qw at N = 256, 128
   // the forward transforms' last pass and the split of the packed spectra in
   // registers (colfft.cuh:row_last_fwd512): one row per 64 threads
   static constexpr bool RSHL = kRowShflLast && RFUSE && N == 512 && RTM * 64 == kRowThreads;
@@ -372,7 +381,7 @@ __device__ __forceinline__ void row_main_item(const Geom& g, const StepParams& s
   constexpr int RT = Tiles<T, N>::RTM, LD = Tiles<T, N>::LD, NT = kRowThreads, LAY = Tiles<T, N>::RLAY;
   // MID / MIDI: forward / inverse hand-off before the last pass in layout 1;
   // LL: layout the inverse's last pass reads
-  constexpr int MID = Tiles<T, N>::RMID, MIDI = Tiles<T, N>::RMIDI, LL = MIDI ? 1 : LAY;
+  constexpr int MID = Tiles<T, N>::RMID, MIDI = Tiles<T, N>::RMIDI, LL = MIDI ? MIDI : LAY;
   const int tid = threadIdx.x;
   const int K = g.K;
   constexpr int R0 = radix_of(N), NB0 = N / R0;
@@ -469,7 +478,7 @@ __device__ __forceinline__ void row_main_item(const Geom& g, const StepParams& s
     // (zeta br, zeta bi) transform first: its halves enter planes 2 and 4
     const RowLastTask tk = row_last_task(tid);
     const int rr = tid / 64, y = y0 + rr;
-    constexpr int LL2 = MID ? 1 : LAY;
+    constexpr int LL2 = MID ? MID : LAY;
     cplx<T> w[8], b[3], zr[3], zi[3];
     row_last_fwd512<T, LL2>(bA + (3 * RT + rr) * LD, tw, tk, w, b);
 #pragma unroll
@@ -882,14 +891,15 @@ __device__ __forceinline__ void row_qw_item(const Geom& g, cplx<T>* __restrict__
       // inverse last pass, the q^w products and the forward first pass in
       // registers (the same (row, butterfly) task holds both ends)
       constexpr int R0 = radix_of(N), NS = LastNS<N>::value, R = N / NS;
-      ip_passes_but_last<T, N, false, 3 * RT, NT, LD, R0, LAY>(bA, tw);
+      constexpr int QM = Tiles<T, N>::QMID, QL = QM ? QM : LAY;
+      ip_passes_but_last<T, N, false, 3 * RT, NT, LD, R0, LAY, QM>(bA, tw);
       const int j = tid % NS, rr = tid / NS;
       cplx<T> v[3][R];
       constexpr int off = tw_off<N>(NS);
 #pragma unroll
       for (int f = 0; f < 3; ++f) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[f][r] = bA[(f * RT + rr) * LD + lay_idx<LAY>(j + r * NS)];
+        for (int r = 0; r < R; ++r) v[f][r] = bA[(f * RT + rr) * LD + lay_idx<QL>(j + r * NS)];
 #pragma unroll
         for (int r = 1; r < R; ++r) {
           cplx<T> w = tw[off + (r - 1) * NS + j];
@@ -912,7 +922,7 @@ __device__ __forceinline__ void row_qw_item(const Geom& g, cplx<T>* __restrict__
       if constexpr (Tiles<T, N>::QSHL) {
         ip_passes_but_last<T, N, true, RT, NT, LD, R0, LAY>(bA, tw);
       } else {
-        ip_passes<T, N, true, RT, NT, LD, R0, LAY>(bA, tw);
+        ip_passes<T, N, true, RT, NT, LD, R0, LAY, QM>(bA, tw);
       }
     } else {
       ip_passes<T, N, false, 3 * RT, NT, LD, radix_of(N), LAY>(bA, tw);
