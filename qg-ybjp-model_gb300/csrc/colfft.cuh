@@ -2,11 +2,19 @@
 // shared memory, with the first pass fed from registers and the last pass
 // handed back in registers.
 //
-// Shared layout: element j of column c of field f at f*FS + pad_idx(j)*CT + c
-// (FS = PadLD<N>*CT).  Threads take tasks (c, j) with c fastest, so a warp
-// touches CT consecutive columns of 32/CT consecutive rows: global loads
-// and stores of the prologue / epilogue are coalesced row segments, and the
-// shared accesses of every pass hit each bank slot equally often.
+// Shared layout: element j of column c of field f at f*FS + col_idx(j)*CT + c
+// (FS = ColPad<N>*CT), col_idx(j) = pad_idx(j) = j + j/16 or, with CP = 8,
+// j + j/8.  Threads take tasks (c, j) with
+// c fastest, so a warp touches CT consecutive columns of 32/CT consecutive
+// rows: global loads and stores of the prologue / epilogue are coalesced row
+// segments.  A half-warp's 8-byte accesses (or a quarter-warp's 16-byte
+// ones) cover CT columns of 16/CT (8/CT) consecutive tasks j; with one pad
+// slot every 8 elements the first pass's writes (index 8j + r), the middle
+// passes' writes and every read fall on distinct bank slots for N >= 64
+// (checked at compile time below); one pad every 16 (pad_idx) leaves the
+// first pass's writes two-way conflicted but needs 6 % less shared memory,
+// which keeps k_col_update and k_col_qw within the 164 KB L1/shared
+// carve-out (with CP = 8 they moved to 196 KB and ran 4-6 % slower).
 //
 // The passes are the Stockham radix-8/4/2 passes of fft_block.cuh (same
 // order of operations and twiddles, so results are bitwise those of fft_ip):
@@ -23,9 +31,63 @@
 
 namespace qg {
 
-template <int N, int CT> struct ColLay {
-  static constexpr int FS = PadLD<N>::value * CT;
+// CP: pad slots every CP elements (8 or 16)
+template <int CP = 16> __host__ __device__ __forceinline__ constexpr int col_idx(int i) {
+  return CP == 8 ? i + (i >> 3) : pad_idx(i);
+}
+template <int N, int CP = 16> struct ColPad { static constexpr int value = CP == 8 ? N + (N >> 3) : PadLD<N>::value; };
+template <int N, int CT, int CP = 16> struct ColLay {
+  static constexpr int FS = ColPad<N, CP>::value * CT;
 };
+
+// Compile-time check of the column layout: for every pass of the radix plan
+// of N (radix_of), the reads (index j + r N/R) and writes (index 8j + r in
+// the first pass, base + r NS in the others) of each group of 128/CB
+// consecutive tasks (c = t % CT, j = t / CT: one 128-byte wavefront of
+// CB-byte elements) hit distinct bank slots, slot = (col_idx<8> * CT + c)
+// mod (128/CB).  The first pass's reads and the last pass's writes are the
+// prologue's and epilogue's registers.
+namespace col_check {
+constexpr bool group_ok(int N, int CT, int CB, int R, int NS, bool write) {
+  const int lanes = 128 / CB, NB = N / R, TASKS = CT * NB;
+  for (int t0 = 0; t0 + lanes <= TASKS; t0 += lanes)
+    for (int r = 0; r < R; ++r) {
+      bool hit[16] = {};
+      for (int t = t0; t < t0 + lanes; ++t) {
+        const int c = t % CT, j = t / CT, k = j & (NS - 1);
+        const int i = write ? (NS == 1 ? j * R + r : (j - k) * R + k + r * NS) : j + r * NB;
+        const int slot = (col_idx<8>(i) * CT + c) % lanes;
+        if (hit[slot]) return false;
+        hit[slot] = true;
+      }
+    }
+  return true;
+}
+constexpr bool conflict_free(int N, int CT, int CB) {
+  for (int ns = 1; ns < N; ns *= radix_of(N / ns)) {
+    const int R = radix_of(N / ns);
+    const bool first = ns == 1, last = ns * R == N;
+    if (!first && !group_ok(N, CT, CB, R, ns, false)) return false;
+    if (!last && !group_ok(N, CT, CB, R, ns, true)) return false;
+  }
+  return true;
+}
+// the tiles of Tiles<T, N>::CT: FP32 (CB 8) 2048/N capped at 8, FP64 (CB 16)
+// 1024/N capped at 8, at least 1
+constexpr int ct_of(int N, int CB) {
+  const int c = (16384 / CB) / N;
+  return c >= 8 ? 8 : (c >= 1 ? c : 1);
+}
+// (N = 16 and 32, whose first passes are radix 2 and 4, keep a two-way
+// conflict in their first pass's writes under either padding)
+constexpr bool all_ok() {
+  for (int N = 64; N <= 1024; N *= 2)
+    for (int CB = 8; CB <= 16; CB *= 2)
+      if (!conflict_free(N, ct_of(N, CB), CB)) return false;
+  return true;
+}
+static_assert(all_ok(), "the pad-8 column layout leaves a bank conflict");
+}  // namespace col_check
 
 // number of passes and the stride NS of the last one
 template <int N> struct LastNS {
@@ -44,9 +106,9 @@ __device__ __forceinline__ void col_cp_wait() {
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
 
-template <typename T, int N, int R, int NS, bool FWD, int NF, int CT, int NT, bool LASTMID>
+template <typename T, int N, int R, int NS, bool FWD, int NF, int CT, int NT, bool LASTMID, int CP>
 __device__ __forceinline__ void col_mid_pass(cplx<T>* __restrict__ sm, const cplx<T>* __restrict__ tw) {
-  constexpr int FS = ColLay<N, CT>::FS;
+  constexpr int FS = ColLay<N, CT, CP>::FS;
   constexpr int NB = N / R;
   constexpr int TASKS = CT * NB;
   constexpr int PER = (TASKS + NT - 1) / NT;
@@ -60,7 +122,7 @@ __device__ __forceinline__ void col_mid_pass(cplx<T>* __restrict__ sm, const cpl
 #pragma unroll
       for (int f = 0; f < NF; ++f)
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[p][f][r] = sm[f * FS + pad_idx(j + r * NB) * CT + c];
+        for (int r = 0; r < R; ++r) v[p][f][r] = sm[f * FS + col_idx<CP>(j + r * NB) * CT + c];
     }
   }
   __syncthreads();
@@ -85,25 +147,25 @@ __device__ __forceinline__ void col_mid_pass(cplx<T>* __restrict__ sm, const cpl
 #pragma unroll
       for (int f = 0; f < NF; ++f)
 #pragma unroll
-        for (int r = 0; r < R; ++r) sm[f * FS + pad_idx(base + r * NS) * CT + c] = v[p][f][r];
+        for (int r = 0; r < R; ++r) sm[f * FS + col_idx<CP>(base + r * NS) * CT + c] = v[p][f][r];
     }
   }
   if constexpr (LASTMID) col_cp_wait();
   __syncthreads();
 }
 
-template <typename T, int N, int NS, bool FWD, int NF, int CT, int NT>
+template <typename T, int N, int NS, bool FWD, int NF, int CT, int NT, int CP>
 __device__ __forceinline__ void col_mid_passes(cplx<T>* sm, const cplx<T>* tw) {
   constexpr int R = radix_of(N / NS);
   if constexpr (NS < LastNS<N>::value) {
-    col_mid_pass<T, N, R, NS, FWD, NF, CT, NT, (NS * R >= LastNS<N>::value)>(sm, tw);
-    col_mid_passes<T, N, NS * R, FWD, NF, CT, NT>(sm, tw);
+    col_mid_pass<T, N, R, NS, FWD, NF, CT, NT, (NS * R >= LastNS<N>::value), CP>(sm, tw);
+    col_mid_passes<T, N, NS * R, FWD, NF, CT, NT, CP>(sm, tw);
   }
 }
 
-template <typename T, int N, bool FWD, int NF, int CT, int NT, class Pro, class Epi>
+template <typename T, int N, bool FWD, int NF, int CT, int NT, int CP = 16, class Pro, class Epi>
 __device__ __forceinline__ void col_fft(cplx<T>* __restrict__ sm, const cplx<T>* __restrict__ tw, Pro pro, Epi epi) {
-  constexpr int FS = ColLay<N, CT>::FS;
+  constexpr int FS = ColLay<N, CT, CP>::FS;
   const int tid = threadIdx.x;
   // pass 0 (NS = 1): inputs from the prologue
   {
@@ -122,14 +184,14 @@ __device__ __forceinline__ void col_fft(cplx<T>* __restrict__ sm, const cplx<T>*
         for (int f = 0; f < NF; ++f) {
           dftR<T, R, FWD>(v[f]);
 #pragma unroll
-          for (int r = 0; r < R; ++r) sm[f * FS + pad_idx(j * R + r) * CT + c] = v[f][r];
+          for (int r = 0; r < R; ++r) sm[f * FS + col_idx<CP>(j * R + r) * CT + c] = v[f][r];
         }
       }
     }
   }
   if constexpr (radix_of(N) >= LastNS<N>::value) col_cp_wait();   // no middle pass
   __syncthreads();
-  col_mid_passes<T, N, radix_of(N), FWD, NF, CT, NT>(sm, tw);
+  col_mid_passes<T, N, radix_of(N), FWD, NF, CT, NT, CP>(sm, tw);
   // last pass: outputs to the epilogue
   {
     constexpr int NS = LastNS<N>::value;
@@ -147,7 +209,7 @@ __device__ __forceinline__ void col_fft(cplx<T>* __restrict__ sm, const cplx<T>*
 #pragma unroll
         for (int f = 0; f < NF; ++f) {
 #pragma unroll
-          for (int r = 0; r < R; ++r) v[f][r] = sm[f * FS + pad_idx(j + r * NB) * CT + c];
+          for (int r = 0; r < R; ++r) v[f][r] = sm[f * FS + col_idx<CP>(j + r * NB) * CT + c];
 #pragma unroll
           for (int r = 1; r < R; ++r) {
             cplx<T> w = tw[off + (r - 1) * NS + j];

@@ -137,7 +137,12 @@ template <typename T, int N> struct Tiles {
   static constexpr int SM6 = (N + 6 * CT * LD) * CB;
   static constexpr int mb0 = 233472 / (SM6 + 1024);
   static constexpr int MINB = mb0 >= 4 ? 4 : (mb0 >= 1 ? mb0 : 1);
-  static constexpr int FSC = PadLD<N>::value * CT;   // interleaved column tile (colfft.cuh)
+  static constexpr int FSC = ColLay<N, CT>::FS;      // interleaved column tile (colfft.cuh)
+  // k_col_inv's column layout: one pad every 8 elements (no bank conflict)
+  // at N >= 512 (0.325 -> 0.300 ms at 512^2 x 256); the pad-16 layout at
+  // smaller N (the C3 ensemble step was 1 % slower with pad 8 there)
+  static constexpr int CIP = N >= 512 ? 8 : 16;
+  static constexpr int FSCI = ColLay<N, CT, CIP>::FS;
   static constexpr int RRT = kRowRT > 0 ? kRowRT : RT;   // rows per CTA of the forward row kernels
   static constexpr int RMINB = imin(CB == 8 ? kRowMinB : 2, smem_ctas((N + 4 * RRT * LD) * CB));
   // rows per k_row_qw CTA: one (row, butterfly) task per thread where its
@@ -186,7 +191,7 @@ template <typename T, int N> struct Tiles {
   // per SM scaled up by CSCALE so that the threads per SM stay the same
   static constexpr int CNT = imin(256, imax(32, CT * (N / radix_of(N))));
   static constexpr int CSCALE = 256 / CNT;
-  static constexpr int CIMINB = imin((CB == 8 ? kColInvMinB : 2) * CSCALE, smem_ctas_cap((N + 3 * FSC) * CB, 32));
+  static constexpr int CIMINB = imin((CB == 8 ? kColInvMinB : 2) * CSCALE, smem_ctas_cap((N + 3 * FSCI) * CB, 32));
   static constexpr int CQMINB = imin((CB == 8 ? kColQwMinB : 2) * CSCALE, smem_ctas_cap((N + 2 * FSC) * CB, 32));
 };
 constexpr int kColThreads = 256;   // the adjoint's column kernels
@@ -237,7 +242,7 @@ k_col_inv(Geom g, int zbase, const cplx<T>* __restrict__ psi, const cplx<T>* __r
   constexpr int R0 = radix_of(N), NB0 = N / R0, NSL = LastNS<N>::value, RL = N / NSL;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* sm = tw + N;                        // [3][FS]
+  cplx<T>* sm = tw + N;                        // [3][FS] (column layout Tiles::CIP)
   const int zb = blockIdx.y, z = zbase + zb;
   const int kx0 = blockIdx.x * CT;
   load_tw<T, N>(tw, twg, NT);
@@ -323,20 +328,20 @@ k_col_inv(Geom g, int zbase, const cplx<T>* __restrict__ psi, const cplx<T>* __r
         for (int r = 0; r < RL; ++r) Qb[q_off(zb, f, j + r * NSL, N, g.KXP) + kx0 + c] = v[f][r];
     };
     if (bmode != 2) {
-      col_fft<T, N, false, 2, CT, NT>(sm, tw, pro2(0), epi2(0));
+      col_fft<T, N, false, 2, CT, NT, Tiles<T, N>::CIP>(sm, tw, pro2(0), epi2(0));
       __syncthreads();
-      col_fft<T, N, false, 2, CT, NT>(sm, tw, pro2(1), epi2(2));
+      col_fft<T, N, false, 2, CT, NT, Tiles<T, N>::CIP>(sm, tw, pro2(1), epi2(2));
     }
     if (bmode == 0) {
       __syncthreads();
-      col_fft<T, N, false, 2, CT, NT>(sm, tw, pro2(2), epi2(4));
+      col_fft<T, N, false, 2, CT, NT, Tiles<T, N>::CIP>(sm, tw, pro2(2), epi2(4));
     } else if (bmode == 2) {
-      col_fft<T, N, false, 2, CT, NT>(sm, tw, pro2(2), epiq);
+      col_fft<T, N, false, 2, CT, NT, Tiles<T, N>::CIP>(sm, tw, pro2(2), epiq);
     }
   } else {
-    col_fft<T, N, false, 3, CT, NT>(sm, tw, pro_psi, epi(0));
+    col_fft<T, N, false, 3, CT, NT, Tiles<T, N>::CIP>(sm, tw, pro_psi, epi(0));
     __syncthreads();
-    col_fft<T, N, false, 3, CT, NT>(sm, tw, pro_raw, epi(3));
+    col_fft<T, N, false, 3, CT, NT, Tiles<T, N>::CIP>(sm, tw, pro_raw, epi(3));
   }
 }
 
