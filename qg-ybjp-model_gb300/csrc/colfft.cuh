@@ -31,11 +31,19 @@
 
 namespace qg {
 
-// CP: pad slots every CP elements (8 or 16)
-template <int CP = 16> __host__ __device__ __forceinline__ constexpr int col_idx(int i) {
-  return CP == 8 ? i + (i >> 3) : pad_idx(i);
+// CP: one pad slot every CP elements (8 or 16), or CP = 0: no padding, the
+// XOR placement i ^ ((i / 8) mod Q) with Q = (128 / element bytes) / CT,
+// which makes the same accesses conflict free (checked below)
+template <int CP = 16, int Q = 1> __host__ __device__ __forceinline__ constexpr int col_idx(int i) {
+  return CP == 0 ? (i ^ ((i >> 3) & (Q - 1))) : (CP == 8 ? i + (i >> 3) : pad_idx(i));
 }
-template <int N, int CP = 16> struct ColPad { static constexpr int value = CP == 8 ? N + (N >> 3) : PadLD<N>::value; };
+template <int N, int CP = 16> struct ColPad {
+  static constexpr int value = CP == 0 ? N : (CP == 8 ? N + (N >> 3) : PadLD<N>::value);
+};
+template <typename T, int CT> struct ColQ {
+  static constexpr int v = (128 / (int)sizeof(cplx<T>)) / CT;
+  static constexpr int value = v >= 1 ? v : 1;
+};
 template <int N, int CT, int CP = 16> struct ColLay {
   static constexpr int FS = ColPad<N, CP>::value * CT;
 };
@@ -48,7 +56,8 @@ template <int N, int CT, int CP = 16> struct ColLay {
 // mod (128/CB).  The first pass's reads and the last pass's writes are the
 // prologue's and epilogue's registers.
 namespace col_check {
-constexpr bool group_ok(int N, int CT, int CB, int R, int NS, bool write) {
+constexpr int cidx(int cp, int q, int i) { return cp == 0 ? (i ^ ((i >> 3) & (q - 1))) : (cp == 8 ? i + (i >> 3) : pad_idx(i)); }
+constexpr bool group_ok(int N, int CT, int CB, int R, int NS, bool write, int cp) {
   const int lanes = 128 / CB, NB = N / R, TASKS = CT * NB;
   for (int t0 = 0; t0 + lanes <= TASKS; t0 += lanes)
     for (int r = 0; r < R; ++r) {
@@ -56,19 +65,30 @@ constexpr bool group_ok(int N, int CT, int CB, int R, int NS, bool write) {
       for (int t = t0; t < t0 + lanes; ++t) {
         const int c = t % CT, j = t / CT, k = j & (NS - 1);
         const int i = write ? (NS == 1 ? j * R + r : (j - k) * R + k + r * NS) : j + r * NB;
-        const int slot = (col_idx<8>(i) * CT + c) % lanes;
+        const int q = lanes / CT >= 1 ? lanes / CT : 1;
+        const int slot = (cidx(cp, q, i) * CT + c) % lanes;
         if (hit[slot]) return false;
         hit[slot] = true;
       }
     }
   return true;
 }
-constexpr bool conflict_free(int N, int CT, int CB) {
+constexpr bool conflict_free(int N, int CT, int CB, int cp) {
   for (int ns = 1; ns < N; ns *= radix_of(N / ns)) {
     const int R = radix_of(N / ns);
     const bool first = ns == 1, last = ns * R == N;
-    if (!first && !group_ok(N, CT, CB, R, ns, false)) return false;
-    if (!last && !group_ok(N, CT, CB, R, ns, true)) return false;
+    if (!first && !group_ok(N, CT, CB, R, ns, false, cp)) return false;
+    if (!last && !group_ok(N, CT, CB, R, ns, true, cp)) return false;
+  }
+  return true;
+}
+constexpr bool permutes(int N, int CT, int CB) {
+  bool seen[1024] = {};
+  const int q = (128 / CB) / CT >= 1 ? (128 / CB) / CT : 1;
+  for (int i = 0; i < N; ++i) {
+    const int p = cidx(0, q, i);
+    if (p < 0 || p >= N || seen[p]) return false;
+    seen[p] = true;
   }
   return true;
 }
@@ -83,10 +103,12 @@ constexpr int ct_of(int N, int CB) {
 constexpr bool all_ok() {
   for (int N = 64; N <= 1024; N *= 2)
     for (int CB = 8; CB <= 16; CB *= 2)
-      if (!conflict_free(N, ct_of(N, CB), CB)) return false;
+      if (!conflict_free(N, ct_of(N, CB), CB, 8) || !conflict_free(N, ct_of(N, CB), CB, 0) ||
+          !permutes(N, ct_of(N, CB), CB))
+        return false;
   return true;
 }
-static_assert(all_ok(), "the pad-8 column layout leaves a bank conflict");
+static_assert(all_ok(), "a pad-8 or XOR column layout leaves a bank conflict");
 }  // namespace col_check
 
 // number of passes and the stride NS of the last one
@@ -122,7 +144,7 @@ __device__ __forceinline__ void col_mid_pass(cplx<T>* __restrict__ sm, const cpl
 #pragma unroll
       for (int f = 0; f < NF; ++f)
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[p][f][r] = sm[f * FS + col_idx<CP>(j + r * NB) * CT + c];
+        for (int r = 0; r < R; ++r) v[p][f][r] = sm[f * FS + col_idx<CP, ColQ<T, CT>::value>(j + r * NB) * CT + c];
     }
   }
   __syncthreads();
@@ -147,7 +169,7 @@ __device__ __forceinline__ void col_mid_pass(cplx<T>* __restrict__ sm, const cpl
 #pragma unroll
       for (int f = 0; f < NF; ++f)
 #pragma unroll
-        for (int r = 0; r < R; ++r) sm[f * FS + col_idx<CP>(base + r * NS) * CT + c] = v[p][f][r];
+        for (int r = 0; r < R; ++r) sm[f * FS + col_idx<CP, ColQ<T, CT>::value>(base + r * NS) * CT + c] = v[p][f][r];
     }
   }
   if constexpr (LASTMID) col_cp_wait();
@@ -184,7 +206,7 @@ __device__ __forceinline__ void col_fft(cplx<T>* __restrict__ sm, const cplx<T>*
         for (int f = 0; f < NF; ++f) {
           dftR<T, R, FWD>(v[f]);
 #pragma unroll
-          for (int r = 0; r < R; ++r) sm[f * FS + col_idx<CP>(j * R + r) * CT + c] = v[f][r];
+          for (int r = 0; r < R; ++r) sm[f * FS + col_idx<CP, ColQ<T, CT>::value>(j * R + r) * CT + c] = v[f][r];
         }
       }
     }
@@ -209,7 +231,7 @@ __device__ __forceinline__ void col_fft(cplx<T>* __restrict__ sm, const cplx<T>*
 #pragma unroll
         for (int f = 0; f < NF; ++f) {
 #pragma unroll
-          for (int r = 0; r < R; ++r) v[f][r] = sm[f * FS + col_idx<CP>(j + r * NB) * CT + c];
+          for (int r = 0; r < R; ++r) v[f][r] = sm[f * FS + col_idx<CP, ColQ<T, CT>::value>(j + r * NB) * CT + c];
 #pragma unroll
           for (int r = 1; r < R; ++r) {
             cplx<T> w = tw[off + (r - 1) * NS + j];

@@ -893,7 +893,7 @@ class Engine : public EngineBase {
                                                           sm_rq<NN>(g.KXP)));
       occ_rm = std::max(occ_rm, 1);
       occ_rq = std::max(occ_rq, 1);
-      QG_CK(cudaFuncSetAttribute(k_col_qw<T, NN>, (cudaFuncAttribute)mx, (int)sm_ci<NN>(2)));
+      QG_CK(cudaFuncSetAttribute(k_col_qw<T, NN>, (cudaFuncAttribute)mx, (int)sm_ci<NN, Tiles<T, NN>::CQP>(2)));
       // per-function attribute shared by every handle: set it for the deepest supported column
       QG_CK(cudaFuncSetAttribute(k_solve<T>, (cudaFuncAttribute)mx, (int)solve_smem(kMaxN3)));
       QG_CK(cudaFuncSetAttribute(k_dcol_inv<T, NN>, (cudaFuncAttribute)mx, (int)sm_colinv()));
@@ -1039,7 +1039,7 @@ class Engine : public EngineBase {
           QG_LAUNCHED();
           if (int rc0 = pend(bs)) return rc0;
           if (int rc0 = pbeg(QG_K_COL_QW, bs)) return rc0;
-          k_col_qw<T, NN><<<gc, Tiles<T, NN>::CNT, sm_ci<NN>(2), bs>>>(g, s, z0, F[F_Q], F[F_QSTAR], Sb, tw, nflag);
+          k_col_qw<T, NN><<<gc, Tiles<T, NN>::CNT, sm_ci<NN, Tiles<T, NN>::CQP>(2), bs>>>(g, s, z0, F[F_Q], F[F_QSTAR], Sb, tw, nflag);
           QG_LAUNCHED();
           if (int rc0 = pend(bs)) return rc0;
         }

@@ -138,11 +138,18 @@ template <typename T, int N> struct Tiles {
   static constexpr int mb0 = 233472 / (SM6 + 1024);
   static constexpr int MINB = mb0 >= 4 ? 4 : (mb0 >= 1 ? mb0 : 1);
   static constexpr int FSC = ColLay<N, CT>::FS;      // interleaved column tile (colfft.cuh)
-  // k_col_inv's column layout: one pad every 8 elements (no bank conflict)
-  // at N >= 512 (0.325 -> 0.300 ms at 512^2 x 256); the pad-16 layout at
-  // smaller N (the C3 ensemble step was 1 % slower with pad 8 there)
+  // column layouts of the three column kernels (colfft.cuh col_idx: 16 or 8
+  // = one pad every 16 or 8 elements, 0 = XOR placement), chosen by timing
+  // the 512^2 x 256 step and the C3 ensemble: k_col_inv pad 8 (0.325 ->
+  // 0.300 ms; XOR spills), k_col_update XOR (1.063 -> 1.048 ms; pad 8 moved
+  // it to the next shared-memory carve-out: 1.10 ms), k_col_qw pad 16 (XOR
+  // and pad 8 no faster); below N = 512 pad 16 (the ensemble 0.5-1 % slower
+  // with the others)
   static constexpr int CIP = N >= 512 ? 8 : 16;
+  static constexpr int CUP = N >= 512 ? 0 : 16;
+  static constexpr int CQP = 16;
   static constexpr int FSCI = ColLay<N, CT, CIP>::FS;
+  static constexpr int FSCQ = ColLay<N, CT, CQP>::FS;
   static constexpr int RRT = kRowRT > 0 ? kRowRT : RT;   // rows per CTA of the forward row kernels
   static constexpr int RMINB = imin(CB == 8 ? kRowMinB : 2, smem_ctas((N + 4 * RRT * LD) * CB));
   // rows per k_row_qw CTA: one (row, butterfly) task per thread where its
@@ -192,7 +199,7 @@ template <typename T, int N> struct Tiles {
   static constexpr int CNT = imin(256, imax(32, CT * (N / radix_of(N))));
   static constexpr int CSCALE = 256 / CNT;
   static constexpr int CIMINB = imin((CB == 8 ? kColInvMinB : 2) * CSCALE, smem_ctas_cap((N + 3 * FSCI) * CB, 32));
-  static constexpr int CQMINB = imin((CB == 8 ? kColQwMinB : 2) * CSCALE, smem_ctas_cap((N + 2 * FSC) * CB, 32));
+  static constexpr int CQMINB = imin((CB == 8 ? kColQwMinB : 2) * CSCALE, smem_ctas_cap((N + 2 * FSCQ) * CB, 32));
 };
 constexpr int kColThreads = 256;   // the adjoint's column kernels
 constexpr int kThreadsB = 256;     // row kernels
@@ -603,8 +610,8 @@ template <typename T, int N> struct UpdLay {
   static constexpr int KYM = 2 * ((N + 2) / 3) + 1;     // >= KY for this n
   static constexpr int FE = CT * KYM;                   // entries per staged field
   // the four q^w inverse transforms reuse the transform and staging regions
-  static constexpr int PAD = 4 * ColLay<N, CT>::FS > 2 * ColLay<N, CT>::FS + 3 * FE
-                                 ? 4 * ColLay<N, CT>::FS - 2 * ColLay<N, CT>::FS - 3 * FE : 0;
+  static constexpr int PAD = 4 * ColLay<N, CT, Tiles<T, N>::CUP>::FS > 2 * ColLay<N, CT, Tiles<T, N>::CUP>::FS + 3 * FE
+                                 ? 4 * ColLay<N, CT, Tiles<T, N>::CUP>::FS - 2 * ColLay<N, CT, Tiles<T, N>::CUP>::FS - 3 * FE : 0;
   // lean (FP32): B^{n+1} re-read from global memory for the q^w transforms
   // (two passes of two) instead of kept in shared memory
   static constexpr bool LEAN = kUpdLean && sizeof(T) == 4;
@@ -613,8 +620,8 @@ template <typename T, int N> struct UpdLay {
   // (kUpdTablesSmem) or read from global memory in the epilogue
   static constexpr bool GTAB = LEAN && !kUpdTablesSmem;
   static constexpr size_t bytes() {
-    return LEAN ? (size_t)(N + 2 * ColLay<N, CT>::FS + 3 * FE) * sizeof(cplx<T>) + (GTAB ? 0 : (size_t)2 * FE * sizeof(T))
-                : (size_t)(N + 2 * ColLay<N, CT>::FS + 5 * FE + PAD) * sizeof(cplx<T>) + (size_t)2 * FE * sizeof(T);
+    return LEAN ? (size_t)(N + 2 * ColLay<N, CT, Tiles<T, N>::CUP>::FS + 3 * FE) * sizeof(cplx<T>) + (GTAB ? 0 : (size_t)2 * FE * sizeof(T))
+                : (size_t)(N + 2 * ColLay<N, CT, Tiles<T, N>::CUP>::FS + 5 * FE + PAD) * sizeof(cplx<T>) + (size_t)2 * FE * sizeof(T);
   }
   // CTAs per SM: scaled with the column CTAs' size (Tiles::CSCALE)
   static constexpr int MINB = imin(MINB0 * Tiles<T, N>::CSCALE, smem_ctas_cap((int)bytes(), 32));
@@ -647,7 +654,7 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* sm = tw + N;                          // [2][FS]
-  cplx<T>* stg = sm + 2 * ColLay<N, CT>::FS;     // [3][FE]: x, x_old, third (dq / AI / AR)
+  cplx<T>* stg = sm + 2 * ColLay<N, CT, Tiles<T, N>::CUP>::FS;   // [3][FE]: x, x_old, third (dq / AI / AR)
   cplx<T>* bnew = stg + 3 * FE + L::PAD;         // [2][FE]: BR, BI at n+1 (not LEAN)
   // [2][FE]: e1, e2 or e1w, e2w (not GTAB)
   T* tab = reinterpret_cast<T*>(L::LEAN ? stg + 3 * FE : bnew + 2 * FE);
@@ -797,13 +804,13 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
     };
   };
   stage(0);
-  col_fft<T, N, true, 2, CT, NT>(sm, tw, pro_planes(0), epi_update(0));
+  col_fft<T, N, true, 2, CT, NT, Tiles<T, N>::CUP>(sm, tw, pro_planes(0), epi_update(0));
   __syncthreads();
   stage(1);
-  col_fft<T, N, true, 2, CT, NT>(sm, tw, pro_planes(2), epi_update(1));
+  col_fft<T, N, true, 2, CT, NT, Tiles<T, N>::CUP>(sm, tw, pro_planes(2), epi_update(1));
   __syncthreads();
   stage(2);
-  col_fft<T, N, true, 2, CT, NT>(sm, tw, pro_planes(4), epi_update(2));
+  col_fft<T, N, true, 2, CT, NT, Tiles<T, N>::CUP>(sm, tw, pro_planes(4), epi_update(2));
   if (!qw_prep) return;
   __syncthreads();
   // y-inverse FFTs of B and i ky B at n+1 (compute_qw, derivatives.f90:929-957)
@@ -849,12 +856,12 @@ k_col_update(Geom g, StepParams sp, int zbase, StateP<T> st, const T* __restrict
   };
   if constexpr (sizeof(T) == 4 && !L::LEAN) {
     using NF4 = std::integral_constant<int, 4>;
-    col_fft<T, N, false, 4, CT, NT>(sm, tw, pro_B(0, NF4{}), epi_store(0, NF4{}));
+    col_fft<T, N, false, 4, CT, NT, Tiles<T, N>::CUP>(sm, tw, pro_B(0, NF4{}), epi_store(0, NF4{}));
   } else {
     using NF2 = std::integral_constant<int, 2>;
-    col_fft<T, N, false, 2, CT, NT>(sm, tw, pro_B(0, NF2{}), epi_store(0, NF2{}));
+    col_fft<T, N, false, 2, CT, NT, Tiles<T, N>::CUP>(sm, tw, pro_B(0, NF2{}), epi_store(0, NF2{}));
     __syncthreads();
-    col_fft<T, N, false, 2, CT, NT>(sm, tw, pro_B(1, NF2{}), epi_store(2, NF2{}));
+    col_fft<T, N, false, 2, CT, NT, Tiles<T, N>::CUP>(sm, tw, pro_B(1, NF2{}), epi_store(2, NF2{}));
   }
 }
 
@@ -1092,7 +1099,7 @@ k_col_qw(Geom g, StepParams sp, int zbase, const cplx<T>* __restrict__ q, cplx<T
       qstar[m] = out;
     }
   };
-  col_fft<T, N, true, 2, CT, NT>(sm, tw, pro, epi);
+  col_fft<T, N, true, 2, CT, NT, Tiles<T, N>::CQP>(sm, tw, pro, epi);
   __syncthreads();
   if (threadIdx.x == 0 && s_bad) raise_wait_flag(nflag);
 }
