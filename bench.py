@@ -40,11 +40,11 @@ FALLBACK_HBM_GBS = 6800.0
 # levels whose scratch planes outgrow L2 as the 256-level batch's do).  The
 # roofline entry scales it by the levels per launch of the run.
 MEASURED_TRAFFIC_PER_LEVEL = {
-    ("col_inv", 512, "mixed"): 6.073e6,
-    ("row_main", 512, "mixed"): 8.501e6,
-    ("col_update", 512, "mixed"): 14.065e6,
-    ("row_qw", 512, "mixed"): 4.356e6,
-    ("col_qw", 512, "mixed"): 2.701e6,
+    ("col_inv", 512, "mixed"): 3.553e6,
+    ("row_main", 512, "mixed"): 8.495e6,
+    ("col_update", 512, "mixed"): 14.114e6,
+    ("row_qw", 512, "mixed"): 4.406e6,
+    ("col_qw", 512, "mixed"): 2.605e6,
 }
 
 
