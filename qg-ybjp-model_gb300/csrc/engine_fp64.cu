@@ -367,7 +367,7 @@ class AdjEngine final : public Engine<double> {
       const int zc = std::min(Zb, g.n3 - z0);
       QG_SWITCH_N(g.n, {
         const dim3 gc(g.KXP / Tiles<double, NN>::CT, zc), gr(g.n / Tiles<double, NN>::RT, zc);
-        k_col_inv<double, NN><<<gc, Tiles<double, NN>::CNT, sm_ci<NN, Tiles<double, NN>::CIP>(3), st>>>(g, z0, psi, q, BR, BI, S, tw, nullptr, 0);
+        k_col_inv<double, NN><<<gc, Tiles<double, NN>::CNT, sm_ci<NN, Tiles<double, NN>::CIP>(Tiles<double, NN>::CINF), st>>>(g, z0, psi, q, BR, BI, S, tw, nullptr, 0);
         QG_LAUNCHED();
         k_adj_col_inv<NN><<<gc, kColThreads, sm_col6<NN>(), st>>>(g, p, z0, L, e1, e2, e1w, e2w, SA, tw);
         QG_LAUNCHED();

@@ -884,7 +884,7 @@ class Engine : public EngineBase {
   int set_smem_attrs() {
     const int mx = cudaFuncAttributeMaxDynamicSharedMemorySize;
     QG_SWITCH_N(g.n, {
-      QG_CK(cudaFuncSetAttribute(k_col_inv<T, NN>, (cudaFuncAttribute)mx, (int)sm_ci<NN, Tiles<T, NN>::CIP>(3)));
+      QG_CK(cudaFuncSetAttribute(k_col_inv<T, NN>, (cudaFuncAttribute)mx, (int)sm_ci<NN, Tiles<T, NN>::CIP>(Tiles<T, NN>::CINF)));
       QG_CK(cudaFuncSetAttribute(k_row_main<T, NN>, (cudaFuncAttribute)mx, (int)sm_rm<NN>(kxp_max<NN>())));
       QG_CK(cudaFuncSetAttribute(k_col_update<T, NN>, (cudaFuncAttribute)mx, (int)UpdLay<T, NN>::bytes()));
       QG_CK(cudaFuncSetAttribute(k_row_qw<T, NN>, (cudaFuncAttribute)mx, (int)sm_rq<NN>(kxp_max<NN>())));
@@ -992,7 +992,7 @@ class Engine : public EngineBase {
             grm(g.n / Tiles<T, NN>::RTM, zc);
         if (int rc0 = pbeg(QG_K_COL_INV, bs)) return rc0;
         C* Qb = Qp ? Qp + (size_t)z0 * kNQ * g.n * g.KXP : nullptr;
-        k_col_inv<T, NN><<<gc, Tiles<T, NN>::CNT, sm_ci<NN, Tiles<T, NN>::CIP>(3), bs>>>(g, z0, F[F_PSI], F[F_Q], F[F_BR], F[F_BI], Sb, tw,
+        k_col_inv<T, NN><<<gc, Tiles<T, NN>::CNT, sm_ci<NN, Tiles<T, NN>::CIP>(Tiles<T, NN>::CINF), bs>>>(g, z0, F[F_PSI], F[F_Q], F[F_BR], F[F_BI], Sb, tw,
                                                                 Qb, Qb ? 1 : 0);
         QG_LAUNCHED();
         if (int rc0 = pend(bs)) return rc0;
@@ -1117,7 +1117,7 @@ class Engine : public EngineBase {
       const int zc = std::min(Zb, g.n3 - z0);
       QG_SWITCH_N(g.n, {
         const dim3 gc((g.K + Tiles<T, NN>::CT) / Tiles<T, NN>::CT, zc);
-        k_col_inv<T, NN><<<gc, Tiles<T, NN>::CNT, sm_ci<NN, Tiles<T, NN>::CIP>(3), st>>>(g, z0, F[F_PSI], F[F_Q], F[F_BR], F[F_BI], S, tw,
+        k_col_inv<T, NN><<<gc, Tiles<T, NN>::CNT, sm_ci<NN, Tiles<T, NN>::CIP>(Tiles<T, NN>::CINF), st>>>(g, z0, F[F_PSI], F[F_Q], F[F_BR], F[F_BI], S, tw,
                                                                 Qp + (size_t)z0 * kNQ * g.n * g.KXP, 2);
         QG_LAUNCHED();
       });

@@ -198,7 +198,9 @@ template <typename T, int N> struct Tiles {
   // per SM scaled up by CSCALE so that the threads per SM stay the same
   static constexpr int CNT = imin(256, imax(32, CT * (N / radix_of(N))));
   static constexpr int CSCALE = 256 / CNT;
-  static constexpr int CIMINB = imin((CB == 8 ? kColInvMinB : 2) * CSCALE, smem_ctas_cap((N + 3 * FSCI) * CB, 32));
+  // transforms in flight in k_col_inv: two per pass in FP32 (kColInvNF2), three in FP64
+  static constexpr int CINF = (kColInvNF2 && CB == 8) ? 2 : 3;
+  static constexpr int CIMINB = imin((CB == 8 ? kColInvMinB : 2) * CSCALE, smem_ctas_cap((N + CINF * FSCI) * CB, 32));
   static constexpr int CQMINB = imin((CB == 8 ? kColQwMinB : 2) * CSCALE, smem_ctas_cap((N + 2 * FSCQ) * CB, 32));
 };
 constexpr int kColThreads = 256;   // the adjoint's column kernels
@@ -249,7 +251,7 @@ k_col_inv(Geom g, int zbase, const cplx<T>* __restrict__ psi, const cplx<T>* __r
   constexpr int R0 = radix_of(N), NB0 = N / R0, NSL = LastNS<N>::value, RL = N / NSL;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* sm = tw + N;                        // [3][FS] (column layout Tiles::CIP)
+  cplx<T>* sm = tw + N;                        // [CINF][FS] (column layout Tiles::CIP)
   const int zb = blockIdx.y, z = zbase + zb;
   const int kx0 = blockIdx.x * CT;
   load_tw<T, N>(tw, twg, NT);
