@@ -758,9 +758,9 @@ def run_reference(args, world, rank, local):
     rc = workload(args)
     workers = os.cpu_count() or 1
     # calibrate the slab depth so that the whole run stays within ~2 minutes
-    # (on 8 levels: a 2-level slab runs from cache and overstates the rate
-    # of a deep one ~2.5x)
-    rate, _ = cpu_oracle_rate(rc, 8, 1, 0, workers)
+    # (on 32 levels: slabs of 2-8 levels run from the host caches and
+    # overstate the rate of a deep, memory-bound one ~2.5x)
+    rate, _ = cpu_oracle_rate(rc, min(32, rc.n3), 1, 0, workers)
     budget = float(args.reference_budget_s)
     per_step = budget / max(1, args.steps + args.warmup)
     nz = int(max(2, min(rc.n3, per_step * rate / (rc.n * rc.n))))
