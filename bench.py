@@ -160,15 +160,18 @@ def algorithmic_bytes(n: int, n3: int, zb: int, precision: str) -> dict:
     modes (the 2/3 disk, L=1) x s bytes, s = 8 (FP32 complex, mixed) or 16
     (FP64).  The step as a whole moves 22 field passes (reads of q, q_old, BR,
     BI, BR_old, BI_old, psi, AR, AI and writes of the seven phase-A results;
-    reads of q*, BR, BI and writes of psi, AR, AI in the solves); k_col_inv and
-    k_col_update each read q, BR and BI, so the kernels' passes add up to 25.
+    reads of q*, BR, BI and writes of psi, AR, AI in the solves); q is read
+    again by k_col_inv and k_col_qw, so the kernels' passes add up to 24 on
+    the mixed path, whose k_col_inv reads psi and q only (B's y-transforms are
+    kept from the previous step's update), and to 26 in FP64 (k_col_inv also
+    reads BR and BI).
     Kernels that touch only the (kx,y) scratch planes perform no field pass:
     those planes are intermediate traffic (see traffic_model)."""
     from qgybj.config import dealias_mask
     s = 8 if precision == "mixed" else 16
     fld = int(dealias_mask(n).sum()) * s      # one state field, one level
     return {
-        "col_inv": zb * 4 * fld,              # psi, q, BR, BI
+        "col_inv": zb * (2 if precision == "mixed" else 4) * fld,   # psi, q (and BR, BI in FP64)
         "row_main": 0,
         "col_update": zb * 14 * fld,          # 8 read (q, qo, BR, BI, BRo, BIo, AR, AI), 6 written
         "row_qw": 0,
@@ -191,7 +194,8 @@ def traffic_model(n: int, zb: int, precision: str) -> dict:
     fld = int(dealias_mask(n).sum()) * s
     pln = n * (kmax(n) + 1) * s
     return {
-        "col_inv": zb * (4 * fld + 6 * pln),
+        # mixed: psi, q -> u, v, zeta, q planes (B's planes kept); FP64: all six
+        "col_inv": zb * ((2 * fld + 4 * pln) if precision == "mixed" else (4 * fld + 6 * pln)),
         "row_main": zb * (6 * pln + 6 * pln),
         "col_update": zb * (6 * pln + 14 * fld + 4 * pln),
         "row_qw": zb * (4 * pln + 2 * pln),
