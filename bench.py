@@ -203,13 +203,15 @@ def traffic_model(n: int, zb: int, precision: str) -> dict:
     }
 
 
-def transform_flops(n: int, n3: int) -> dict:
+def transform_flops(n: int, n3: int, precision: str = "mixed") -> dict:
     """Floating-point operations of the transforms of one step as the kernels
     execute them: radix-8/4/2 Stockham passes (a radix-8 butterfly is 56 real
-    additions/multiplications, a twiddle 6), 18 column transforms per retained
-    kx and level and 11 complex row transforms (two real rows each) per y and
-    level, plus the FP64 column solves (6 recurrences of 3 operations per
-    level and column, an FMA counted as 2)."""
+    additions/multiplications, a twiddle 6), column transforms per retained
+    kx and level (16 on the mixed path, whose update keeps B's y-transforms
+    for the next step: k_col_inv 4, k_col_update 6 + 4, k_col_qw 2; 18 in
+    FP64, whose k_col_inv transforms B as well) and 11 complex row transforms
+    (two real rows each) per y and level, plus the FP64 column solves (6
+    recurrences of 3 operations per level and column, an FMA counted as 2)."""
     from qgybj.config import dealias_mask, kmax
     rad, rem = [], n
     while rem > 1:
@@ -222,7 +224,8 @@ def transform_flops(n: int, n3: int) -> dict:
         per_fft += (n // r) * (bfly[r] + (6 * (r - 1) if ns > 1 else 0))
         ns *= r
     K = kmax(n)
-    fft = (18 * (K + 1) + 11 * n) * per_fft * n3
+    ncol = 16 if precision == "mixed" else 18
+    fft = (ncol * (K + 1) + 11 * n) * per_fft * n3
     solve = 6 * n3 * int(dealias_mask(n).sum()) * 5
     return {"transforms": fft, "solve_fp64": solve, "per_complex_fft": per_fft}
 
@@ -413,7 +416,7 @@ def run_ours(args, world, rank, local):
         sim64.synchronize()
         ref = state_fields(sim64, params["Bu"])
         sim64.close()
-        fl = transform_flops(n, n3)
+        fl = transform_flops(n, n3, "fp64")
         peak64 = measured_fp64_peak(dev)
         fp64 = {"value": cells * k64 / (ms64 / 1e3), "ms_per_step": ms64 / k64, "steps": k64,
                 "flops_per_step": fl["transforms"] + fl["solve_fp64"],
@@ -442,7 +445,7 @@ def run_ours(args, world, rank, local):
         dom_ms = prof[dom][0] / prof[dom][1]
         achieved = ab[dom] / (dom_ms / 1e3) / 1e9
         step_ms = ms / args.steps
-        fl = transform_flops(n, n3)
+        fl = transform_flops(n, n3, precision)
         meas = MEASURED_TRAFFIC_PER_LEVEL.get((dom, n, precision))
         out = {
             "metric": "cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world,
