@@ -109,6 +109,57 @@ def test_error_status_text():
     assert qgybj.lib().qg_step(None, 0) == _lib.QG_ERR_ARG
 
 
+_BAD_CONFIGS = [
+    # (field, value, status, message fragment): qg_create validates on the
+    # host, before any device call
+    ("n2", 64, "QG_ERR_UNSUPPORTED", b"n1 must equal n2"),
+    ("n1", 48, "QG_ERR_UNSUPPORTED", b"power of two"),
+    ("n3", 1, "QG_ERR_ARG", b"n3 must be >= 2"),
+    ("n3", 2048, "QG_ERR_UNSUPPORTED", b"n3 must be <= 1024"),
+    ("precision", 7, "QG_ERR_ARG", b"bad precision"),
+    ("ybj_plus", 2, "QG_ERR_ARG", b"ybj_plus must be 0 or 1"),
+    ("a_ell_ut", None, "QG_ERR_ARG", b"a_ell_ut is required"),
+    ("dz", 0.0, "QG_ERR_ARG", b"must be positive"),
+    ("Ro", -1.0, "QG_ERR_ARG", b"must be positive"),
+    ("delt", float("nan"), "QG_ERR_NONFINITE", b"non-finite"),
+    ("nuh1", float("inf"), "QG_ERR_NONFINITE", b"non-finite"),
+    ("ilap2", 12, "QG_ERR_ARG", b"ilap out of range"),
+]
+
+
+@pytest.mark.parametrize("field,value,status,msg", _BAD_CONFIGS)
+def test_create_rejects_bad_configuration(field, value, status, msg):
+    """qg_create's configuration checks (csrc/capi.cu:validate_config): each
+    rule returns its status and message with no handle made."""
+    from qgybj.model import make_config
+    rc = scaled(CONFIGS["c0"], 32, 8)
+    ic = make_initial_condition(rc)
+    cfg, keep = make_config(model_parameters(rc, ic.delt), "fp64")
+    if field == "n1":
+        cfg.n1 = cfg.n2 = value
+    elif field == "a_ell_ut":
+        cfg.a_ell_ut = None
+    else:
+        setattr(cfg, field, value)
+    h = C.c_void_p()
+    assert qgybj.lib().qg_create(C.byref(cfg), C.byref(h)) == getattr(_lib, status)
+    assert not h.value
+    assert msg in qgybj.lib().qg_last_error(None)
+
+
+def test_create_rejects_non_finite_profile():
+    from qgybj.model import make_config
+    rc = scaled(CONFIGS["c1"], 32, 8)
+    ic = make_initial_condition(rc)
+    params = model_parameters(rc, ic.delt)
+    a = np.array(params["a_ell_ut"], dtype=np.float64)
+    a[3] = np.nan
+    params = dict(params, a_ell_ut=a)
+    cfg, keep = make_config(params, "mixed")
+    h = C.c_void_p()
+    assert qgybj.lib().qg_create(C.byref(cfg), C.byref(h)) == _lib.QG_ERR_NONFINITE
+
+
 @pytest.mark.parametrize("name", ["c0", "c1", "c4"])
 def test_initial_condition_properties(name):
     rc = CONFIGS[name] if name != "c1" else scaled(CONFIGS["c1"], 64, 32)
