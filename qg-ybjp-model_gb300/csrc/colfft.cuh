@@ -12,9 +12,10 @@
 // slot every 8 elements the first pass's writes (index 8j + r), the middle
 // passes' writes and every read fall on distinct bank slots for N >= 64
 // (checked at compile time below); one pad every 16 (pad_idx) leaves the
-// first pass's writes two-way conflicted but needs 6 % less shared memory,
-// which keeps k_col_update and k_col_qw within the 164 KB L1/shared
-// carve-out (with CP = 8 they moved to 196 KB and ran 4-6 % slower).
+// first pass's writes two-way conflicted but needs 6 % less shared memory:
+// with CP = 8, k_col_update and k_col_qw ran 4-6 % slower (likely because
+// their CTAs' shared memory then crosses the 164 KB L1/shared carve-out
+// step, leaving less L1).
 //
 // The passes are the Stockham radix-8/4/2 passes of fft_block.cuh (same
 // order of operations and twiddles, so results are bitwise those of fft_ip):

@@ -141,10 +141,10 @@ template <typename T, int N> struct Tiles {
   // column layouts of the three column kernels (colfft.cuh col_idx: 16 or 8
   // = one pad every 16 or 8 elements, 0 = XOR placement), chosen by timing
   // the 512^2 x 256 step and the C3 ensemble: k_col_inv pad 8 (0.325 ->
-  // 0.300 ms; XOR spills), k_col_update XOR (1.063 -> 1.048 ms; pad 8 moved
-  // it to the next shared-memory carve-out: 1.10 ms), k_col_qw pad 16 (XOR
-  // and pad 8 no faster); below N = 512 pad 16 (the ensemble 0.5-1 % slower
-  // with the others)
+  // 0.300 ms; XOR spills), k_col_update XOR (1.063 -> 1.048 ms; with pad 8,
+  // whose extra shared memory likely crosses a carve-out step: 1.10 ms),
+  // k_col_qw pad 16 (XOR and pad 8 no faster); below N = 512 pad 16 (the
+  // ensemble 0.5-1 % slower with the others)
   static constexpr int CIP = N >= 512 ? 8 : 16;
   static constexpr int CUP = N >= 512 ? 0 : 16;
   static constexpr int CQP = 16;
